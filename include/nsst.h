@@ -1,0 +1,165 @@
+/* nsst.h — C ABI of the GB300-native NSST engine (libnsst.so).
+ *
+ * Drop-in boundary for the 2-D nonsubsampled shearlet transform hot path of
+ * ShearCuda: decompose -> hard/soft threshold -> reconstruct.  Each entry point
+ * names the reference interface it replaces (paths relative to the ShearCuda
+ * tree).  All pointers passed as "device" are CUDA device pointers; `stream`
+ * is a cudaStream_t (NULL = legacy default stream).  Images are row-major
+ * float32, H rows x W columns, W fastest.  No call aborts the process: every
+ * call returns an nsst_status and nsst_last_error() describes the last
+ * failure on the calling thread.
+ *
+ * Coefficient layout (nsst_shear_trans / nsst_thresh / nsst_inverse_shear):
+ * nbands = 1 + sum_i 2^dcomp[i] planes of H x W floats; plane 0 is the
+ * lowpass image, then level 0 (coarsest) directions 0..2^dcomp[0]-1, level 1,
+ * ... — the MATLAB cell {lowpass, L x L x ndir per scale} of
+ * shear_trans_cuda.cpp:207-216 flattened level-major, direction-minor.
+ */
+#ifndef NSST_H
+#define NSST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nsst_status {
+  NSST_OK = 0,
+  NSST_ERR_INVALID_ARG = 1,      /* bad pointer, size or parameter */
+  NSST_ERR_UNSUPPORTED_SIZE = 2, /* H/W outside the supported transform lengths */
+  NSST_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+  NSST_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+  NSST_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out */
+  NSST_ERR_NUMERIC = 6           /* e.g. filter normalisation divides by zero */
+} nsst_status;
+
+enum { NSST_THRESH_HARD = 0, NSST_THRESH_SOFT = 1 };
+enum { NSST_PYRAMID_AUTO = 0, NSST_PYRAMID_DIRECT = 1, NSST_PYRAMID_SPECTRAL = 2 };
+enum { NSST_MAX_LEVELS = 8, NSST_MAX_BANDS = 1 + 8 * 64 };
+
+/* Transform configuration.  Mirrors the reference's shear_parameters struct
+ * (nsst_dec2.m:11-20: .dcomp, .dsize) plus the pyramid filter name
+ * (atrousfilters.m:26: '9-7' | 'maxflat' | 'pyr' | 'pyrexc'). */
+typedef struct nsst_config {
+  int nlevels;                  /* length of dcomp/dsize (<= NSST_MAX_LEVELS) */
+  int dcomp[NSST_MAX_LEVELS];   /* level i has 2^dcomp[i] directions, coarse -> fine */
+  int dsize[NSST_MAX_LEVELS];   /* local support of level i's shearing filter */
+  char lpfilt[16];              /* pyramid filter name, NUL-terminated */
+  int pyramid;                  /* NSST_PYRAMID_*: direct dilated conv or DCT-domain */
+} nsst_config;
+
+typedef struct nsst_plan nsst_plan;
+
+/* Last error message of the calling thread ("" if none). */
+const char* nsst_last_error(void);
+
+/* Library version string. */
+const char* nsst_version(void);
+
+/* Build a transform plan for H x W images: pyramid filters, Meyer shearing
+ * filters and their normalised spectra are constructed in FP64 on the host
+ * and uploaded as FP32; work buffers are allocated once here.
+ * Replaces prepare_shearing_filters_cuda (prepare_shearing_filters_cuda.cpp:61-249)
+ * and the standalone GpuShearDictionary::prepare (demo_denoise/shearcuda/gpusheardictionary.cpp:54-147). */
+nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out);
+
+/* Release a plan and all its device memory.
+ * Replaces clear_shearing_filters_cuda (clear_shearing_filters_cuda.cpp:51-96). */
+nsst_status nsst_plan_destroy(nsst_plan* plan);
+
+/* Number of coefficient planes (1 + sum 2^dcomp[i]). */
+int nsst_plan_num_bands(const nsst_plan* plan);
+
+/* Level of each band (0 = lowpass, i+1 = directional level i); out has nbands entries. */
+nsst_status nsst_plan_band_levels(const nsst_plan* plan, int* out);
+
+/* Device bytes held by the plan (filter spectra + work buffers). */
+size_t nsst_plan_device_bytes(const nsst_plan* plan);
+
+/* The pyramid filters (h0, h1, g0, g1 as FP64, row-major, sizes in F[4]);
+ * `taps` must hold F0^2+F1^2+F2^2+F3^2 doubles (pass NULL to query sizes).
+ * Mirrors atrousfilters.m:26-237. */
+nsst_status nsst_pyramid_filters(const char* name, int* F, double* taps);
+
+/* The Meyer shearing filters of one level in FP64 (2^level x n1 x n1).
+ * Mirrors shearing_filters_Myer.m:18-26. */
+nsst_status nsst_shearing_filters(int n1, int level, double* out);
+
+/* Host-only (no GPU needed): normalised spectra of one directional level,
+ * 2^dcomp Meyer filters of support dsize zero-padded top-left to H x W,
+ * FP64 [2^dcomp][H][W/2+1] interleaved (re, im).  Mirrors nsst_dec2.m:47-57. */
+nsst_status nsst_level_spectra(int dsize, int dcomp, int H, int W, double* out);
+
+/* The normalised spectra of the plan's directional level `level` as FP64,
+ * [ndir][H][W/2+1] interleaved (re, im).  Mirrors nsst_dec2.m:47-57. */
+nsst_status nsst_plan_level_spectra(const nsst_plan* plan, int level, double* out);
+
+/* À trous analysis: x (H x W, device) -> y ((nlevels+1) x H x W, device):
+ * plane 0 lowpass, planes 1..nlevels bandpass from coarse to fine.
+ * Replaces atrousdec (atrousdec.cpp:41-131; atrousdec.m:19-51). */
+nsst_status nsst_atrousdec(nsst_plan* plan, const float* x, float* y, void* stream);
+
+/* À trous synthesis: y ((nlevels+1) x H x W) -> x (H x W).
+ * Replaces atrousrec (atrousrec.cpp:42-132; atrousrec.m:18-41). */
+nsst_status nsst_atrousrec(nsst_plan* plan, const float* y, float* x, void* stream);
+
+/* Forward NSST: x (H x W, device) -> coeffs (nbands x H x W, device).
+ * Replaces shear_trans_cuda (shear_trans_cuda.cpp:56-287) and
+ * Shearcuda::shearTrans (demo_denoise/shearcuda/shearcuda.cpp:273-318). */
+nsst_status nsst_shear_trans(nsst_plan* plan, const float* x, float* coeffs, void* stream);
+
+/* Threshold coefficients in place: band b of level l uses
+ * t = K[l] * sigma * scalars[b]  (K has nlevels+1 entries, K[0] lowpass);
+ * hard keeps c where |c| > t, soft maps c to sign(c) max(|c| - t, 0).
+ * Replaces thresh_cuda (thresh_cuda.cpp:57-217) / softth_cuda
+ * (softth_cuda.cpp:49-112) / nsst_HT (nsst_HT.m:32-47) /
+ * Shearcuda::hardThreshold (shearcuda.cpp:320-358). */
+nsst_status nsst_thresh(nsst_plan* plan, float* coeffs, double sigma, const double* K, const double* scalars,
+                        int mode, void* stream);
+
+/* Inverse NSST: coeffs (nbands x H x W) -> x (H x W).
+ * Replaces inverse_shear_cuda (inverse_shear_cuda.cpp:57-286) and
+ * Shearcuda::inverseShear (shearcuda.cpp:360-396). */
+nsst_status nsst_inverse_shear(nsst_plan* plan, const float* coeffs, float* x, void* stream);
+
+/* Fused decompose -> threshold -> reconstruct (the coefficients are never
+ * materialised).  Same threshold rule as nsst_thresh; scalars may be NULL to
+ * use the plan's stored scalars (nsst_plan_set_scalars / nsst_compute_scalars).
+ * Replaces the shear_trans_cuda -> thresh -> inverse_shear_cuda sequence of
+ * shear_denoise_cuda.m:16-20 and demoImageDenoise mainwindow.cpp:221-234. */
+nsst_status nsst_denoise(nsst_plan* plan, const float* x, float* out, double sigma, const double* K,
+                         const double* scalars, int mode, void* stream);
+
+/* Store per-band noise scalars in the plan (nbands doubles). */
+nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
+
+/* Per-band noise scalars by the Monte-Carlo rule of nsst_scalars.m:28-45:
+ * a seeded N(0,1) image (generated in FP64 on the host) is transformed on the
+ * GPU and each band's MAD/0.6745 is taken on the host in FP64.  Writes nbands
+ * doubles to out and stores them in the plan.  Synchronous.
+ * Replaces nsst_scalars.m / Shearcuda::computeShearNorm (shearcuda.cpp:205-271). */
+nsst_status nsst_compute_scalars(nsst_plan* plan, uint64_t seed, double* out);
+
+/* Per-stage timing with CUDA events on the call's stream (no device syncs on
+ * the execute path).  When enabled, every execute call records one event per
+ * stage; nsst_timers_read waits for the last call's final event and returns
+ * the stage names ("\n"-separated into `names`, up to names_len bytes) and
+ * durations in milliseconds (up to max_stages).  Returns the stage count.
+ * Replaces GpuTimes / shear_timers (GpuTimes.h:25-78, shear_timers.cpp:40-85),
+ * which synchronised the device around every step. */
+nsst_status nsst_timers_enable(nsst_plan* plan, int enable);
+int nsst_timers_read(nsst_plan* plan, char* names, size_t names_len, float* ms, int max_stages);
+
+/* Number of kernels this library has launched since load (all plans, all threads). */
+uint64_t nsst_launch_count(void);
+
+/* Test hook: make the n-th device allocation from now fail with
+ * NSST_ERR_OUT_OF_MEMORY (n <= 0 disarms).  Host-side fault injection only. */
+void nsst_debug_fail_next_alloc(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSST_H */

@@ -1,0 +1,30 @@
+/* Minimal, project-written stand-in for MATLAB's matrix.h.
+ *
+ * Test infrastructure only: it lets the reference's MEX source
+ * shearlet_toolbox_1/atrousc.cpp compile unchanged as a plain shared
+ * library so that its convolution loop can serve as the oracle's
+ * ground truth.  Only the handful of calls that file makes are provided
+ * (atrousc.cpp:83-125).  Arrays are column-major like MATLAB's. */
+#ifndef NSST_ORACLE_MATRIX_H
+#define NSST_ORACLE_MATRIX_H
+#include <stddef.h>
+
+typedef size_t mwSize;
+typedef enum { mxUNKNOWN_CLASS = 0, mxDOUBLE_CLASS = 6, mxSINGLE_CLASS = 7 } mxClassID;
+typedef enum { mxREAL = 0, mxCOMPLEX = 1 } mxComplexity;
+
+typedef struct mxArray_tag {
+  mxClassID cls;
+  size_t m, n;
+  void* data;
+  int owns;
+} mxArray;
+
+size_t mxGetM(const mxArray* a);
+size_t mxGetN(const mxArray* a);
+bool mxIsDouble(const mxArray* a);
+bool mxIsClass(const mxArray* a, const char* name);
+double* mxGetPr(const mxArray* a);
+void* mxGetData(const mxArray* a);
+mxArray* mxCreateNumericArray(mwSize ndim, const mwSize* dims, mxClassID cls, mxComplexity cplx);
+#endif

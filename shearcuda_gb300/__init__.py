@@ -1,0 +1,7 @@
+"""GB300-native NSST (nonsubsampled shearlet transform) engine.
+
+The compute path is libnsst.so (hand-written sm_103a kernels behind the C ABI
+in include/nsst.h); this package is its Python host side.
+"""
+from ._lib import NsstError, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, PYRAMID_DIRECT, PYRAMID_SPECTRAL  # noqa: F401
+from .ops import *  # noqa: F401,F403

@@ -1,0 +1,85 @@
+"""ctypes binding of libnsst.so (the C ABI declared in include/nsst.h).
+
+The library is built in-tree by ``shearcuda_gb300.build``.  There is no
+fallback: if the shared library is missing or fails to load, importing the
+binding raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libnsst.so')
+
+NSST_OK = 0
+STATUS_NAMES = {0: 'NSST_OK', 1: 'NSST_ERR_INVALID_ARG', 2: 'NSST_ERR_UNSUPPORTED_SIZE',
+                3: 'NSST_ERR_OUT_OF_MEMORY', 4: 'NSST_ERR_CUDA', 5: 'NSST_ERR_TIMEOUT', 6: 'NSST_ERR_NUMERIC'}
+THRESH_HARD, THRESH_SOFT = 0, 1
+PYRAMID_AUTO, PYRAMID_DIRECT, PYRAMID_SPECTRAL = 0, 1, 2
+MAX_LEVELS = 8
+
+
+class NsstConfig(ctypes.Structure):
+    _fields_ = [('nlevels', ctypes.c_int), ('dcomp', ctypes.c_int * MAX_LEVELS),
+                ('dsize', ctypes.c_int * MAX_LEVELS), ('lpfilt', ctypes.c_char * 16),
+                ('pyramid', ctypes.c_int)]
+
+
+class NsstError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__('%s: %s' % (STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+_vp, _ci, _cd, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+# (name, restype, argtypes)
+SIGNATURES = [
+    ('nsst_last_error', ctypes.c_char_p, []),
+    ('nsst_version', ctypes.c_char_p, []),
+    ('nsst_plan_create', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, ctypes.POINTER(_vp)]),
+    ('nsst_plan_destroy', _ci, [_vp]),
+    ('nsst_plan_num_bands', _ci, [_vp]),
+    ('nsst_plan_band_levels', _ci, [_vp, _ip]),
+    ('nsst_plan_device_bytes', _sz, [_vp]),
+    ('nsst_pyramid_filters', _ci, [ctypes.c_char_p, _ip, _dp]),
+    ('nsst_shearing_filters', _ci, [_ci, _ci, _dp]),
+    ('nsst_level_spectra', _ci, [_ci, _ci, _ci, _ci, _dp]),
+    ('nsst_plan_level_spectra', _ci, [_vp, _ci, _dp]),
+    ('nsst_atrousdec', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_atrousrec', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_shear_trans', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_thresh', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _vp]),
+    ('nsst_inverse_shear', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_denoise', _ci, [_vp, _vp, _vp, _cd, _dp, _dp, _ci, _vp]),
+    ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
+    ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
+    ('nsst_timers_enable', _ci, [_vp, _ci]),
+    ('nsst_timers_read', _ci, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_float), _ci]),
+    ('nsst_launch_count', ctypes.c_uint64, []),
+    ('nsst_debug_fail_next_alloc', None, [_ci]),
+]
+
+_lib = None
+
+
+def lib():
+    """Load libnsst.so (once).  Raises OSError if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError('libnsst.so is not built (%s); run shearcuda_gb300.build.build()' % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != NSST_OK:
+        raise NsstError(status, lib().nsst_last_error().decode())
+    return status

@@ -1,0 +1,289 @@
+// Block-cooperative FP32 FFTs in shared memory, for the NSST directional stage.
+//
+// Layout convention used by every kernel: a CTA owns `NSEQ` sequences of
+// length N; element (sequence s, index i) lives at buf[i * LD + s] with
+// LD = NSEQ + 1 (one float2 of padding per index keeps the row-to-column
+// staging and the butterflies free of shared-memory bank conflicts).
+//
+// The transform is a Stockham auto-sort FFT: every pass reads its R inputs
+// at stride N/R, twiddles them, runs an R-point DFT in registers and writes
+// the outputs to their sorted positions, so the result is in natural order
+// with no bit-reversal pass.  Radices 2, 3, 4 and 8 cover every length of
+// the form 2^a * 3^b (b <= 1) that the pyramid sizes need.
+//
+// Twiddles come from a table tw[t] = exp(-2 pi i t / N) computed in FP64 on
+// the host and rounded once to FP32 (no on-device trigonometry).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nsst {
+
+struct cpx {
+  float x, y;
+};
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by -i (DIR<0) or +i (DIR>0)
+template <int DIR>
+__device__ __forceinline__ float2 mul_i(float2 a) {
+  return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+
+// ---------------------------------------------------------------------------
+// R-point DFTs in registers.  DIR = -1 forward (exp(-2 pi i ...)), +1 inverse.
+// ---------------------------------------------------------------------------
+template <int R, int DIR>
+struct Dft;
+
+template <int DIR>
+struct Dft<2, DIR> {
+  __device__ __forceinline__ static void run(float2* v) {
+    float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <int DIR>
+struct Dft<3, DIR> {
+  __device__ __forceinline__ static void run(float2* v) {
+    const float c = -0.5f;
+    const float s = 0.86602540378443864676f;  // sin(2 pi / 3)
+    float2 a0 = v[0], a1 = v[1], a2 = v[2];
+    float2 t = cadd(a1, a2);
+    float2 d = csub(a1, a2);
+    v[0] = cadd(a0, t);
+    float2 m = make_float2(a0.x + c * t.x, a0.y + c * t.y);
+    // forward: -i * s * d ; inverse: +i * s * d
+    float2 u = mul_i<DIR>(cscale(d, s));
+    v[1] = cadd(m, u);
+    v[2] = csub(m, u);
+  }
+};
+
+template <int DIR>
+struct Dft<4, DIR> {
+  __device__ __forceinline__ static void run(float2* v) {
+    float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    float2 s13 = cadd(v[1], v[3]), d13 = mul_i<DIR>(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+  }
+};
+
+template <int DIR>
+struct Dft<8, DIR> {
+  __device__ __forceinline__ static void run(float2* v) {
+    const float r = 0.70710678118654752440f;
+    float2 e[4] = {v[0], v[2], v[4], v[6]};
+    float2 o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<4, DIR>::run(e);
+    Dft<4, DIR>::run(o);
+    // twiddle o[k] by exp(DIR * 2 pi i k / 8)
+    float2 o1 = o[1], o2 = o[2], o3 = o[3];
+    // k=1: (1 + DIR*i) * r   (forward: (1 - i) r)
+    o[1] = DIR < 0 ? make_float2((o1.x + o1.y) * r, (o1.y - o1.x) * r)
+                   : make_float2((o1.x - o1.y) * r, (o1.y + o1.x) * r);
+    o[2] = mul_i<DIR>(o2);
+    // k=3: forward (-1 - i) r ; inverse (-1 + i) r
+    o[3] = DIR < 0 ? make_float2((-o3.x + o3.y) * r, (-o3.y - o3.x) * r)
+                   : make_float2((-o3.x - o3.y) * r, (-o3.y + o3.x) * r);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[k] = cadd(e[k], o[k]);
+      v[k + 4] = csub(e[k], o[k]);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Radix plans per length (product of radices == N).
+// ---------------------------------------------------------------------------
+template <int... Rs>
+struct RadixList {};
+
+template <int N>
+struct FftPlan;
+template <> struct FftPlan<64> { using type = RadixList<8, 8>; };
+template <> struct FftPlan<96> { using type = RadixList<3, 4, 8>; };
+template <> struct FftPlan<128> { using type = RadixList<8, 4, 4>; };
+template <> struct FftPlan<192> { using type = RadixList<3, 8, 8>; };
+template <> struct FftPlan<256> { using type = RadixList<4, 8, 8>; };
+template <> struct FftPlan<384> { using type = RadixList<3, 2, 8, 8>; };
+template <> struct FftPlan<512> { using type = RadixList<8, 8, 8>; };
+template <> struct FftPlan<768> { using type = RadixList<3, 4, 8, 8>; };
+template <> struct FftPlan<1024> { using type = RadixList<2, 8, 8, 8>; };
+template <> struct FftPlan<2048> { using type = RadixList<4, 8, 8, 8>; };
+
+// One Stockham pass of radix R over NSEQ sequences of length N, in place.
+// NS = product of the radices already applied.  All threads participate.
+template <int N, int NSEQ, int T, int R, int NS, int DIR>
+__device__ __forceinline__ void stockham_pass(float2* buf, const float2* __restrict__ tw) {
+  constexpr int LD = NSEQ + 1;
+  constexpr int NB = N / R;            // butterflies per sequence
+  constexpr int TOTAL = NB * NSEQ;     // butterflies in the CTA
+  constexpr int IPT = (TOTAL + T - 1) / T;
+  constexpr int STEP = N / (NS * R);   // twiddle index stride
+  float2 v[IPT][R];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      int s = w % NSEQ;
+      int j = w / NSEQ;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[it][r] = buf[(j + r * NB) * LD + s];
+      if (NS > 1) {
+        int k = j % NS;
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+          float2 t = __ldg(&tw[r * k * STEP]);
+          v[it][r] = DIR < 0 ? cmul(v[it][r], t) : cmulc(v[it][r], t);
+        }
+      }
+      Dft<R, DIR>::run(v[it]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      int s = w % NSEQ;
+      int j = w / NSEQ;
+      int k = j % NS;
+      int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) buf[(base + r * NS) * LD + s] = v[it][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <int N, int NSEQ, int T, int DIR, int NS>
+__device__ __forceinline__ void fft_passes(float2*, const float2* __restrict__, RadixList<>) {}
+
+template <int N, int NSEQ, int T, int DIR, int NS, int R, int... Rest>
+__device__ __forceinline__ void fft_passes(float2* buf, const float2* __restrict__ tw, RadixList<R, Rest...>) {
+  stockham_pass<N, NSEQ, T, R, NS, DIR>(buf, tw);
+  fft_passes<N, NSEQ, T, DIR, NS * R>(buf, tw, RadixList<Rest...>{});
+}
+
+// In-place FFT of NSEQ sequences of length N held in shared memory
+// (layout buf[i * (NSEQ+1) + s]).  Unnormalised in both directions.
+// Caller must __syncthreads() before (data staged) — this routine ends synced.
+template <int N, int NSEQ, int T, int DIR>
+__device__ __forceinline__ void block_fft(float2* buf, const float2* __restrict__ tw) {
+  fft_passes<N, NSEQ, T, DIR, 1>(buf, tw, typename FftPlan<N>::type{});
+}
+
+// ---------------------------------------------------------------------------
+// Real <-> packed-complex row transforms.
+//
+// A real row x[0..W) is viewed as W/2 complex z[n] = x[2n] + i x[2n+1].
+// Forward: after Z = FFT_{W/2}(z) the packed half spectrum is
+//   X[k] = E + w^k O,  X[W/2-k] = conj(E - w^k O),  E = (Z[k]+conj(Z[-k]))/2,
+//   O = (Z[k]-conj(Z[-k]))/(2i), w = exp(-2 pi i / W),
+// with slot 0 holding the two real bins (X[0], X[W/2]).
+// Inverse (before an unnormalised inverse FFT_{W/2}) forms
+//   Z[k] = E + iO,  Z[W/2-k] = conj(E - iO),  E = X[k]+conj(X[W/2-k]),
+//   O = w^-k (X[k]-conj(X[W/2-k])),
+// so that inverse(forward(x)) = W x.
+// twW[k] = exp(-2 pi i k / W), k < W/2.
+// ---------------------------------------------------------------------------
+template <int WH, int NSEQ, int T>
+__device__ __forceinline__ void r2c_post(float2* buf, const float2* __restrict__ twW) {
+  constexpr int LD = NSEQ + 1;
+  constexpr int PAIRS = WH / 2 + 1;  // k = 0 .. WH/2
+  constexpr int TOTAL = PAIRS * NSEQ;
+  constexpr int IPT = (TOTAL + T - 1) / T;
+  float2 a[IPT], b[IPT];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (w < TOTAL) {
+      int s = w % NSEQ, k = w / NSEQ;
+      float2 zk = buf[k * LD + s];
+      if (k == 0) {
+        a[it] = make_float2(zk.x + zk.y, zk.x - zk.y);
+      } else {
+        float2 zm = buf[(WH - k) * LD + s];
+        float2 zmc = cconj(zm);
+        float2 E = cscale(cadd(zk, zmc), 0.5f);
+        float2 d = cscale(csub(zk, zmc), 0.5f);
+        float2 O = make_float2(d.y, -d.x);  // d / i
+        float2 To = cmul(__ldg(&twW[k]), O);
+        a[it] = cadd(E, To);
+        b[it] = cconj(csub(E, To));
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (w < TOTAL) {
+      int s = w % NSEQ, k = w / NSEQ;
+      buf[k * LD + s] = a[it];
+      if (k != 0 && k != WH - k) buf[(WH - k) * LD + s] = b[it];
+    }
+  }
+  __syncthreads();
+}
+
+template <int WH, int NSEQ, int T>
+__device__ __forceinline__ void c2r_pre(float2* buf, const float2* __restrict__ twW) {
+  constexpr int LD = NSEQ + 1;
+  constexpr int PAIRS = WH / 2 + 1;
+  constexpr int TOTAL = PAIRS * NSEQ;
+  constexpr int IPT = (TOTAL + T - 1) / T;
+  float2 a[IPT], b[IPT];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (w < TOTAL) {
+      int s = w % NSEQ, k = w / NSEQ;
+      float2 xk = buf[k * LD + s];
+      if (k == 0) {
+        // X[0] = xk.x, X[W/2] = xk.y (both real)
+        a[it] = make_float2(xk.x + xk.y, xk.x - xk.y);
+      } else {
+        float2 xmc = cconj(buf[(WH - k) * LD + s]);
+        float2 E = cadd(xk, xmc);
+        float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));  // * w^-k
+        float2 iO = make_float2(-O.y, O.x);
+        a[it] = cadd(E, iO);
+        b[it] = cconj(csub(E, iO));
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    int w = tid + it * T;
+    if (w < TOTAL) {
+      int s = w % NSEQ, k = w / NSEQ;
+      buf[k * LD + s] = a[it];
+      if (k != 0 && k != WH - k) buf[(WH - k) * LD + s] = b[it];
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace nsst

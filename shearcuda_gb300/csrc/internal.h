@@ -1,0 +1,132 @@
+// Internal declarations shared by the NSST host library and its kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <complex>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nsst.h"
+
+namespace nsst {
+
+enum { THRESH_HARD = NSST_THRESH_HARD, THRESH_SOFT = NSST_THRESH_SOFT };
+
+// ---------------------------------------------------------------- job lists
+// Row/column jobs hold element offsets; the launch passes the base pointers.
+// That keeps a plan's job lists static in device memory while the caller's
+// buffers change from call to call.
+struct RowJob {
+  size_t src;    // offset (in float2) of the job's first row in the source
+  size_t dst;    // offset (in float2) in the destination
+  int th_index;  // index into the threshold array (threshold kernels)
+  int pad;
+};
+
+struct ColJob {
+  size_t src;    // offset (float2) of the packed H x W/2 source
+  size_t dst;    // offset (float2) of the destination
+  size_t spec;   // offset (float2) of the band spectrum (first band for synthesis)
+  size_t m0;     // offset (float2) of the column-0 side array
+  int nbands;    // synthesis: number of bands summed
+  int pad;
+};
+
+struct AtrousJob {
+  const float* xa;
+  const float* xb;  // optional second input (synthesis)
+  float* out;
+  int H, W;
+};
+constexpr int kMaxAtrousJobs = 64;
+struct AtrousJobs {  // passed by value
+  AtrousJob j[kMaxAtrousJobs];
+};
+
+template <int F>
+struct AtrousTaps {
+  float w[F * F];  // filter flipped in both axes, row-major
+  int cols[F];     // tap columns that hold a nonzero coefficient
+  int ncols;
+};
+template <>
+struct AtrousTaps<0> {
+  float w[1];
+  int cols[1];
+  int ncols;
+};
+
+template <int F>
+inline void fill_taps(AtrousTaps<F>& t, const float* hflip) {
+  t.ncols = 0;
+  for (int b = 0; b < F; b++) {
+    bool nz = false;
+    for (int a = 0; a < F; a++) {
+      t.w[a * F + b] = hflip[a * F + b];
+      nz |= hflip[a * F + b] != 0.0f;
+    }
+    if (nz) t.cols[t.ncols++] = b;
+  }
+}
+inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
+
+enum class RowOp { Fwd, Inv, Thresh };
+enum class ColOp { Fwd, Inv, Analysis, Synthesis };
+
+bool row_len_supported(int wh);
+bool col_len_supported(int h);
+int row_tile(int wh);
+int col_tile(int h);
+
+cudaError_t prepare_row_kernels(int wh);
+cudaError_t prepare_col_kernels(int h);
+cudaError_t prepare_atrous_kernels(int FA, int FB, int Mmax);
+cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int H, int W, const void* src_base,
+                        void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
+                        cudaStream_t st);
+cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int H, int W, const float2* src_base,
+                        float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
+                        cudaStream_t st);
+cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,
+                          int FB, const float* hb, cudaStream_t st);
+bool atrous_pair_supported(int FA, int FB);
+cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
+
+// ------------------------------------------------------- host-side FP64 math
+using cd = std::complex<double>;
+
+struct PyramidFilters {
+  std::string name;
+  int F[4];                       // sizes of h0, h1, g0, g1
+  std::vector<double> h[4];       // row-major F x F each: h0, h1, g0, g1
+};
+
+// atrousfilters.m tables; returns false for an unknown name.
+bool pyramid_filters(const std::string& name, PyramidFilters* out);
+
+// shearing_filters_Myer.m: (2^level) filters of n1 x n1, row-major, FP64.
+std::vector<double> shearing_filters_myer(int n1, int level);
+
+// In-place complex FFT of length n (n = 2^a 3^b), sign -1 forward / +1 inverse, unnormalised.
+void fft_inplace(cd* data, int n, int sign);
+
+// Spectra of one level: ndir filters zero-padded top-left to H x W, transformed,
+// then divided by d = sqrt(sum_k |W_k|^2) (nsst_dec2.m:47-57).  Output: only the
+// W/2+1 non-redundant columns, row-major [ndir][H][W/2+1].  Returns false if d
+// vanishes somewhere.
+bool level_spectra(const std::vector<double>& filters, int ndir, int n1, int H, int W, std::vector<cd>* out,
+                   int nthreads);
+
+std::vector<float2> twiddle_table(int n);            // exp(-2 pi i t / n), t < n
+std::vector<float2> half_twiddle_table(int n);       // exp(-2 pi i k / n), k < n/2
+
+// error reporting
+void set_error(const std::string& msg);
+
+// launch accounting (every kernel launch site calls this once per launch)
+void count_launch(int n = 1);
+
+}  // namespace nsst

@@ -1,0 +1,205 @@
+// À trous (dilated) pyramid filtering on sm_103a: the "direct" pyramid path.
+//
+// One call computes, for every output pixel,
+//     out[r][c] = sum_{a,b} hf[a][b] * xe[r - M*c0 + M*a][c - M*c0 + M*b]
+//               (+ the same with a second input / filter, summed),
+// where hf is the filter flipped in both axes, c0 = (F-1)/2 and xe is the
+// half-sample symmetric extension of x.  That is exactly one
+// atrousc(symext(x, upsample2df(h, log2 M), shift), h, M) call of the
+// reference (atrousc.cpp:43-73 with symext.m:18-31 and the shifts of
+// atrousdec.m:33,44 / atrousrec.m:33,40; for every level those shifts centre
+// the dilated filter, so the extension is a mirror with the edge sample
+// repeated).  The GPU reference materialises the extension (symExt kernel,
+// shear_cuda.cu:828-883) and a polyphase copy (atrousSubsample, :330-361)
+// before convolving (atrousConvolution, :462-585); here the mirror is applied
+// while the halo tile is staged into shared memory, so each launch reads its
+// input once and writes its output once.
+//
+// Tiling: a CTA owns 64 columns x 64 rows of one polyphase row class
+// (rows r = phase + M*t); with that split every tap row of the dilated filter
+// is a neighbouring tile row.  Each thread keeps 16 vertically adjacent
+// outputs in registers and streams one tap column at a time: 16+F-1 shared
+// loads feed 16*F FMAs.
+#include "internal.h"
+
+namespace nsst {
+
+constexpr int kAtTX = 64;   // tile width (columns)
+constexpr int kAtP = 16;    // outputs per thread (poly rows)
+constexpr int kAtTY = 4;    // thread rows
+constexpr int kAtRows = kAtP * kAtTY;  // poly rows per tile
+constexpr int kAtThreads = kAtTX * kAtTY;
+
+__device__ __forceinline__ int mirror_index(int i, int n) {
+  if (i < 0) i = -1 - i;
+  if (i >= n) i = 2 * n - 1 - i;
+  // Only outputs that are never stored can reach past one reflection.
+  return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+template <int F>
+__device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
+                                                  int prow0, int col0, const float* __restrict__ taps,
+                                                  const int* __restrict__ tapcols, int ntapcols, float* tile,
+                                                  float (&acc)[kAtP]) {
+  constexpr int C0 = (F - 1) / 2;
+  constexpr int TR = kAtRows + F - 1;
+  const int TC = kAtTX + M * (F - 1);
+  const int tid = threadIdx.x;
+  for (int e = tid; e < TR * TC; e += kAtThreads) {
+    int tr = e / TC, tc = e - tr * TC;
+    int r = mirror_index(phase + M * (prow0 + tr - C0), H);
+    int c = mirror_index(col0 - M * C0 + tc, W);
+    tile[e] = __ldg(&x[(size_t)r * W + c]);
+  }
+  __syncthreads();
+  const int tx = tid % kAtTX, ty = tid / kAtTX;
+  const float* base = tile + (ty * kAtP) * TC + tx;
+  for (int ib = 0; ib < ntapcols; ib++) {
+    const int b = tapcols[ib];
+    float col[kAtP + F - 1];
+#pragma unroll
+    for (int t = 0; t < kAtP + F - 1; t++) col[t] = base[t * TC + M * b];
+#pragma unroll
+    for (int a = 0; a < F; a++) {
+      const float w = taps[a * F + b];
+#pragma unroll
+      for (int p = 0; p < kAtP; p++) acc[p] = fmaf(w, col[p + a], acc[p]);
+    }
+  }
+  __syncthreads();
+}
+
+// out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/64), njobs)
+template <int FA, int FB>
+__global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
+                                                        const __grid_constant__ AtrousTaps<FA> ta,
+                                                        const __grid_constant__ AtrousTaps<FB> tb) {
+  extern __shared__ float at_smem[];
+  __shared__ float s_taps[(FA > FB ? FA * FA : FB * FB)];
+  __shared__ int s_cols[(FA > FB ? FA : FB)];
+  const AtrousJob& job = jobs.j[blockIdx.z];
+  const int H = job.H, W = job.W;
+  const int col0 = blockIdx.x * kAtTX;
+  const int phase = blockIdx.y % M;
+  const int prow0 = (blockIdx.y / M) * kAtRows;
+  const int nprow = (H - phase + M - 1) / M;  // poly rows of this phase
+  if (col0 >= W || prow0 >= nprow) return;
+  float acc[kAtP];
+#pragma unroll
+  for (int p = 0; p < kAtP; p++) acc[p] = 0.f;
+
+  for (int e = threadIdx.x; e < FA * FA; e += kAtThreads) s_taps[e] = ta.w[e];
+  for (int e = threadIdx.x; e < ta.ncols; e += kAtThreads) s_cols[e] = ta.cols[e];
+  __syncthreads();
+  atrous_accumulate<FA>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
+  if (FB > 0 && job.xb != nullptr) {
+    for (int e = threadIdx.x; e < FB * FB; e += kAtThreads) s_taps[e] = tb.w[e];
+    for (int e = threadIdx.x; e < tb.ncols; e += kAtThreads) s_cols[e] = tb.cols[e];
+    __syncthreads();
+    atrous_accumulate<(FB > 0 ? FB : 1)>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
+                                          at_smem, acc);
+  }
+  const int tx = threadIdx.x % kAtTX, ty = threadIdx.x / kAtTX;
+  const int c = col0 + tx;
+  if (c < W) {
+#pragma unroll
+    for (int p = 0; p < kAtP; p++) {
+      int pr = prow0 + ty * kAtP + p;
+      if (pr < nprow) job.out[(size_t)(phase + M * pr) * W + c] = acc[p];
+    }
+  }
+}
+
+template <int F>
+static size_t atrous_smem(int M) {
+  return sizeof(float) * (size_t)(kAtRows + F - 1) * (kAtTX + M * (F - 1));
+}
+
+template <int FA, int FB>
+static size_t atrous_smem_pair(int M) {
+  size_t sm = atrous_smem<FA>(M);
+  if (FB > 0) sm = std::max(sm, atrous_smem<(FB > 0 ? FB : 1)>(M));
+  return sm;
+}
+
+template <int FA, int FB>
+static cudaError_t prepare_atrous_t(int Mmax) {
+  return cudaFuncSetAttribute(k_atrous<FA, FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)atrous_smem_pair<FA, FB>(Mmax));
+}
+
+template <int FA, int FB>
+static cudaError_t launch_atrous_t(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, const float* ha,
+                                   const float* hb, cudaStream_t st) {
+  AtrousTaps<FA> ta;
+  AtrousTaps<FB> tb;
+  fill_taps(ta, ha);
+  if (FB > 0) fill_taps(tb, hb);
+  const size_t sm = atrous_smem_pair<FA, FB>(M);
+  const int nprow_max = (maxH + M - 1) / M;
+  dim3 grid((maxW + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
+  count_launch();
+  k_atrous<FA, FB><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  return cudaGetLastError();
+}
+
+#define NSST_AT_PAIRS(X) X(13, 0) X(19, 0) X(19, 13) X(9, 0) X(7, 0) X(5, 0) X(7, 9) X(7, 5) X(7, 7)
+
+cudaError_t prepare_atrous_kernels(int FA, int FB, int Mmax) {
+#define NSST_AT(a, b) \
+  if (FA == a && FB == b) return prepare_atrous_t<a, b>(Mmax);
+  NSST_AT_PAIRS(NSST_AT)
+#undef NSST_AT
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,
+                          int FB, const float* hb, cudaStream_t st) {
+  if (njobs == 0) return cudaSuccess;
+  if (njobs > kMaxAtrousJobs) return cudaErrorInvalidValue;
+#define NSST_AT(a, b) \
+  if (FA == a && FB == b) return launch_atrous_t<a, b>(jobs, njobs, maxH, maxW, M, ha, hb, st);
+  NSST_AT_PAIRS(NSST_AT)
+#undef NSST_AT
+  return cudaErrorInvalidValue;
+}
+
+bool atrous_pair_supported(int FA, int FB) {
+#define NSST_AT(a, b) \
+  if (FA == a && FB == b) return true;
+  NSST_AT_PAIRS(NSST_AT)
+#undef NSST_AT
+  return false;
+}
+
+// Elementwise threshold of a band (used for the lowpass band and the
+// standalone thresh entry point).  One launch covers nbands bands of n
+// values each; band b uses thr[b].
+__global__ void k_thresh_bands(float* __restrict__ data, size_t n, int nbands, const float* __restrict__ thr,
+                               int mode) {
+  size_t total = n * (size_t)nbands;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    float th = thr[i / n];
+    float v = data[i];
+    float r;
+    if (mode == THRESH_HARD) {
+      r = fabsf(v) > th ? v : 0.0f;
+    } else {
+      float a = fabsf(v) - th;
+      r = a > 0.0f ? copysignf(a, v) : 0.0f;
+    }
+    data[i] = r;
+  }
+}
+
+cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st) {
+  size_t total = n * (size_t)nbands;
+  if (total == 0) return cudaSuccess;
+  int blocks = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
+  count_launch();
+  k_thresh_bands<<<blocks, 256, 0, st>>>(data, n, nbands, thr, mode);
+  return cudaGetLastError();
+}
+
+}  // namespace nsst

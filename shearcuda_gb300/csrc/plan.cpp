@@ -1,0 +1,703 @@
+// NSST plan: filter bank construction, device buffers, job lists and the
+// C ABI entry points declared in include/nsst.h.
+//
+// The plan plays the role of the reference's shearing dictionary
+// (ShearDictionary.h:18-48 / prepare_shearing_filters_cuda.cpp:234-248):
+// it owns the filter spectra, the pyramid filters, the transform tables and
+// every work buffer, so execute calls allocate nothing.  Unlike the
+// reference it also owns static job lists for each kernel stage, so one call
+// is a fixed sequence of launches on the caller's stream.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <thread>
+
+#include "internal.h"
+
+namespace nsst {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+// Host-side fault injection for the allocation path (tests only): the n-th
+// device allocation from now fails as if the device were out of memory.
+static std::atomic<int> g_fail_alloc_countdown{0};
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+static cudaError_t dev_alloc(void** p, size_t bytes) {
+  int c = g_fail_alloc_countdown.load();
+  if (c > 0) {
+    if (g_fail_alloc_countdown.fetch_sub(1) == 1) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+
+}  // namespace nsst
+
+using namespace nsst;
+
+struct nsst_plan {
+  nsst_config cfg{};
+  int H = 0, W = 0, WH = 0, nlev = 0, nbands = 0, ndir_total = 0;
+  std::vector<int> ndir, first_band, band_level;  // per level / per band
+  PyramidFilters pf;
+  std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1
+  int device = 0;
+
+  // one device arena
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  // views into the arena (float2 offsets where noted)
+  float2* spec = nullptr;  // [ndir_total][H][WH] then m0 side arrays [ndir_total][H]
+  size_t m0_off = 0;       // offset (float2) of the side arrays from spec
+  float2 *twH = nullptr, *twWh = nullptr, *twW = nullptr;
+  float* pyr = nullptr;    // (nlev+1) x H x W   analysis pyramid
+  float* tmp = nullptr;    // 2 x H x W          lowpass ping-pong
+  float2* lev = nullptr;   // nlev x H x WH      level spectra
+  float2* band = nullptr;  // ndir_total x H x WH band scratch
+  float2* sum = nullptr;   // nlev x H x WH      synthesis sums
+  float* rec = nullptr;    // (nlev+1) x H x W   synthesis pyramid inputs
+  float* th = nullptr;     // nbands thresholds
+  RowJob* jobs_rows_levels_fwd = nullptr;  // pyr[1..] -> lev
+  ColJob* jobs_cols_levels = nullptr;      // lev in place
+  ColJob* jobs_analysis = nullptr;         // lev -> band
+  RowJob* jobs_rows_bands = nullptr;       // band in place (threshold) / band -> coeffs
+  RowJob* jobs_rows_coeff_fwd = nullptr;   // coeffs -> band (src relative to the caller's buffer)
+  RowJob* jobs_rows_band_to_coeff = nullptr;  // band -> coeffs (dst relative to the caller's buffer)
+  ColJob* jobs_synthesis = nullptr;        // band -> sum
+  RowJob* jobs_rows_levels_inv = nullptr;  // sum -> rec[1..]
+
+  std::vector<double> scalars;
+  bool has_scalars = false;
+  // stage timers
+  bool timing = false;
+  static constexpr int kMaxStages = 32;
+  cudaEvent_t ev[kMaxStages + 1] = {};
+  const char* stage_name[kMaxStages] = {};
+  int nstage = 0;
+  std::mutex mu;  // serialises execute calls that share the plan's work buffers
+};
+
+namespace {
+
+nsst_status fail(nsst_status s, const std::string& msg) {
+  set_error(msg);
+  return s;
+}
+
+nsst_status cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? NSST_ERR_OUT_OF_MEMORY : NSST_ERR_CUDA;
+}
+
+#define NSST_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+  } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+std::vector<float> flip_to_float(const std::vector<double>& h, int F) {
+  std::vector<float> out((size_t)F * F);
+  for (int a = 0; a < F; a++)
+    for (int b = 0; b < F; b++) out[(size_t)a * F + b] = (float)h[(size_t)(F - 1 - a) * F + (F - 1 - b)];
+  return out;
+}
+
+int host_threads() {
+  unsigned n = std::thread::hardware_concurrency();
+  return n == 0 ? 4 : (int)std::min(n, 32u);
+}
+
+nsst_status validate_config(const nsst_config* cfg, int H, int W) {
+  if (!cfg) return fail(NSST_ERR_INVALID_ARG, "config is NULL");
+  if (cfg->nlevels < 1 || cfg->nlevels > NSST_MAX_LEVELS)
+    return fail(NSST_ERR_INVALID_ARG, "nlevels must be in [1, 8]");
+  int nb = 1;
+  for (int i = 0; i < cfg->nlevels; i++) {
+    if (cfg->dcomp[i] < 0 || cfg->dcomp[i] > 6) return fail(NSST_ERR_INVALID_ARG, "dcomp must be in [0, 6]");
+    if (cfg->dsize[i] < 2 || cfg->dsize[i] > 256 || (cfg->dsize[i] & 1))
+      return fail(NSST_ERR_INVALID_ARG, "dsize must be even and in [2, 256]");
+    if ((2 * cfg->dsize[i]) % (1 << cfg->dcomp[i]) != 0 || (2 * cfg->dsize[i]) / (1 << cfg->dcomp[i]) < 2 ||
+        ((2 * cfg->dsize[i]) / (1 << cfg->dcomp[i])) % 2 != 0)
+      return fail(NSST_ERR_INVALID_ARG, "2*dsize must be an even multiple of 2^dcomp (Meyer window period)");
+    nb += 1 << cfg->dcomp[i];
+  }
+  if (nb > NSST_MAX_BANDS) return fail(NSST_ERR_INVALID_ARG, "too many bands");
+  if (H <= 0 || W <= 0 || (W & 1)) return fail(NSST_ERR_INVALID_ARG, "H and W must be positive, W even");
+  if (!col_len_supported(H) || !row_len_supported(W / 2))
+    return fail(NSST_ERR_UNSUPPORTED_SIZE,
+                "unsupported image size: H must be one of 128,192,256,384,512,768,1024,2048 and W/2 one of "
+                "64,96,128,192,256,384,512,1024");
+  for (int i = 0; i < cfg->nlevels; i++)
+    if (cfg->dsize[i] > H || cfg->dsize[i] > W) return fail(NSST_ERR_INVALID_ARG, "dsize larger than the image");
+  return NSST_OK;
+}
+
+}  // namespace
+
+// ===================================================================== API
+extern "C" {
+
+const char* nsst_last_error(void) { return g_last_error.c_str(); }
+const char* nsst_version(void) { return "nsst-gb300 0.1 (sm_103a)"; }
+
+void nsst_debug_fail_next_alloc(int n) { g_fail_alloc_countdown.store(n); }
+
+nsst_status nsst_pyramid_filters(const char* name, int* F, double* taps) {
+  if (!name || !F) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  PyramidFilters pf;
+  if (!pyramid_filters(name, &pf)) return fail(NSST_ERR_INVALID_ARG, std::string("unknown filter ") + name);
+  size_t at = 0;
+  for (int k = 0; k < 4; k++) {
+    F[k] = pf.F[k];
+    if (taps) std::memcpy(taps + at, pf.h[k].data(), pf.h[k].size() * sizeof(double));
+    at += pf.h[k].size();
+  }
+  return NSST_OK;
+}
+
+nsst_status nsst_shearing_filters(int n1, int level, double* out) {
+  if (!out || n1 < 2 || (n1 & 1) || level < 0 || level > 6) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
+  std::vector<double> w = shearing_filters_myer(n1, level);
+  std::memcpy(out, w.data(), w.size() * sizeof(double));
+  return NSST_OK;
+}
+
+nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out) {
+  if (!out) return fail(NSST_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  nsst_status vs = validate_config(cfg, H, W);
+  if (vs != NSST_OK) return vs;
+
+  nsst_plan* p = new (std::nothrow) nsst_plan();
+  if (!p) return fail(NSST_ERR_OUT_OF_MEMORY, "host allocation failed");
+  p->cfg = *cfg;
+  p->cfg.lpfilt[sizeof(p->cfg.lpfilt) - 1] = 0;
+  p->H = H;
+  p->W = W;
+  p->WH = W / 2;
+  p->nlev = cfg->nlevels;
+  p->band_level.push_back(0);
+  for (int l = 0; l < p->nlev; l++) {
+    int nd = 1 << cfg->dcomp[l];
+    p->first_band.push_back(p->ndir_total);
+    p->ndir.push_back(nd);
+    for (int k = 0; k < nd; k++) p->band_level.push_back(l + 1);
+    p->ndir_total += nd;
+  }
+  p->nbands = 1 + p->ndir_total;
+
+  auto destroy = [&](nsst_status s) {
+    nsst_plan_destroy(p);
+    return s;
+  };
+
+  const char* fname = p->cfg.lpfilt[0] ? p->cfg.lpfilt : "maxflat";
+  if (!pyramid_filters(fname, &p->pf)) return destroy(fail(NSST_ERR_INVALID_ARG, "unknown pyramid filter"));
+  if (!atrous_pair_supported(p->pf.F[0], 0) || !atrous_pair_supported(p->pf.F[1], 0) ||
+      !atrous_pair_supported(p->pf.F[2], p->pf.F[3]))
+    return destroy(fail(NSST_ERR_INVALID_ARG, "pyramid filter sizes not compiled"));
+  for (int k = 0; k < 4; k++) p->hflip[k] = flip_to_float(p->pf.h[k], p->pf.F[k]);
+  // One reflection must cover the widest dilated filter (symext.m needs
+  // p + shift <= image size; the coarsest level dilates by 2^(nlevels-1)).
+  const int Mmax = 1 << (p->nlev - 1);
+  int Fmax = *std::max_element(p->pf.F, p->pf.F + 4);
+  if (Mmax * Fmax + 1 > std::min(H, W))
+    return destroy(fail(NSST_ERR_UNSUPPORTED_SIZE, "image too small for the pyramid depth (symmetric extension)"));
+
+  cudaError_t ce = cudaGetDevice(&p->device);
+  if (ce != cudaSuccess) return destroy(cuda_fail(ce, "cudaGetDevice"));
+
+  // ---- arena layout
+  const size_t HW = (size_t)H * W, HWh = (size_t)H * p->WH;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  size_t o_spec = take(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
+  size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH), o_twW = take(sizeof(float2) * p->WH);
+  size_t o_pyr = take(sizeof(float) * HW * (p->nlev + 1));
+  size_t o_tmp = take(sizeof(float) * HW * 2);
+  size_t o_lev = take(sizeof(float2) * HWh * p->nlev);
+  size_t o_band = take(sizeof(float2) * HWh * p->ndir_total);
+  size_t o_sum = take(sizeof(float2) * HWh * p->nlev);
+  size_t o_rec = take(sizeof(float) * HW * (p->nlev + 1));
+  size_t o_th = take(sizeof(float) * p->nbands);
+  size_t o_j1 = take(sizeof(RowJob) * p->nlev), o_j2 = take(sizeof(ColJob) * p->nlev);
+  size_t o_j3 = take(sizeof(ColJob) * p->ndir_total), o_j4 = take(sizeof(RowJob) * p->ndir_total);
+  size_t o_j5 = take(sizeof(RowJob) * p->ndir_total), o_j6 = take(sizeof(ColJob) * p->nlev);
+  size_t o_j7 = take(sizeof(RowJob) * p->nlev), o_j8 = take(sizeof(RowJob) * p->ndir_total);
+  p->arena_bytes = off;
+  ce = dev_alloc((void**)&p->arena, p->arena_bytes);
+  if (ce != cudaSuccess) {
+    p->arena = nullptr;
+    return destroy(cuda_fail(ce, "device allocation of the plan arena"));
+  }
+  char* A = p->arena;
+  p->spec = (float2*)(A + o_spec);
+  p->m0_off = (size_t)p->ndir_total * HWh;
+  p->twH = (float2*)(A + o_twH);
+  p->twWh = (float2*)(A + o_twWh);
+  p->twW = (float2*)(A + o_twW);
+  p->pyr = (float*)(A + o_pyr);
+  p->tmp = (float*)(A + o_tmp);
+  p->lev = (float2*)(A + o_lev);
+  p->band = (float2*)(A + o_band);
+  p->sum = (float2*)(A + o_sum);
+  p->rec = (float*)(A + o_rec);
+  p->th = (float*)(A + o_th);
+  p->jobs_rows_levels_fwd = (RowJob*)(A + o_j1);
+  p->jobs_cols_levels = (ColJob*)(A + o_j2);
+  p->jobs_analysis = (ColJob*)(A + o_j3);
+  p->jobs_rows_bands = (RowJob*)(A + o_j4);
+  p->jobs_rows_coeff_fwd = (RowJob*)(A + o_j5);
+  p->jobs_synthesis = (ColJob*)(A + o_j6);
+  p->jobs_rows_levels_inv = (RowJob*)(A + o_j7);
+  p->jobs_rows_band_to_coeff = (RowJob*)(A + o_j8);
+
+  // ---- filter spectra (FP64 host) -> packed FP32 layout, scaled by 1/(H W)
+  {
+    std::vector<float2> hspec((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H);
+    const int WC = p->WH + 1;
+    const double scale = 1.0 / ((double)H * W);
+    for (int l = 0; l < p->nlev; l++) {
+      std::vector<double> w = shearing_filters_myer(cfg->dsize[l], cfg->dcomp[l]);
+      std::vector<cd> S;
+      if (!level_spectra(w, p->ndir[l], cfg->dsize[l], H, W, &S, host_threads()))
+        return destroy(fail(NSST_ERR_NUMERIC, "shearing filter normalisation divides by zero"));
+      for (int k = 0; k < p->ndir[l]; k++) {
+        const int b = p->first_band[l] + k;
+        const cd* s = S.data() + (size_t)k * H * WC;
+        float2* dst = hspec.data() + (size_t)b * HWh;
+        float2* m0 = hspec.data() + p->m0_off + (size_t)b * H;
+        for (int u = 0; u < H; u++) {
+          for (int v = 1; v < p->WH; v++) {
+            cd z = s[(size_t)u * WC + v] * scale;
+            dst[(size_t)u * p->WH + v] = make_float2((float)z.real(), (float)z.imag());
+          }
+          cd w0 = s[(size_t)u * WC + 0] * scale, wn = s[(size_t)u * WC + p->WH] * scale;
+          cd P = (w0 + wn) * 0.5, Mm = (w0 - wn) * 0.5;
+          dst[(size_t)u * p->WH] = make_float2((float)P.real(), (float)P.imag());
+          m0[u] = make_float2((float)Mm.real(), (float)Mm.imag());
+        }
+      }
+    }
+    ce = cudaMemcpy(p->spec, hspec.data(), hspec.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload spectra"));
+  }
+  {
+    auto tH = twiddle_table(H), tWh = twiddle_table(p->WH), tW = half_twiddle_table(W);
+    ce = cudaMemcpy(p->twH, tH.data(), tH.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->twWh, tWh.data(), tWh.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->twW, tW.data(), tW.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload twiddles"));
+  }
+  // ---- static job lists (offsets in float2 units from the launch bases)
+  {
+    const size_t base_pyr = (size_t)((char*)p->pyr - A) / sizeof(float2);
+    const size_t base_lev = (size_t)((char*)p->lev - A) / sizeof(float2);
+    const size_t base_band = (size_t)((char*)p->band - A) / sizeof(float2);
+    const size_t base_sum = (size_t)((char*)p->sum - A) / sizeof(float2);
+    const size_t base_rec = (size_t)((char*)p->rec - A) / sizeof(float2);
+    std::vector<RowJob> j1(p->nlev), j4(p->ndir_total), j5(p->ndir_total), j7(p->nlev), j8(p->ndir_total);
+    std::vector<ColJob> j2(p->nlev), j3(p->ndir_total), j6(p->nlev);
+    for (int l = 0; l < p->nlev; l++) {
+      j1[l] = RowJob{base_pyr + (size_t)(l + 1) * HWh, base_lev + (size_t)l * HWh, 0, 0};
+      j2[l] = ColJob{base_lev + (size_t)l * HWh, base_lev + (size_t)l * HWh, 0, 0, 0, 0};
+      j6[l] = ColJob{base_band + (size_t)p->first_band[l] * HWh, base_sum + (size_t)l * HWh,
+                     (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], 0};
+      j7[l] = RowJob{base_sum + (size_t)l * HWh, base_rec + (size_t)(l + 1) * HWh, 0, 0};
+      for (int k = 0; k < p->ndir[l]; k++) {
+        const int b = p->first_band[l] + k;
+        j3[b] = ColJob{base_lev + (size_t)l * HWh, base_band + (size_t)b * HWh, (size_t)b * HWh,
+                       p->m0_off + (size_t)b * H, 1, 0};
+        j4[b] = RowJob{base_band + (size_t)b * HWh, base_band + (size_t)b * HWh, 1 + b, 0};
+        // coefficient plane (1 + b) of the caller's buffer -> band scratch
+        j5[b] = RowJob{(size_t)(1 + b) * HWh, base_band + (size_t)b * HWh, 1 + b, 0};
+        j8[b] = RowJob{base_band + (size_t)b * HWh, (size_t)(1 + b) * HWh, 1 + b, 0};
+      }
+    }
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+      return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    ce = up(p->jobs_rows_levels_fwd, j1.data(), j1.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_cols_levels, j2.data(), j2.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_analysis, j3.data(), j3.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_rows_bands, j4.data(), j4.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_rows_coeff_fwd, j5.data(), j5.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_synthesis, j6.data(), j6.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_rows_levels_inv, j7.data(), j7.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->jobs_rows_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
+    if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload job lists"));
+  }
+  ce = prepare_row_kernels(p->WH);
+  if (ce == cudaSuccess) ce = prepare_col_kernels(H);
+  if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[0], 0, Mmax);
+  if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[1], 0, Mmax);
+  if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[2], p->pf.F[3], Mmax);
+  if (ce != cudaSuccess) return destroy(cuda_fail(ce, "kernel attribute setup"));
+  *out = p;
+  return NSST_OK;
+}
+
+nsst_status nsst_plan_destroy(nsst_plan* p) {
+  if (!p) return NSST_OK;
+  for (cudaEvent_t e : p->ev)
+    if (e) cudaEventDestroy(e);
+  if (p->arena) cudaFree(p->arena);
+  delete p;
+  return NSST_OK;
+}
+
+int nsst_plan_num_bands(const nsst_plan* p) { return p ? p->nbands : 0; }
+
+nsst_status nsst_plan_band_levels(const nsst_plan* p, int* out) {
+  if (!p || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  std::copy(p->band_level.begin(), p->band_level.end(), out);
+  return NSST_OK;
+}
+
+size_t nsst_plan_device_bytes(const nsst_plan* p) { return p ? p->arena_bytes : 0; }
+
+nsst_status nsst_level_spectra(int dsize, int dcomp, int H, int W, double* out) {
+  if (!out || dsize < 2 || (dsize & 1) || dcomp < 0 || dcomp > 6 || H < dsize || W < dsize || (W & 1))
+    return fail(NSST_ERR_INVALID_ARG, "bad arguments");
+  std::vector<double> w = shearing_filters_myer(dsize, dcomp);
+  std::vector<cd> S;
+  if (!level_spectra(w, 1 << dcomp, dsize, H, W, &S, host_threads()))
+    return fail(NSST_ERR_NUMERIC, "normalisation divides by zero");
+  std::memcpy(out, S.data(), S.size() * sizeof(cd));
+  return NSST_OK;
+}
+
+nsst_status nsst_plan_level_spectra(const nsst_plan* p, int level, double* out) {
+  if (!p || !out || level < 0 || level >= p->nlev) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
+  std::vector<double> w = shearing_filters_myer(p->cfg.dsize[level], p->cfg.dcomp[level]);
+  std::vector<cd> S;
+  if (!level_spectra(w, p->ndir[level], p->cfg.dsize[level], p->H, p->W, &S, host_threads()))
+    return fail(NSST_ERR_NUMERIC, "normalisation divides by zero");
+  std::memcpy(out, S.data(), S.size() * sizeof(cd));
+  return NSST_OK;
+}
+
+nsst_status nsst_plan_set_scalars(nsst_plan* p, const double* s) {
+  if (!p || !s) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  for (int b = 0; b < p->nbands; b++)
+    if (!std::isfinite(s[b]) || s[b] < 0) return fail(NSST_ERR_INVALID_ARG, "scalars must be finite and >= 0");
+  p->scalars.assign(s, s + p->nbands);
+  p->has_scalars = true;
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+// ============================================================ stage helpers
+namespace {
+
+void timer_begin(nsst_plan* p, cudaStream_t st) {
+  p->nstage = 0;
+  if (p->timing) cudaEventRecord(p->ev[0], st);
+}
+void timer_mark(nsst_plan* p, const char* name, cudaStream_t st) {
+  if (!p->timing || p->nstage >= nsst_plan::kMaxStages) return;
+  p->stage_name[p->nstage] = name;
+  cudaEventRecord(p->ev[++p->nstage], st);
+}
+
+// atrousdec.m:19-51 on the device: x -> y[0] lowpass, y[1..nlev] bandpass coarse -> fine.
+nsst_status run_atrousdec(nsst_plan* p, const float* x, float* const* y, cudaStream_t st) {
+  const int H = p->H, W = p->W, L = p->nlev;
+  const float* cur = x;
+  for (int i = 0; i < L; i++) {  // i = 0 is the undilated first level
+    const int M = 1 << i;
+    float* lo = (i == L - 1) ? y[0] : p->tmp + (size_t)(i & 1) * H * W;
+    AtrousJobs jl{}, jh{};
+    jl.j[0] = AtrousJob{cur, nullptr, lo, H, W};
+    jh.j[0] = AtrousJob{cur, nullptr, y[L - i], H, W};
+    static const char* kHi[] = {"atrous_dec_h1_M1", "atrous_dec_h1_M2", "atrous_dec_h1_M4", "atrous_dec_h1_M8",
+                                "atrous_dec_h1_M16", "atrous_dec_h1_M32", "atrous_dec_h1_M64", "atrous_dec_h1_M128"};
+    static const char* kLo[] = {"atrous_dec_h0_M1", "atrous_dec_h0_M2", "atrous_dec_h0_M4", "atrous_dec_h0_M8",
+                                "atrous_dec_h0_M16", "atrous_dec_h0_M32", "atrous_dec_h0_M64", "atrous_dec_h0_M128"};
+    cudaError_t e = launch_atrous(jh, 1, H, W, M, p->pf.F[1], p->hflip[1].data(), 0, nullptr, st);
+    if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+    timer_mark(p, kHi[i], st);
+    e = launch_atrous(jl, 1, H, W, M, p->pf.F[0], p->hflip[0].data(), 0, nullptr, st);
+    if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+    timer_mark(p, kLo[i], st);
+    cur = lo;
+  }
+  return NSST_OK;
+}
+
+// atrousrec.m:18-41 on the device: y[0..nlev] -> out.
+nsst_status run_atrousrec(nsst_plan* p, const float* const* y, float* out, cudaStream_t st) {
+  const int H = p->H, W = p->W, L = p->nlev;
+  const float* cur = y[0];
+  for (int i = L - 1; i >= 0; i--) {
+    const int M = 1 << i;
+    float* dst = (i == 0) ? out : p->tmp + (size_t)(i & 1) * H * W;
+    AtrousJobs j{};
+    j.j[0] = AtrousJob{cur, y[L - i], dst, H, W};
+    static const char* kRec[] = {"atrous_rec_M1", "atrous_rec_M2", "atrous_rec_M4", "atrous_rec_M8",
+                                 "atrous_rec_M16", "atrous_rec_M32", "atrous_rec_M64", "atrous_rec_M128"};
+    cudaError_t e = launch_atrous(j, 1, H, W, M, p->pf.F[2], p->hflip[2].data(), p->pf.F[3], p->hflip[3].data(), st);
+    if (e != cudaSuccess) return cuda_fail(e, "atrous synthesis launch");
+    timer_mark(p, kRec[i], st);
+    cur = dst;
+  }
+  return NSST_OK;
+}
+
+nsst_status upload_thresholds(nsst_plan* p, double sigma, const double* K, const double* scalars,
+                              std::vector<float>* hth, cudaStream_t st) {
+  if (!K) return fail(NSST_ERR_INVALID_ARG, "K is NULL");
+  if (!scalars) {
+    if (!p->has_scalars) return fail(NSST_ERR_INVALID_ARG, "no scalars given and none stored in the plan");
+    scalars = p->scalars.data();
+  }
+  if (!std::isfinite(sigma) || sigma < 0) return fail(NSST_ERR_INVALID_ARG, "sigma must be finite and >= 0");
+  hth->resize(p->nbands);
+  for (int b = 0; b < p->nbands; b++) {
+    double k = K[p->band_level[b]];
+    double t = k * sigma * scalars[b];
+    if (!std::isfinite(t) || t < 0) return fail(NSST_ERR_INVALID_ARG, "thresholds must be finite and >= 0");
+    (*hth)[b] = (float)t;
+  }
+  cudaError_t e = cudaMemcpyAsync(p->th, hth->data(), p->nbands * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "upload thresholds");
+  return NSST_OK;
+}
+
+bool aligned16(const void* ptr) { return ((uintptr_t)ptr & 15) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream) {
+  if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t HW = (size_t)p->H * p->W;
+  std::vector<float*> ys(p->nlev + 1);
+  for (int i = 0; i <= p->nlev; i++) ys[i] = y + i * HW;
+  return run_atrousdec(p, x, ys.data(), (cudaStream_t)stream);
+}
+
+nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream) {
+  if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t HW = (size_t)p->H * p->W;
+  std::vector<const float*> ys(p->nlev + 1);
+  for (int i = 0; i <= p->nlev; i++) ys[i] = y + i * HW;
+  return run_atrousrec(p, ys.data(), x, (cudaStream_t)stream);
+}
+
+nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* stream) {
+  if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t HW = (size_t)p->H * p->W;
+  std::vector<float*> ys(p->nlev + 1);
+  ys[0] = coeffs;  // lowpass goes straight to plane 0
+  for (int i = 1; i <= p->nlev; i++) ys[i] = p->pyr + i * HW;
+  nsst_status s = run_atrousdec(p, x, ys.data(), st);
+  if (s != NSST_OK) return s;
+  char* A = p->arena;
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_levels_fwd, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr,
+                        0, st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->jobs_cols_levels, p->nlev, p->H, p->W, (float2*)A, (float2*)A, nullptr, 0,
+                        p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->jobs_analysis, p->ndir_total, p->H, p->W, (float2*)A, (float2*)A,
+                        p->spec, 0, p->twH, st));
+  // band scratch -> coefficient planes 1.. of the caller's buffer
+  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_band_to_coeff, p->ndir_total, p->H, p->W, A, coeffs, p->twWh,
+                        p->twW, nullptr, 0, st));
+  return NSST_OK;
+}
+
+nsst_status nsst_thresh(nsst_plan* p, float* coeffs, double sigma, const double* K, const double* scalars, int mode,
+                        void* stream) {
+  if (!p || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<float> hth;
+  nsst_status s = upload_thresholds(p, sigma, K, scalars, &hth, st);
+  if (s != NSST_OK) return s;
+  NSST_CUDA(launch_thresh_bands(coeffs, (size_t)p->H * p->W, p->nbands, p->th, mode, st));
+  return NSST_OK;
+}
+
+nsst_status nsst_inverse_shear(nsst_plan* p, const float* coeffs, float* x, void* stream) {
+  if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  char* A = p->arena;
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_coeff_fwd, p->ndir_total, p->H, p->W, coeffs, A, p->twWh, p->twW,
+                        nullptr, 0, st));
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->jobs_synthesis, p->nlev, p->H, p->W, (float2*)A, (float2*)A, p->spec,
+                        (size_t)p->H * p->WH, p->twH, st));
+  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_levels_inv, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+                        st));
+  const size_t HW = (size_t)p->H * p->W;
+  std::vector<const float*> ys(p->nlev + 1);
+  ys[0] = coeffs;
+  for (int i = 1; i <= p->nlev; i++) ys[i] = p->rec + i * HW;
+  return run_atrousrec(p, ys.data(), x, st);
+}
+
+nsst_status nsst_denoise(nsst_plan* p, const float* x, float* out, double sigma, const double* K,
+                         const double* scalars, int mode, void* stream) {
+  if (!p || !x || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<float> hth;
+  nsst_status s = upload_thresholds(p, sigma, K, scalars, &hth, st);
+  if (s != NSST_OK) return s;
+  timer_begin(p, st);
+  const size_t HW = (size_t)p->H * p->W;
+  std::vector<float*> ys(p->nlev + 1);
+  for (int i = 0; i <= p->nlev; i++) ys[i] = p->pyr + i * HW;
+  s = run_atrousdec(p, x, ys.data(), st);
+  if (s != NSST_OK) return s;
+  char* A = p->arena;
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_levels_fwd, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr,
+                        0, st));
+  timer_mark(p, "fft_rows_fwd", st);
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->jobs_cols_levels, p->nlev, p->H, p->W, (float2*)A, (float2*)A, nullptr, 0,
+                        p->twH, st));
+  timer_mark(p, "fft_cols_fwd", st);
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->jobs_analysis, p->ndir_total, p->H, p->W, (float2*)A, (float2*)A,
+                        p->spec, 0, p->twH, st));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Thresh, p->jobs_rows_bands, p->ndir_total, p->H, p->W, A, A, p->twWh, p->twW, p->th,
+                        mode, st));
+  timer_mark(p, "band_rows_threshold", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->jobs_synthesis, p->nlev, p->H, p->W, (float2*)A, (float2*)A, p->spec,
+                        (size_t)p->H * p->WH, p->twH, st));
+  timer_mark(p, "band_synthesis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_levels_inv, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+                        st));
+  timer_mark(p, "fft_rows_inv", st);
+  // lowpass band: threshold only when it can change anything (t > 0)
+  const float* low = p->pyr;
+  if (hth[0] > 0.0f) {
+    NSST_CUDA(cudaMemcpyAsync(p->rec, p->pyr, HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    NSST_CUDA(launch_thresh_bands(p->rec, HW, 1, p->th, mode, st));
+    low = p->rec;
+    timer_mark(p, "lowpass_threshold", st);
+  }
+  std::vector<const float*> yr(p->nlev + 1);
+  yr[0] = low;
+  for (int i = 1; i <= p->nlev; i++) yr[i] = p->rec + i * HW;
+  return run_atrousrec(p, yr.data(), out, st);
+}
+
+nsst_status nsst_timers_enable(nsst_plan* p, int enable) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (enable && !p->ev[0]) {
+    for (cudaEvent_t& e : p->ev) {
+      cudaError_t ce = cudaEventCreate(&e);
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaEventCreate");
+    }
+  }
+  p->timing = enable != 0;
+  p->nstage = 0;
+  return NSST_OK;
+}
+
+int nsst_timers_read(nsst_plan* p, char* names, size_t names_len, float* ms, int max_stages) {
+  if (!p || !p->timing || p->nstage == 0) return 0;
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (cudaEventSynchronize(p->ev[p->nstage]) != cudaSuccess) return -1;
+  std::string all;
+  int n = std::min(p->nstage, max_stages);
+  for (int i = 0; i < n; i++) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, p->ev[i], p->ev[i + 1]);
+    if (ms) ms[i] = t;
+    all += p->stage_name[i];
+    all += '\n';
+  }
+  if (names && names_len) {
+    size_t m = std::min(all.size(), names_len - 1);
+    std::memcpy(names, all.data(), m);
+    names[m] = 0;
+  }
+  return n;
+}
+
+uint64_t nsst_launch_count(void) { return g_launches.load(); }
+
+nsst_status nsst_compute_scalars(nsst_plan* p, uint64_t seed, double* out) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  const size_t HW = (size_t)p->H * p->W;
+  // seeded N(0,1) image in FP64 (Box-Muller over a 64-bit Mersenne twister)
+  std::mt19937_64 gen(seed);
+  std::vector<float> noise(HW);
+  for (size_t i = 0; i < HW; i += 2) {
+    double u1 = ((gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    double u2 = ((gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    double r = std::sqrt(-2.0 * std::log(u1));
+    noise[i] = (float)(r * std::cos(2 * M_PI * u2));
+    if (i + 1 < HW) noise[i + 1] = (float)(r * std::sin(2 * M_PI * u2));
+  }
+  float *dx = nullptr, *dc = nullptr;
+  cudaError_t e = dev_alloc((void**)&dx, HW * sizeof(float));
+  if (e != cudaSuccess) return cuda_fail(e, "scalar scratch");
+  e = dev_alloc((void**)&dc, HW * sizeof(float) * p->nbands);
+  if (e != cudaSuccess) {
+    cudaFree(dx);
+    return cuda_fail(e, "scalar scratch");
+  }
+  nsst_status s = NSST_OK;
+  std::vector<float> coeffs(HW * p->nbands);
+  e = cudaMemcpy(dx, noise.data(), HW * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    s = nsst_shear_trans(p, dx, dc, nullptr);
+    if (s == NSST_OK) e = cudaMemcpy(coeffs.data(), dc, coeffs.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dx);
+  cudaFree(dc);
+  if (e != cudaSuccess) return cuda_fail(e, "compute scalars");
+  if (s != NSST_OK) return s;
+  // MAD / 0.6745 per band (nsst_scalars.m:36,43), FP64 on the host
+  std::vector<double> sc(p->nbands);
+  std::vector<double> v(HW);
+  auto median = [](std::vector<double>& a) {
+    size_t n = a.size(), h = n / 2;
+    std::nth_element(a.begin(), a.begin() + h, a.end());
+    double hi = a[h];
+    if (n % 2) return hi;
+    double lo = *std::max_element(a.begin(), a.begin() + h);
+    return 0.5 * (lo + hi);
+  };
+  for (int b = 0; b < p->nbands; b++) {
+    for (size_t i = 0; i < HW; i++) v[i] = coeffs[(size_t)b * HW + i];
+    double m = median(v);
+    for (size_t i = 0; i < HW; i++) v[i] = std::fabs(v[i] - m);
+    sc[b] = median(v) / 0.6745;
+  }
+  p->scalars = sc;
+  p->has_scalars = true;
+  if (out) std::copy(sc.begin(), sc.end(), out);
+  return NSST_OK;
+}
+
+}  // extern "C"

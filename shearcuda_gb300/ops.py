@@ -1,0 +1,260 @@
+"""Python mirror of ShearCuda's GPU operator surface over libnsst.so.
+
+Function names, argument meaning and error behaviour follow the reference's
+MEX operators so that code written against them reads the same:
+
+=============================================  =====================================================
+here                                           reference (ShearCuda tree)
+=============================================  =====================================================
+``prepare_shearing_filters_cuda``              shearcuda/src_cuda/prepare_shearing_filters_cuda.cpp:61-249
+``clear_shearing_filters_cuda``                shearcuda/src_cuda/clear_shearing_filters_cuda.cpp:51-96
+``shear_trans_cuda``                           shearcuda/src_cuda/shear_trans_cuda.cpp:56-217
+``thresh_cuda`` / ``softth_cuda``              shearcuda/src_cuda/thresh_cuda.cpp:57-217, softth_cuda.cpp:49-112
+``inverse_shear_cuda``                         shearcuda/src_cuda/inverse_shear_cuda.cpp:57-219
+``atrousdec`` / ``atrousrec``                  shearcuda/src_cuda/atrousdec.cpp:41-131, atrousrec.cpp:42-132
+``nsst_scalars``                               shearlet_toolbox_1/nsst_scalars.m:28-45
+``nsst_denoise``                               shearcuda/test/shear_denoise_cuda.m:14-23 (fused)
+=============================================  =====================================================
+
+Device arrays are ``torch`` CUDA float32 tensors (PyTorch supplies device
+memory and streams only; all compute runs in libnsst.so's kernels).  The
+coefficient "cell array" of the reference is returned as a list
+``[lowpass (H, W), level 0 (ndir0, H, W), ...]`` of views into one
+contiguous (nbands, H, W) tensor.  Errors raise ``NsstError`` (the
+reference raises MATLAB errors through mexErrMsgTxt).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from ._lib import (NsstConfig, NsstError, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, check, lib)
+
+__all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters_cuda', 'shear_trans_cuda',
+           'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'nsst_scalars',
+           'nsst_denoise', 'pyramid_filters', 'shearing_filters', 'level_spectra', 'launch_count', 'NsstError']
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dev(t, name, shape=None):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float32:
+        raise NsstError(1, '%s must be a CUDA float32 tensor' % name)
+    if not t.is_contiguous():
+        raise NsstError(1, '%s must be contiguous' % name)
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise NsstError(1, '%s has shape %s, expected %s' % (name, tuple(t.shape), tuple(shape)))
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class ShearPlan:
+    """The prepared shearing dictionary (the ``shear`` struct the reference's
+    prepare_shearing_filters_cuda returns): filter spectra, pyramid filters
+    and work buffers for one image size."""
+
+    def __init__(self, dcomp, dsize, H, W, lpfilt='maxflat', pyramid=PYRAMID_AUTO):
+        if len(dcomp) != len(dsize):
+            raise NsstError(1, 'dcomp and dsize must have the same length')
+        cfg = NsstConfig()
+        cfg.nlevels = len(dcomp)
+        for i, (c, s) in enumerate(zip(dcomp, dsize)):
+            cfg.dcomp[i] = int(c)
+            cfg.dsize[i] = int(s)
+        cfg.lpfilt = lpfilt.encode()
+        cfg.pyramid = pyramid
+        h = ctypes.c_void_p()
+        check(lib().nsst_plan_create(ctypes.byref(cfg), int(H), int(W), ctypes.byref(h)))
+        self._h = h
+        self.dcomp, self.dsize, self.H, self.W, self.lpfilt = list(dcomp), list(dsize), int(H), int(W), lpfilt
+        self.nlevels = len(dcomp)
+        self.nbands = lib().nsst_plan_num_bands(h)
+        lv = (ctypes.c_int * self.nbands)()
+        check(lib().nsst_plan_band_levels(h, lv))
+        self.band_levels = list(lv)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise NsstError(1, 'plan has been cleared')
+        return self._h
+
+    def device_bytes(self):
+        return lib().nsst_plan_device_bytes(self.handle)
+
+    def set_scalars(self, scalars):
+        s = np.ascontiguousarray(flatten_scalars(scalars), dtype=np.float64)
+        if s.size != self.nbands:
+            raise NsstError(1, 'need %d scalars' % self.nbands)
+        check(lib().nsst_plan_set_scalars(self.handle, _dptr(s)))
+
+    def level_spectra(self, level):
+        nd = 1 << self.dcomp[level]
+        out = np.empty((nd, self.H, self.W // 2 + 1), dtype=np.complex128)
+        check(lib().nsst_plan_level_spectra(self.handle, level, _dptr(out.view(np.float64))))
+        return out
+
+    def enable_timers(self, on=True):
+        check(lib().nsst_timers_enable(self.handle, 1 if on else 0))
+
+    def read_timers(self, max_stages=32):
+        """Per-stage milliseconds of the last execute call, as [(name, ms)]."""
+        names = ctypes.create_string_buffer(4096)
+        ms = (ctypes.c_float * max_stages)()
+        n = lib().nsst_timers_read(self.handle, names, 4096, ms, max_stages)
+        if n < 0:
+            raise NsstError(4, 'timer read failed')
+        labels = names.value.decode().split('\n')[:n]
+        return list(zip(labels, [float(ms[i]) for i in range(n)]))
+
+    def close(self):
+        if self._h is not None:
+            lib().nsst_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def split(self, coeffs):
+        """(nbands, H, W) tensor -> [lowpass, level0 (ndir0,H,W), ...] views."""
+        out = [coeffs[0]]
+        at = 1
+        for c in self.dcomp:
+            out.append(coeffs[at:at + (1 << c)])
+            at += 1 << c
+        return out
+
+
+def flatten_scalars(scalars):
+    """Accept the reference's cell layout {lowpass, [per-direction]...} or a flat list."""
+    if isinstance(scalars, (list, tuple)) and len(scalars) and np.ndim(scalars[0]) == 0 and \
+            any(np.ndim(s) > 0 for s in scalars[1:]):
+        return np.concatenate([np.atleast_1d(np.asarray(s, np.float64)) for s in scalars])
+    return np.asarray(scalars, dtype=np.float64).ravel()
+
+
+def _kvec(plan, K):
+    K = np.ascontiguousarray(np.asarray(K, dtype=np.float64).ravel())
+    if K.size == 3 and plan.nlevels != 2:
+        # nsst_HT.m Tscalars: [lowpass, levels 1..J-1, finest level J]
+        K = np.array([K[0]] + [K[1]] * (plan.nlevels - 1) + [K[2]], dtype=np.float64)
+    if K.size != plan.nlevels + 1:
+        raise NsstError(1, 'K needs nlevels+1 (or 3, Tscalars-style) entries')
+    return K
+
+
+def prepare_shearing_filters_cuda(dcomp, dsize, H, W=None, lpfilt='maxflat', pyramid=PYRAMID_AUTO):
+    return ShearPlan(dcomp, dsize, H, H if W is None else W, lpfilt, pyramid)
+
+
+def clear_shearing_filters_cuda(shear):
+    shear.close()
+
+
+def atrousdec(x, shear, stream=None):
+    y = torch.empty((shear.nlevels + 1, shear.H, shear.W), device=x.device, dtype=torch.float32)
+    check(lib().nsst_atrousdec(shear.handle, _dev(x, 'x', (shear.H, shear.W)), _dev(y, 'y'), _stream(stream)))
+    return y
+
+
+def atrousrec(y, shear, stream=None):
+    x = torch.empty((shear.H, shear.W), device=y.device, dtype=torch.float32)
+    check(lib().nsst_atrousrec(shear.handle, _dev(y, 'y', (shear.nlevels + 1, shear.H, shear.W)), _dev(x, 'x'),
+                               _stream(stream)))
+    return x
+
+
+def shear_trans_cuda(x, lpfilt, shear, coeff=None, stream=None):
+    """Forward NSST.  ``coeff`` (optional) is written in place, like the
+    reference's coeff_inplace argument (shear_trans_cuda.cpp:191-205)."""
+    if lpfilt != shear.lpfilt:
+        raise NsstError(1, 'lpfilt %r does not match the prepared dictionary (%r)' % (lpfilt, shear.lpfilt))
+    if coeff is None:
+        coeff = torch.empty((shear.nbands, shear.H, shear.W), device=x.device, dtype=torch.float32)
+    check(lib().nsst_shear_trans(shear.handle, _dev(x, 'x', (shear.H, shear.W)),
+                                 _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W)), _stream(stream)))
+    return coeff
+
+
+def thresh_cuda(coeff, sigma, K, scalars, shear, mode=THRESH_HARD, stream=None):
+    """In-place threshold of all bands: t_b = K[level(b)] * sigma * scalars[b]."""
+    s = np.ascontiguousarray(flatten_scalars(scalars), dtype=np.float64)
+    if s.size != shear.nbands:
+        raise NsstError(1, 'need %d scalars' % shear.nbands)
+    K = _kvec(shear, K)
+    check(lib().nsst_thresh(shear.handle, _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W)), float(sigma),
+                            _dptr(K), _dptr(s), mode, _stream(stream)))
+    return coeff
+
+
+def softth_cuda(coeff, sigma, K, scalars, shear, stream=None):
+    return thresh_cuda(coeff, sigma, K, scalars, shear, THRESH_SOFT, stream)
+
+
+def inverse_shear_cuda(coeff, lpfilt, shear, stream=None):
+    if lpfilt != shear.lpfilt:
+        raise NsstError(1, 'lpfilt %r does not match the prepared dictionary (%r)' % (lpfilt, shear.lpfilt))
+    x = torch.empty((shear.H, shear.W), device=coeff.device, dtype=torch.float32)
+    check(lib().nsst_inverse_shear(shear.handle, _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W)),
+                                   _dev(x, 'x'), _stream(stream)))
+    return x
+
+
+def nsst_denoise(x, shear, sigma, K, scalars=None, mode=THRESH_HARD, out=None, stream=None):
+    if out is None:
+        out = torch.empty_like(x)
+    K = _kvec(shear, K)
+    sp = None
+    if scalars is not None:
+        s = np.ascontiguousarray(flatten_scalars(scalars), dtype=np.float64)
+        if s.size != shear.nbands:
+            raise NsstError(1, 'need %d scalars' % shear.nbands)
+        sp = _dptr(s)
+    check(lib().nsst_denoise(shear.handle, _dev(x, 'x', (shear.H, shear.W)), _dev(out, 'out', (shear.H, shear.W)),
+                             float(sigma), _dptr(K), sp, mode, _stream(stream)))
+    return out
+
+
+def launch_count():
+    """Kernels launched by libnsst.so since it was loaded."""
+    return int(lib().nsst_launch_count())
+
+
+def nsst_scalars(shear, seed=0):
+    out = np.empty(shear.nbands, dtype=np.float64)
+    check(lib().nsst_compute_scalars(shear.handle, ctypes.c_uint64(seed), _dptr(out)))
+    return out
+
+
+# ------------------------------------------------------------ host-only helpers
+def pyramid_filters(name='maxflat'):
+    F = (ctypes.c_int * 4)()
+    check(lib().nsst_pyramid_filters(name.encode(), F, None))
+    taps = np.empty(sum(f * f for f in F), dtype=np.float64)
+    check(lib().nsst_pyramid_filters(name.encode(), F, _dptr(taps)))
+    out, at = [], 0
+    for f in F:
+        out.append(taps[at:at + f * f].reshape(f, f))
+        at += f * f
+    return tuple(out)
+
+
+def shearing_filters(n1, level):
+    out = np.empty((1 << level, n1, n1), dtype=np.float64)
+    check(lib().nsst_shearing_filters(n1, level, _dptr(out)))
+    return out
+
+
+def level_spectra(dsize, dcomp, H, W):
+    out = np.empty((1 << dcomp, H, W // 2 + 1), dtype=np.complex128)
+    check(lib().nsst_level_spectra(dsize, dcomp, H, W, _dptr(out.view(np.float64))))
+    return out

@@ -1,0 +1,53 @@
+"""Seeded synthetic test images for the NSST denoising workloads.
+
+No public dataset is involved: the reference demos use photographs that are
+not shipped (shearcuda/test/deno_*_shearlets.m:17), so images are drawn from
+a fixed generator: a linear intensity gradient, then 1-20 filled ellipses
+(centre uniform over the image, semi-axes U[0.02, 0.3] * min(H, W), angle
+U[0, pi), intensity U[0, 255]; later ellipses overwrite earlier ones), plus
+i.i.d. N(0, sigma^2) noise.  All FP64 from numpy's PCG64 generator.
+"""
+import numpy as np
+
+BATCH_SIZES = ((256, 256), (384, 512), (512, 512), (768, 1024), (1024, 1024))
+
+
+def clean_image(H, W, rng):
+    yy, xx = np.mgrid[0:H, 0:W].astype(np.float64)
+    u, v = yy / max(H - 1, 1), xx / max(W - 1, 1)
+    theta = rng.uniform(0, 2 * np.pi)
+    g0, g1 = rng.uniform(0, 128), rng.uniform(0, 96)
+    img = g0 + g1 * (np.cos(theta) * u + np.sin(theta) * v)
+    m = min(H, W)
+    for _ in range(int(rng.integers(1, 21))):
+        cy, cx = rng.uniform(0, H), rng.uniform(0, W)
+        a, b = rng.uniform(0.02, 0.3, size=2) * m
+        ang = rng.uniform(0, np.pi)
+        val = rng.uniform(0, 255)
+        c, s = np.cos(ang), np.sin(ang)
+        dy, dx = yy - cy, xx - cx
+        r1 = (c * dx + s * dy) / a
+        r2 = (-s * dx + c * dy) / b
+        img[r1 * r1 + r2 * r2 <= 1.0] = val
+    return img
+
+
+def noisy_image(H, W, sigma, seed):
+    """(clean, noisy) FP64 pair for one seed."""
+    rng = np.random.default_rng(seed)
+    clean = clean_image(H, W, rng)
+    noisy = clean + sigma * rng.standard_normal((H, W))
+    return clean, noisy
+
+
+def uneven_batch(n, seed, sizes=BATCH_SIZES, sigma_range=(10.0, 40.0)):
+    """n (clean, noisy, sigma) triples with sizes drawn uniformly from `sizes`
+    and sigma ~ U[sigma_range] per image."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        H, W = sizes[int(rng.integers(0, len(sizes)))]
+        sigma = float(rng.uniform(*sigma_range))
+        clean, noisy = noisy_image(H, W, sigma, seed * 100003 + i)
+        out.append((clean, noisy, sigma))
+    return out

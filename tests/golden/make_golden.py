@@ -1,0 +1,127 @@
+"""Generate the golden fixtures under tests/golden/ from the reference tree.
+
+Run in the container that holds the read-only reference checkout:
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+It writes two kinds of fixtures, both small enough to commit:
+
+* ``pyramid_filter_tables.json``: the tabulated à trous filter matrices of
+  ``shearlet_toolbox_1/atrousfilters.m`` (cases '9-7' lines 27-104,
+  'maxflat' lines 106-175, 'pyr' lines 178-206, 'pyrexc' lines 208-236),
+  parsed from the MATLAB source text (the numbers are data that defines the
+  filters; they are read, never retyped).  The mirroring / scaling steps that
+  follow each table stay in code (oracle and product restate them).
+* ``atrousc_ref_cases.npz``: inputs and outputs of the reference's own
+  ``atrousc.cpp`` (compiled unchanged through the project-written MEX shim in
+  ``oracle/mex_shim``; see ``oracle/build_oracle.py``) on seeded random
+  signals, for every (filter size, dilation) pair the 4-level pyramid uses,
+  plus odd-sized ragged cases.  These pin the C and NumPy restatements.
+"""
+import argparse
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def _strip_comments(line):
+    out = []
+    in_str = False
+    for ch in line:
+        if ch == "'":
+            in_str = not in_str
+        if ch == '%' and not in_str:
+            break
+        out.append(ch)
+    return ''.join(out)
+
+
+def parse_matlab_case(text, case_name):
+    """Return {var: 2-D list} for every ``var = [ ... ];`` literal inside
+    ``case '<case_name>'`` of a MATLAB switch statement."""
+    lines = text.splitlines()
+    start = None
+    for i, ln in enumerate(lines):
+        if re.match(r"\s*case\s+'%s'" % re.escape(case_name), ln):
+            start = i + 1
+            break
+    if start is None:
+        raise ValueError('case %r not found' % case_name)
+    body = []
+    for ln in lines[start:]:
+        if re.match(r"\s*(case\s+'|end\s*$|otherwise)", ln):
+            break
+        body.append(_strip_comments(ln))
+    # join continuation lines
+    joined = ' '.join(l.replace('...', ' ') for l in body)
+    mats = {}
+    for m in re.finditer(r"(\w+)\s*=\s*\[([^\]]*)\]", joined):
+        name, inner = m.group(1), m.group(2)
+        if not re.search(r'\d', inner) or re.search(r'[A-Za-z_]\w*\s*\(', inner):
+            continue  # mirroring statements such as [h0 fliplr(h0(:,1:end-1))]
+        rows = [r for r in inner.split(';') if r.strip()]
+        mat = [[float(tok) for tok in r.replace(',', ' ').split()] for r in rows]
+        widths = {len(r) for r in mat}
+        if len(widths) != 1:
+            raise ValueError('ragged matrix %s in case %s: %s' % (name, case_name, widths))
+        mats[name] = mat
+    return mats
+
+
+def filter_tables(reference):
+    path = os.path.join(reference, 'shearlet_toolbox_1', 'atrousfilters.m')
+    text = open(path).read()
+    out = {'source': 'shearlet_toolbox_1/atrousfilters.m'}
+    for case in ('9-7', 'maxflat', 'pyr', 'pyrexc'):
+        mats = parse_matlab_case(text, case)
+        for v in ('h0', 'h1', 'g0', 'g1'):
+            if v not in mats:
+                raise ValueError('missing %s in case %s' % (v, case))
+        out[case] = {v: mats[v] for v in ('h0', 'h1', 'g0', 'g1')}
+    return out
+
+
+def atrousc_cases(seed=1234):
+    sys.path.insert(0, ROOT)
+    from oracle import atrous_ref  # noqa: E402  (reference atrousc via the MEX shim)
+    if not atrous_ref.available():
+        raise SystemExit('oracle/_ref not built: run python oracle/build_oracle.py first')
+    rng = np.random.default_rng(seed)
+    cases = {}
+    # (signal rows, signal cols, filter size, dilation)
+    shapes = []
+    for F in (13, 19):
+        for M in (1, 2, 4, 8):
+            shapes.append((12 + M * F, 10 + M * F, F, M))
+    shapes += [(37, 29, 7, 3), (20, 33, 5, 2), (9, 9, 9, 1)]
+    for idx, (sr, sc, F, M) in enumerate(shapes):
+        S = rng.standard_normal((sr, sc))
+        Fm = rng.standard_normal((F, F))
+        out = atrous_ref.atrousc(S, Fm, M)
+        cases['S_%d' % idx] = S
+        cases['F_%d' % idx] = Fm
+        cases['M_%d' % idx] = np.array([M])
+        cases['out_%d' % idx] = out
+    cases['n'] = np.array([len(shapes)])
+    return cases
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--reference', default='/root/reference')
+    args = ap.parse_args()
+    tables = filter_tables(args.reference)
+    with open(os.path.join(HERE, 'pyramid_filter_tables.json'), 'w') as f:
+        json.dump(tables, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, 'atrousc_ref_cases.npz'), **atrousc_cases())
+    print('wrote', os.listdir(HERE))
+
+
+if __name__ == '__main__':
+    main()
