@@ -1,0 +1,396 @@
+"""Benchmark: NSST decompose + hard threshold + reconstruct, images/s.
+
+Default workload (N=1): a batch of 64 synthetic 512x512 images denoised in
+one batched pass per step (dcomp [3 3 4 4], dsize [32 32 16 16], maxflat
+pyramid, K = [0 3 3 3 4], sigma 20).  `value` times the batched pass with
+inputs already in HBM (CUDA events on the launching stream, L2 flushed
+between steps); `e2e` times the same pass through the public C ABI with the
+host->device copy of the inputs and the device->host copy of the outputs in
+the timed region.  Extra keys report the plain one-image-per-call path, the
+uneven 64-image batch (sizes from {256^2, 384x512, 512^2, 768x1024, 1024^2})
+and the per-stage roofline of the dominant kernel.
+
+`--impl reference` times the reference's CPU path (the FP64 oracle port of
+nsst_dec2 / nsst_HT / nsst_rec2 with the C restatement of atrousc.cpp) on the
+host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DCOMP, DSIZE, K = [3, 3, 4, 4], [32, 32, 16, 16], [0, 3, 3, 3, 4]
+H = W = 512
+BATCH = 64
+SIGMA = 20.0
+METRIC = 'NSST dec+thresh+rec images/s at 512^2 fp32, batched'
+UNIT = 'images/s'
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# --------------------------------------------------------------- CPU baseline
+def cpu_baseline(min_seconds=10.0, max_images=8):
+    """The oracle (FP64 NumPy/SciPy + C atrous restatement) on the host cores,
+    on a bounded sample of the same workload: whole 512x512 images of the
+    batch, one at a time, until min_seconds have passed."""
+    from oracle import nsst2d
+    from shearcuda_gb300.synth import noisy_image
+    cores = os.cpu_count() or 1
+    sf = nsst2d.shear_spectra(H, W, DCOMP, DSIZE)
+    scal = nsst2d.nsst_scalars(H, W, sf, seed=100, nthreads=cores)
+    n = 0
+    t0 = time.perf_counter()
+    while n < max_images:
+        _, noisy = noisy_image(H, W, SIGMA, n)
+        nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=cores)
+        n += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {'value': n / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '%d of the 512x512 images, dec+thresh+rec, filter/scalar setup excluded, %.1f s' % (n, dt)}
+
+
+def run_reference(args):
+    """Each step denoises one 512x512 image of the batch on the host cores
+    (a bounded sample of the 64-image workload); rank 0 only."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import nsst2d
+    from shearcuda_gb300.synth import noisy_image
+    cores = os.cpu_count() or 1
+    sf = nsst2d.shear_spectra(H, W, DCOMP, DSIZE)
+    scal = nsst2d.nsst_scalars(H, W, sf, seed=100, nthreads=cores)
+    steps = max(1, min(args.steps, 60))
+    for i in range(min(args.warmup, 1)):
+        _, noisy = noisy_image(H, W, SIGMA, 10000 + i)
+        nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=cores)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        _, noisy = noisy_image(H, W, SIGMA, i)
+        nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=cores)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    cb = {'value': v, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+          'sample': '%d of the 512x512 images (one per step), dec+thresh+rec in FP64, setup excluded' % steps}
+    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': world,
+            'steps': steps, 'warmup': args.warmup, 'ms_per_step': 1000.0 * dt / steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': 'reference CPU path (FP64 oracle port of nsst_dec2/nsst_HT/nsst_rec2 + atrousc '
+                                   'restatement), one 512x512 image of the 64-image batch per step',
+                       'H': H, 'W': W, 'dcomp': DCOMP, 'dsize': DSIZE, 'K': K},
+            'cpu_baseline': cb,
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- clock sampler
+class ClockSampler:
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(',')])
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
+    """Algorithmic HBM bytes of one launch of a stage over nimg images of
+    H_ x W_ (FP32 real images: 4 B/px; packed spectra: 8 B per 2 px)."""
+    N = H_ * W_
+    per = {
+        # band round trip: read the band's packed spectrum and write it back
+        'band_rows_threshold': 8 * N * nbands_dir,
+        # read the level spectrum once per band (L2-shared) + write the band
+        'band_analysis_cols': 4 * N * nbands_dir + 4 * N * nlev,
+        # read every band once, write the level sum
+        'band_synthesis_cols': 4 * N * nbands_dir + 4 * N * nlev,
+        'fft_rows_fwd': 8 * N * nlev, 'fft_cols_fwd': 8 * N * nlev, 'fft_rows_inv': 8 * N * nlev,
+    }
+    if stage.startswith('atrous_dec'):
+        return 8 * N * nimg  # read the lowpass, write one output
+    if stage.startswith('atrous_rec'):
+        return 12 * N * nimg  # read two inputs, write one output
+    b = per.get(stage, 0) * nimg
+    # spectra: read once per launch (shared by the batch) where used
+    if stage in ('band_analysis_cols', 'band_synthesis_cols'):
+        b += 4 * N * nbands_dir
+    return b
+
+
+def run_gpu(args):
+    import torch
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300.synth import noisy_image, uneven_batch, BATCH_SIZES
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    stream = torch.cuda.current_stream()
+
+    plan = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=BATCH)
+    scal = sc.nsst_scalars(plan, seed=100)  # product's Monte-Carlo scalars (setup, untimed)
+    plan.use_graphs(True)
+    host = []
+    for i in range(BATCH):
+        _, noisy = noisy_image(H, W, SIGMA, 1000 * rank + i)
+        host.append(noisy.astype(np.float32))
+    xs = [torch.tensor(h, device=dev) for h in host]
+    outs = [torch.empty_like(x) for x in xs]
+    sig = [SIGMA] * BATCH
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        sc.nsst_denoise_batch(xs, plan, sig, K, None, outs=outs)
+
+    # kernels per step: one eager pass counted by the library
+    plan.use_graphs(False)
+    c0 = sc.launch_count()
+    step()
+    kernels_per_step = sc.launch_count() - c0
+    plan.use_graphs(True)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # evict L2 between timed steps (256 MB > 129 MB L2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        times.append((e0, e1))
+    barrier()
+    clocks = sampler.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in times)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = BATCH * world * args.steps / (total_ms / 1000.0)
+
+    # ---- per-stage timing of the same batched pass (eager, events per stage)
+    plan.use_graphs(False)
+    plan.enable_timers(True)
+    stage_ms = {}
+    for _ in range(3):
+        flush.fill_(1.0)
+        step()
+        for name, ms in plan.read_timers():
+            stage_ms.setdefault(name, []).append(ms)
+    plan.enable_timers(False)
+    plan.use_graphs(True)
+    stage_avg = {k: float(np.median(v)) for k, v in stage_ms.items()}
+    dom = max(stage_avg, key=stage_avg.get)
+    peak, peak_kind = measured_peak()
+    alg = algorithmic_bytes(dom, BATCH, H, W)
+    achieved = alg / (stage_avg[dom] / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, 'profiles', 'ncu_traffic.json')
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom)
+        except ValueError:
+            traffic = None
+    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                'traffic': traffic, 'kernel': dom, 'peak_source': peak_kind,
+                'kernel_ms': stage_avg[dom], 'algorithmic_bytes_per_launch': alg,
+                'stages_ms': stage_avg}
+
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded ellipses + gradient + N(0, 20^2))',
+            'config': {'workload': 'batch of 64 x 512x512 images, one batched NSST dec+hard-thresh+rec pass per step',
+                       'H': H, 'W': W, 'batch_per_gpu': BATCH, 'dcomp': DCOMP, 'dsize': DSIZE, 'lpfilt': 'maxflat',
+                       'K': K, 'sigma': SIGMA, 'parallelism': 'replicas' if world > 1 else 'single',
+                       'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True},
+            'gpu_launches': kernels_per_step * args.steps, 'kernels_per_step': kernels_per_step,
+            'clocks': clocks, 'roofline': roofline}
+
+    if not args.no_extras:
+        # ---- e2e through the public API with host buffers
+        pin_in = [torch.from_numpy(h).pin_memory() for h in host]
+        pin_out = [torch.empty((H, W), dtype=torch.float32).pin_memory() for _ in range(BATCH)]
+        def e2e_step():
+            for p_, x_ in zip(pin_in, xs):
+                x_.copy_(p_, non_blocking=True)
+            step()
+            for o_, p_ in zip(outs, pin_out):
+                p_.copy_(o_, non_blocking=True)
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ne = max(3, args.steps // 2)
+        e0.record(stream)
+        for _ in range(ne):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / ne
+        line['e2e'] = {'value': BATCH * world / (e2e_ms / 1000.0), 'unit': UNIT,
+                       'h2d_bytes_per_step': BATCH * H * W * 4, 'd2h_bytes_per_step': BATCH * H * W * 4,
+                       'ms_per_step': e2e_ms}
+
+        # ---- plain path: one image per call through a single-image plan
+        p1 = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W)
+        p1.set_scalars(scal)
+        o1 = torch.empty_like(xs[0])
+        for _ in range(3):
+            sc.nsst_denoise(xs[0], p1, SIGMA, K, None, out=o1)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(BATCH):
+            sc.nsst_denoise(xs[i], p1, SIGMA, K, None, out=o1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain = BATCH / (e0.elapsed_time(e1) / 1000.0)
+        line['plain_images_per_s'] = plain
+        line['batched_vs_plain'] = value / world / plain
+
+        # ---- uneven batch of 64 (sizes from the batched config), one captured graph
+        items = uneven_batch(BATCH, seed=3, sizes=BATCH_SIZES)
+        counts = {}
+        for _, nz, _ in items:
+            counts[nz.shape] = counts.get(nz.shape, 0) + 1
+        plans = []
+        for shp, cnt in counts.items():
+            pp = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, shp[0], shp[1], batch=cnt)
+            sc.nsst_scalars(pp, seed=100)
+            plans.append(pp)
+        m = sc.MultiBatch(plans)
+        uxs = [torch.tensor(nz.astype(np.float32), device=dev) for _, nz, _ in items]
+        uouts = [torch.empty_like(x) for x in uxs]
+        usig = [s for _, _, s in items]
+        for _ in range(3):
+            m.denoise(uxs, usig, K, outs=uouts)
+        torch.cuda.synchronize()
+        nu = max(3, args.steps // 2)
+        ut = 0.0
+        for _ in range(nu):
+            flush.fill_(1.0)
+            e0.record(stream)
+            m.denoise(uxs, usig, K, outs=uouts)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ut += e0.elapsed_time(e1)
+        npx = sum(x.numel() for x in uxs)
+        line['uneven_b64'] = {'images_per_s': BATCH / (ut / nu / 1000.0), 'ms_per_batch': ut / nu,
+                              'megapixels': npx / 1e6, 'sizes': {'%dx%d' % k: v for k, v in counts.items()}}
+        m.close()
+        del plans
+
+    if rank == 0:
+        cb = cpu_baseline()
+        line['cpu_baseline'] = cb
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()

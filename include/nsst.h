@@ -65,6 +65,18 @@ const char* nsst_version(void);
  * and the standalone GpuShearDictionary::prepare (demo_denoise/shearcuda/gpusheardictionary.cpp:54-147). */
 nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out);
 
+/* Like nsst_plan_create, with work buffers for up to B images of this size
+ * processed together by nsst_denoise_batch (the filter spectra are shared). */
+nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, nsst_plan** out);
+
+/* Batch capacity B of a plan. */
+int nsst_plan_batch_capacity(const nsst_plan* plan);
+
+/* Replay nsst_denoise_batch's launch sequence as a CUDA graph (captured on
+ * the first call with a given set of image pointers; thresholds stay a
+ * per-call upload).  enable = 0 launches kernels one by one. */
+nsst_status nsst_plan_use_graphs(nsst_plan* plan, int enable);
+
 /* Release a plan and all its device memory.
  * Replaces clear_shearing_filters_cuda (clear_shearing_filters_cuda.cpp:51-96). */
 nsst_status nsst_plan_destroy(nsst_plan* plan);
@@ -131,6 +143,29 @@ nsst_status nsst_inverse_shear(nsst_plan* plan, const float* coeffs, float* x, v
  * shear_denoise_cuda.m:16-20 and demoImageDenoise mainwindow.cpp:221-234. */
 nsst_status nsst_denoise(nsst_plan* plan, const float* x, float* out, double sigma, const double* K,
                          const double* scalars, int mode, void* stream);
+
+/* Fused denoise of n <= B images of the plan's size in one pass: every stage
+ * is one launch over all n images; image i uses sigma[i].  x[i], out[i] are
+ * device pointers (H x W each). */
+nsst_status nsst_denoise_batch(nsst_plan* plan, const float* const* x, float* const* out, int n, const double* sigma,
+                               const double* K, const double* scalars, int mode, void* stream);
+
+/* Uneven batches: images of several sizes denoised together.  A multi object
+ * groups the items by plan (one plan per distinct size, each with enough
+ * batch capacity), runs the groups on forked streams and captures the whole
+ * batch (threshold uploads included) as one CUDA graph that is replayed while
+ * the item pointers stay the same.  Each plan must hold its scalars
+ * (nsst_plan_set_scalars or nsst_compute_scalars). */
+typedef struct nsst_item {
+  const float* x; /* device, H x W of the item's plan */
+  float* out;     /* device, H x W */
+  double sigma;
+  int plan;       /* index into the plans array */
+} nsst_item;
+typedef struct nsst_multi nsst_multi;
+nsst_status nsst_multi_create(nsst_plan* const* plans, int nplans, nsst_multi** out);
+nsst_status nsst_multi_denoise(nsst_multi* m, const nsst_item* items, int n, const double* K, int mode, void* stream);
+nsst_status nsst_multi_destroy(nsst_multi* m);
 
 /* Store per-band noise scalars in the plan (nbands doubles). */
 nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);

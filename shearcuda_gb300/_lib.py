@@ -24,6 +24,10 @@ class NsstConfig(ctypes.Structure):
                 ('pyramid', ctypes.c_int)]
 
 
+class NsstItem(ctypes.Structure):
+    _fields_ = [('x', ctypes.c_void_p), ('out', ctypes.c_void_p), ('sigma', ctypes.c_double), ('plan', ctypes.c_int)]
+
+
 class NsstError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__('%s: %s' % (STATUS_NAMES.get(status, status), msg))
@@ -39,6 +43,9 @@ SIGNATURES = [
     ('nsst_last_error', ctypes.c_char_p, []),
     ('nsst_version', ctypes.c_char_p, []),
     ('nsst_plan_create', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, ctypes.POINTER(_vp)]),
+    ('nsst_plan_create_batch', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, _ci, ctypes.POINTER(_vp)]),
+    ('nsst_plan_batch_capacity', _ci, [_vp]),
+    ('nsst_plan_use_graphs', _ci, [_vp, _ci]),
     ('nsst_plan_destroy', _ci, [_vp]),
     ('nsst_plan_num_bands', _ci, [_vp]),
     ('nsst_plan_band_levels', _ci, [_vp, _ip]),
@@ -53,6 +60,10 @@ SIGNATURES = [
     ('nsst_thresh', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _vp]),
     ('nsst_inverse_shear', _ci, [_vp, _vp, _vp, _vp]),
     ('nsst_denoise', _ci, [_vp, _vp, _vp, _cd, _dp, _dp, _ci, _vp]),
+    ('nsst_denoise_batch', _ci, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _ci, _dp, _dp, _dp, _ci, _vp]),
+    ('nsst_multi_create', _ci, [ctypes.POINTER(_vp), _ci, ctypes.POINTER(_vp)]),
+    ('nsst_multi_denoise', _ci, [_vp, ctypes.POINTER(NsstItem), _ci, _dp, _ci, _vp]),
+    ('nsst_multi_destroy', _ci, [_vp]),
     ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
     ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst_timers_enable', _ci, [_vp, _ci]),

@@ -23,7 +23,7 @@ struct RowJob {
   size_t src;    // offset (in float2) of the job's first row in the source
   size_t dst;    // offset (in float2) in the destination
   int th_index;  // index into the threshold array (threshold kernels)
-  int pad;
+  int item;      // batch item; jobs with item >= n_active are skipped
 };
 
 struct ColJob {
@@ -32,7 +32,7 @@ struct ColJob {
   size_t spec;   // offset (float2) of the band spectrum (first band for synthesis)
   size_t m0;     // offset (float2) of the column-0 side array
   int nbands;    // synthesis: number of bands summed
-  int pad;
+  int item;      // batch item; jobs with item >= n_active are skipped
 };
 
 struct AtrousJob {
@@ -84,10 +84,10 @@ int col_tile(int h);
 cudaError_t prepare_row_kernels(int wh);
 cudaError_t prepare_col_kernels(int h);
 cudaError_t prepare_atrous_kernels(int FA, int FB, int Mmax);
-cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int H, int W, const void* src_base,
+cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                         void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
                         cudaStream_t st);
-cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int H, int W, const float2* src_base,
+cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, int H, int W, const float2* src_base,
                         float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                         cudaStream_t st);
 cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,

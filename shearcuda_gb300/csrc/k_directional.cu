@@ -52,12 +52,13 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
 
 // real rows -> packed half-spectrum rows (forward R2C along W)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_fwd(const RowJob* __restrict__ jobs, const float2* src_base,
+__global__ void __launch_bounds__(kThreads) k_rows_fwd(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
                                                         float2* dst_base, const float2* __restrict__ twWh,
                                                         const float2* __restrict__ twW) {
   constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
   extern __shared__ float2 smem[];
   const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const int row0 = blockIdx.x * RS;
   const float2* src = src_base + job.src + (size_t)row0 * WH;
   for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
@@ -76,12 +77,13 @@ __global__ void __launch_bounds__(kThreads) k_rows_fwd(const RowJob* __restrict_
 
 // packed rows -> real rows (inverse C2R along W, unnormalised: x W)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_inv(const RowJob* __restrict__ jobs, const float2* src_base,
+__global__ void __launch_bounds__(kThreads) k_rows_inv(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
                                                         float2* dst_base, const float2* __restrict__ twWh,
                                                         const float2* __restrict__ twW) {
   constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
   extern __shared__ float2 smem[];
   const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const int row0 = blockIdx.x * RS;
   const float2* src = src_base + job.src + (size_t)row0 * WH;
   for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
@@ -100,13 +102,14 @@ __global__ void __launch_bounds__(kThreads) k_rows_inv(const RowJob* __restrict_
 
 // packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_thresh(const RowJob* __restrict__ jobs, const float2* src_base,
+__global__ void __launch_bounds__(kThreads) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
                                                            float2* dst_base, const float2* __restrict__ twWh,
                                                            const float2* __restrict__ twW,
                                                            const float* __restrict__ thr, int mode) {
   constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
   extern __shared__ float2 smem[];
   const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const float th = thr[job.th_index];
   const int row0 = blockIdx.x * RS;
   const float2* src = src_base + job.src + (size_t)row0 * WH;
@@ -140,11 +143,12 @@ __global__ void __launch_bounds__(kThreads) k_rows_thresh(const RowJob* __restri
 
 // plain column FFT (forward or inverse) src -> dst
 template <int H, int DIR>
-__global__ void __launch_bounds__(kThreads) k_cols(const ColJob* __restrict__ jobs, int WH, const float2* src_base,
+__global__ void __launch_bounds__(kThreads) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base,
                                                     float2* dst_base, const float2* __restrict__ twH) {
   constexpr int CS = ColCfg<H>::CS, LD = CS + 1;
   extern __shared__ float2 smem[];
   const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const int col0 = blockIdx.x * CS;
   for (int e = threadIdx.x; e < H * CS; e += kThreads) {
     int i = e / CS, s = e % CS;
@@ -160,13 +164,14 @@ __global__ void __launch_bounds__(kThreads) k_cols(const ColJob* __restrict__ jo
 
 // analysis band: dst = colIFFT( Wk .* src ), src = fully transformed level spectrum
 template <int H>
-__global__ void __launch_bounds__(kThreads) k_band_analysis(const ColJob* __restrict__ jobs, int WH,
+__global__ void __launch_bounds__(kThreads) k_band_analysis(const ColJob* __restrict__ jobs, int n_active, int WH,
                                                              const float2* src_base, float2* dst_base,
                                                              const float2* __restrict__ spec_base,
                                                              const float2* __restrict__ twH) {
   constexpr int CS = ColCfg<H>::CS, LD = CS + 1;
   extern __shared__ float2 smem[];
   const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const int col0 = blockIdx.x * CS;
   for (int e = threadIdx.x; e < H * CS; e += kThreads) {
     int i = e / CS, s = e % CS;
@@ -192,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_band_analysis(const ColJob* __rest
 // bands stored at src + k * band_stride, spectra at spec + k * band_stride,
 // side arrays at m0 + k * H.
 template <int H>
-__global__ void __launch_bounds__(kThreads) k_band_synthesis(const ColJob* __restrict__ jobs, int WH,
+__global__ void __launch_bounds__(kThreads) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active, int WH,
                                                               const float2* src_base, float2* dst_base,
                                                               const float2* __restrict__ spec_base,
                                                               size_t band_stride,
@@ -202,6 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_band_synthesis(const ColJob* __res
   static_assert(H * CS % kThreads == 0, "tile must divide evenly");
   extern __shared__ float2 smem[];
   const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
   const int col0 = blockIdx.x * CS;
   float2 acc[EPT];
 #pragma unroll
@@ -318,7 +324,7 @@ cudaError_t prepare_col_kernels(int h) {
   }
 }
 
-cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int H, int W, const void* src_base,
+cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                         void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
                         cudaStream_t st) {
   const int WH = W / 2;
@@ -332,11 +338,11 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int H, int W, c
     constexpr size_t sm = RowCfg<n>::smem();                                           \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                               \
     if (op == RowOp::Fwd)                                                              \
-      k_rows_fwd<n><<<grid, kThreads, sm, st>>>(jobs, sb, db, twWh, twW);              \
+      k_rows_fwd<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
     else if (op == RowOp::Inv)                                                         \
-      k_rows_inv<n><<<grid, kThreads, sm, st>>>(jobs, sb, db, twWh, twW);              \
+      k_rows_inv<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
     else                                                                               \
-      k_rows_thresh<n><<<grid, kThreads, sm, st>>>(jobs, sb, db, twWh, twW, thr, mode); \
+      k_rows_thresh<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
   }
     NSST_ROW_SIZES(CASE)
@@ -346,7 +352,7 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int H, int W, c
   }
 }
 
-cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int H, int W, const float2* src_base,
+cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, int H, int W, const float2* src_base,
                         float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                         cudaStream_t st) {
   const int WH = W / 2;
@@ -358,13 +364,13 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int H, int W, c
     constexpr size_t sm = ColCfg<n>::smem();                                                          \
     dim3 grid(WH / ColCfg<n>::CS, njobs);                                                             \
     if (op == ColOp::Fwd)                                                                             \
-      k_cols<n, -1><<<grid, kThreads, sm, st>>>(jobs, WH, src_base, dst_base, twH);                   \
+      k_cols<n, -1><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                   \
     else if (op == ColOp::Inv)                                                                        \
-      k_cols<n, 1><<<grid, kThreads, sm, st>>>(jobs, WH, src_base, dst_base, twH);                    \
+      k_cols<n, 1><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                    \
     else if (op == ColOp::Analysis)                                                                   \
-      k_band_analysis<n><<<grid, kThreads, sm, st>>>(jobs, WH, src_base, dst_base, spec_base, twH);   \
+      k_band_analysis<n><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base, twH);   \
     else                                                                                              \
-      k_band_synthesis<n><<<grid, kThreads, sm, st>>>(jobs, WH, src_base, dst_base, spec_base,        \
+      k_band_synthesis<n><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,        \
                                                       band_stride, twH);                              \
     return cudaGetLastError();                                                                        \
   }

@@ -46,7 +46,7 @@ using namespace nsst;
 
 struct nsst_plan {
   nsst_config cfg{};
-  int H = 0, W = 0, WH = 0, nlev = 0, nbands = 0, ndir_total = 0;
+  int H = 0, W = 0, WH = 0, nlev = 0, nbands = 0, ndir_total = 0, B = 1;
   std::vector<int> ndir, first_band, band_level;  // per level / per band
   PyramidFilters pf;
   std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1
@@ -55,35 +55,47 @@ struct nsst_plan {
   // one device arena
   char* arena = nullptr;
   size_t arena_bytes = 0;
-  // views into the arena (float2 offsets where noted)
-  float2* spec = nullptr;  // [ndir_total][H][WH] then m0 side arrays [ndir_total][H]
+  float2* spec = nullptr;  // [ndir_total][H][WH] then the column-0 side arrays [ndir_total][H]
   size_t m0_off = 0;       // offset (float2) of the side arrays from spec
   float2 *twH = nullptr, *twWh = nullptr, *twW = nullptr;
+  // per-item work buffers (item i at base + i * stride)
   float* pyr = nullptr;    // (nlev+1) x H x W   analysis pyramid
   float* tmp = nullptr;    // 2 x H x W          lowpass ping-pong
   float2* lev = nullptr;   // nlev x H x WH      level spectra
   float2* band = nullptr;  // ndir_total x H x WH band scratch
   float2* sum = nullptr;   // nlev x H x WH      synthesis sums
   float* rec = nullptr;    // (nlev+1) x H x W   synthesis pyramid inputs
-  float* th = nullptr;     // nbands thresholds
-  RowJob* jobs_rows_levels_fwd = nullptr;  // pyr[1..] -> lev
-  ColJob* jobs_cols_levels = nullptr;      // lev in place
-  ColJob* jobs_analysis = nullptr;         // lev -> band
-  RowJob* jobs_rows_bands = nullptr;       // band in place (threshold) / band -> coeffs
-  RowJob* jobs_rows_coeff_fwd = nullptr;   // coeffs -> band (src relative to the caller's buffer)
-  RowJob* jobs_rows_band_to_coeff = nullptr;  // band -> coeffs (dst relative to the caller's buffer)
-  ColJob* jobs_synthesis = nullptr;        // band -> sum
-  RowJob* jobs_rows_levels_inv = nullptr;  // sum -> rec[1..]
+  size_t s_pyr = 0, s_tmp = 0, s_lev = 0, s_band = 0, s_sum = 0, s_rec = 0;  // strides (elements)
+  float* th = nullptr;     // B x nbands thresholds
+  float* th_host = nullptr;  // pinned staging for th
+  cudaEvent_t th_done = nullptr;
+
+  RowJob* j_rows_lev_fwd = nullptr;   // pyr[1..] -> lev           (B*nlev)
+  ColJob* j_cols_lev = nullptr;       // lev in place              (B*nlev)
+  ColJob* j_analysis = nullptr;       // lev -> band, band-major   (B*ndir_total)
+  RowJob* j_rows_bands = nullptr;     // band in place, band-major (B*ndir_total)
+  ColJob* j_synthesis = nullptr;      // band -> sum, level-major  (B*nlev)
+  RowJob* j_rows_lev_inv = nullptr;   // sum -> rec[1..]           (B*nlev)
+  RowJob* j_coeff_fwd = nullptr;      // caller coeffs -> band (item 0)
+  RowJob* j_band_to_coeff = nullptr;  // band -> caller coeffs (item 0)
 
   std::vector<double> scalars;
   bool has_scalars = false;
+
+  // CUDA graph replay of the batched denoise launch sequence
+  bool use_graphs = false;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<const void*> gkey;
+  int gkey_n = -1, gkey_mode = -1;
+
   // stage timers
   bool timing = false;
-  static constexpr int kMaxStages = 32;
+  static constexpr int kMaxStages = 40;
   cudaEvent_t ev[kMaxStages + 1] = {};
   const char* stage_name[kMaxStages] = {};
   int nstage = 0;
-  std::mutex mu;  // serialises execute calls that share the plan's work buffers
+  std::mutex mu;  // serialises calls that share the plan's work buffers
 };
 
 namespace {
@@ -98,10 +110,15 @@ nsst_status cuda_fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? NSST_ERR_OUT_OF_MEMORY : NSST_ERR_CUDA;
 }
 
-#define NSST_CUDA(call)                                   \
-  do {                                                    \
-    cudaError_t _e = (call);                              \
-    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+#define NSST_CUDA(call)                                 \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+#define NSST_TRY(call)                  \
+  do {                                  \
+    nsst_status _s = (call);            \
+    if (_s != NSST_OK) return _s;       \
   } while (0)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -143,13 +160,25 @@ nsst_status validate_config(const nsst_config* cfg, int H, int W) {
   return NSST_OK;
 }
 
+void timer_begin(nsst_plan* p, cudaStream_t st) {
+  p->nstage = 0;
+  if (p->timing) cudaEventRecord(p->ev[0], st);
+}
+void timer_mark(nsst_plan* p, const char* name, cudaStream_t st) {
+  if (!p->timing || p->nstage >= nsst_plan::kMaxStages) return;
+  p->stage_name[p->nstage] = name;
+  cudaEventRecord(p->ev[++p->nstage], st);
+}
+
+bool aligned16(const void* ptr) { return ((uintptr_t)ptr & 15) == 0; }
+
 }  // namespace
 
 // ===================================================================== API
 extern "C" {
 
 const char* nsst_last_error(void) { return g_last_error.c_str(); }
-const char* nsst_version(void) { return "nsst-gb300 0.1 (sm_103a)"; }
+const char* nsst_version(void) { return "nsst-gb300 0.2 (sm_103a)"; }
 
 void nsst_debug_fail_next_alloc(int n) { g_fail_alloc_countdown.store(n); }
 
@@ -173,11 +202,11 @@ nsst_status nsst_shearing_filters(int n1, int level, double* out) {
   return NSST_OK;
 }
 
-nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out) {
+nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, nsst_plan** out) {
   if (!out) return fail(NSST_ERR_INVALID_ARG, "out is NULL");
   *out = nullptr;
-  nsst_status vs = validate_config(cfg, H, W);
-  if (vs != NSST_OK) return vs;
+  NSST_TRY(validate_config(cfg, H, W));
+  if (B < 1 || B > 4096) return fail(NSST_ERR_INVALID_ARG, "batch capacity must be in [1, 4096]");
 
   nsst_plan* p = new (std::nothrow) nsst_plan();
   if (!p) return fail(NSST_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -186,6 +215,7 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
   p->H = H;
   p->W = W;
   p->WH = W / 2;
+  p->B = B;
   p->nlev = cfg->nlevels;
   p->band_level.push_back(0);
   for (int l = 0; l < p->nlev; l++) {
@@ -220,31 +250,47 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
 
   // ---- arena layout
   const size_t HW = (size_t)H * W, HWh = (size_t)H * p->WH;
+  p->s_pyr = HW * (p->nlev + 1);
+  p->s_tmp = HW * 2;
+  p->s_lev = HWh * p->nlev;
+  p->s_band = HWh * p->ndir_total;
+  p->s_sum = HWh * p->nlev;
+  p->s_rec = HW * (p->nlev + 1);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     size_t at = off;
     off = align_up(off + bytes, 256);
     return at;
   };
+  const size_t NB = (size_t)B;
   size_t o_spec = take(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
-  size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH), o_twW = take(sizeof(float2) * p->WH);
-  size_t o_pyr = take(sizeof(float) * HW * (p->nlev + 1));
-  size_t o_tmp = take(sizeof(float) * HW * 2);
-  size_t o_lev = take(sizeof(float2) * HWh * p->nlev);
-  size_t o_band = take(sizeof(float2) * HWh * p->ndir_total);
-  size_t o_sum = take(sizeof(float2) * HWh * p->nlev);
-  size_t o_rec = take(sizeof(float) * HW * (p->nlev + 1));
-  size_t o_th = take(sizeof(float) * p->nbands);
-  size_t o_j1 = take(sizeof(RowJob) * p->nlev), o_j2 = take(sizeof(ColJob) * p->nlev);
-  size_t o_j3 = take(sizeof(ColJob) * p->ndir_total), o_j4 = take(sizeof(RowJob) * p->ndir_total);
-  size_t o_j5 = take(sizeof(RowJob) * p->ndir_total), o_j6 = take(sizeof(ColJob) * p->nlev);
-  size_t o_j7 = take(sizeof(RowJob) * p->nlev), o_j8 = take(sizeof(RowJob) * p->ndir_total);
+  size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH),
+         o_twW = take(sizeof(float2) * p->WH);
+  size_t o_pyr = take(sizeof(float) * p->s_pyr * NB);
+  size_t o_tmp = take(sizeof(float) * p->s_tmp * NB);
+  size_t o_lev = take(sizeof(float2) * p->s_lev * NB);
+  size_t o_band = take(sizeof(float2) * p->s_band * NB);
+  size_t o_sum = take(sizeof(float2) * p->s_sum * NB);
+  size_t o_rec = take(sizeof(float) * p->s_rec * NB);
+  size_t o_th = take(sizeof(float) * p->nbands * NB);
+  const size_t nL = NB * p->nlev, nD = NB * p->ndir_total;
+  size_t o_j1 = take(sizeof(RowJob) * nL), o_j2 = take(sizeof(ColJob) * nL);
+  size_t o_j3 = take(sizeof(ColJob) * nD), o_j4 = take(sizeof(RowJob) * nD);
+  size_t o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
+  size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
   p->arena_bytes = off;
   ce = dev_alloc((void**)&p->arena, p->arena_bytes);
   if (ce != cudaSuccess) {
     p->arena = nullptr;
     return destroy(cuda_fail(ce, "device allocation of the plan arena"));
   }
+  ce = cudaMallocHost((void**)&p->th_host, sizeof(float) * p->nbands * NB);
+  if (ce != cudaSuccess) {
+    p->th_host = nullptr;
+    return destroy(cuda_fail(ce, "pinned threshold staging"));
+  }
+  ce = cudaEventCreateWithFlags(&p->th_done, cudaEventDisableTiming);
+  if (ce != cudaSuccess) return destroy(cuda_fail(ce, "cudaEventCreate"));
   char* A = p->arena;
   p->spec = (float2*)(A + o_spec);
   p->m0_off = (size_t)p->ndir_total * HWh;
@@ -258,14 +304,14 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
   p->sum = (float2*)(A + o_sum);
   p->rec = (float*)(A + o_rec);
   p->th = (float*)(A + o_th);
-  p->jobs_rows_levels_fwd = (RowJob*)(A + o_j1);
-  p->jobs_cols_levels = (ColJob*)(A + o_j2);
-  p->jobs_analysis = (ColJob*)(A + o_j3);
-  p->jobs_rows_bands = (RowJob*)(A + o_j4);
-  p->jobs_rows_coeff_fwd = (RowJob*)(A + o_j5);
-  p->jobs_synthesis = (ColJob*)(A + o_j6);
-  p->jobs_rows_levels_inv = (RowJob*)(A + o_j7);
-  p->jobs_rows_band_to_coeff = (RowJob*)(A + o_j8);
+  p->j_rows_lev_fwd = (RowJob*)(A + o_j1);
+  p->j_cols_lev = (ColJob*)(A + o_j2);
+  p->j_analysis = (ColJob*)(A + o_j3);
+  p->j_rows_bands = (RowJob*)(A + o_j4);
+  p->j_synthesis = (ColJob*)(A + o_j5);
+  p->j_rows_lev_inv = (RowJob*)(A + o_j6);
+  p->j_coeff_fwd = (RowJob*)(A + o_j7);
+  p->j_band_to_coeff = (RowJob*)(A + o_j8);
 
   // ---- filter spectra (FP64 host) -> packed FP32 layout, scaled by 1/(H W)
   {
@@ -306,40 +352,53 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
   }
   // ---- static job lists (offsets in float2 units from the launch bases)
   {
-    const size_t base_pyr = (size_t)((char*)p->pyr - A) / sizeof(float2);
-    const size_t base_lev = (size_t)((char*)p->lev - A) / sizeof(float2);
-    const size_t base_band = (size_t)((char*)p->band - A) / sizeof(float2);
-    const size_t base_sum = (size_t)((char*)p->sum - A) / sizeof(float2);
-    const size_t base_rec = (size_t)((char*)p->rec - A) / sizeof(float2);
-    std::vector<RowJob> j1(p->nlev), j4(p->ndir_total), j5(p->ndir_total), j7(p->nlev), j8(p->ndir_total);
-    std::vector<ColJob> j2(p->nlev), j3(p->ndir_total), j6(p->nlev);
-    for (int l = 0; l < p->nlev; l++) {
-      j1[l] = RowJob{base_pyr + (size_t)(l + 1) * HWh, base_lev + (size_t)l * HWh, 0, 0};
-      j2[l] = ColJob{base_lev + (size_t)l * HWh, base_lev + (size_t)l * HWh, 0, 0, 0, 0};
-      j6[l] = ColJob{base_band + (size_t)p->first_band[l] * HWh, base_sum + (size_t)l * HWh,
-                     (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], 0};
-      j7[l] = RowJob{base_sum + (size_t)l * HWh, base_rec + (size_t)(l + 1) * HWh, 0, 0};
-      for (int k = 0; k < p->ndir[l]; k++) {
-        const int b = p->first_band[l] + k;
-        j3[b] = ColJob{base_lev + (size_t)l * HWh, base_band + (size_t)b * HWh, (size_t)b * HWh,
-                       p->m0_off + (size_t)b * H, 1, 0};
-        j4[b] = RowJob{base_band + (size_t)b * HWh, base_band + (size_t)b * HWh, 1 + b, 0};
-        // coefficient plane (1 + b) of the caller's buffer -> band scratch
-        j5[b] = RowJob{(size_t)(1 + b) * HWh, base_band + (size_t)b * HWh, 1 + b, 0};
-        j8[b] = RowJob{base_band + (size_t)b * HWh, (size_t)(1 + b) * HWh, 1 + b, 0};
+    auto f2 = [&](const void* ptr) { return (size_t)((const char*)ptr - A) / sizeof(float2); };
+    std::vector<RowJob> j1, j4, j6, j7, j8;
+    std::vector<ColJob> j2, j3, j5;
+    for (int i = 0; i < B; i++) {
+      const size_t pyr = f2(p->pyr + i * p->s_pyr), lev = f2(p->lev + i * p->s_lev);
+      const size_t sum = f2(p->sum + i * p->s_sum), rec = f2(p->rec + i * p->s_rec);
+      for (int l = 0; l < p->nlev; l++) {
+        j1.push_back(RowJob{pyr + (size_t)(l + 1) * HWh, lev + (size_t)l * HWh, 0, i});
+        j2.push_back(ColJob{lev + (size_t)l * HWh, lev + (size_t)l * HWh, 0, 0, 0, i});
+        j6.push_back(RowJob{sum + (size_t)l * HWh, rec + (size_t)(l + 1) * HWh, 0, i});
       }
+    }
+    // band-major over items: CTAs running together read the same spectrum tile
+    for (int b = 0; b < p->ndir_total; b++) {
+      const int l = p->band_level[1 + b] - 1;
+      for (int i = 0; i < B; i++) {
+        const size_t lev = f2(p->lev + i * p->s_lev), band = f2(p->band + i * p->s_band);
+        j3.push_back(ColJob{lev + (size_t)l * HWh, band + (size_t)b * HWh, (size_t)b * HWh,
+                            p->m0_off + (size_t)b * H, 1, i});
+        j4.push_back(RowJob{band + (size_t)b * HWh, band + (size_t)b * HWh, i * p->nbands + 1 + b, i});
+      }
+    }
+    for (int l = 0; l < p->nlev; l++) {
+      for (int i = 0; i < B; i++) {
+        const size_t band = f2(p->band + i * p->s_band), sum = f2(p->sum + i * p->s_sum);
+        j5.push_back(ColJob{band + (size_t)p->first_band[l] * HWh, sum + (size_t)l * HWh,
+                            (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l],
+                            i});
+      }
+    }
+    for (int b = 0; b < p->ndir_total; b++) {
+      const size_t band0 = f2(p->band);
+      // coefficient plane 1+b of the caller's buffer <-> band scratch of item 0
+      j7.push_back(RowJob{(size_t)(1 + b) * HWh, band0 + (size_t)b * HWh, 1 + b, 0});
+      j8.push_back(RowJob{band0 + (size_t)b * HWh, (size_t)(1 + b) * HWh, 1 + b, 0});
     }
     auto up = [&](void* dst, const void* src, size_t bytes) {
       return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
     };
-    ce = up(p->jobs_rows_levels_fwd, j1.data(), j1.size() * sizeof(RowJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_cols_levels, j2.data(), j2.size() * sizeof(ColJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_analysis, j3.data(), j3.size() * sizeof(ColJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_rows_bands, j4.data(), j4.size() * sizeof(RowJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_rows_coeff_fwd, j5.data(), j5.size() * sizeof(RowJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_synthesis, j6.data(), j6.size() * sizeof(ColJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_rows_levels_inv, j7.data(), j7.size() * sizeof(RowJob));
-    if (ce == cudaSuccess) ce = up(p->jobs_rows_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
+    ce = up(p->j_rows_lev_fwd, j1.data(), j1.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->j_cols_lev, j2.data(), j2.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->j_analysis, j3.data(), j3.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->j_rows_bands, j4.data(), j4.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->j_synthesis, j5.data(), j5.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->j_rows_lev_inv, j6.data(), j6.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->j_coeff_fwd, j7.data(), j7.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->j_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
     if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload job lists"));
   }
   ce = prepare_row_kernels(p->WH);
@@ -352,16 +411,26 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
   return NSST_OK;
 }
 
+nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out) {
+  return nsst_plan_create_batch(cfg, H, W, 1, out);
+}
+
 nsst_status nsst_plan_destroy(nsst_plan* p) {
   if (!p) return NSST_OK;
+  if (p->arena || p->th_host) cudaDeviceSynchronize();  // outstanding work may still use the buffers
   for (cudaEvent_t e : p->ev)
     if (e) cudaEventDestroy(e);
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->th_done) cudaEventDestroy(p->th_done);
+  if (p->th_host) cudaFreeHost(p->th_host);
   if (p->arena) cudaFree(p->arena);
   delete p;
   return NSST_OK;
 }
 
 int nsst_plan_num_bands(const nsst_plan* p) { return p ? p->nbands : 0; }
+int nsst_plan_batch_capacity(const nsst_plan* p) { return p ? p->B : 0; }
 
 nsst_status nsst_plan_band_levels(const nsst_plan* p, int* out) {
   if (!p || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
@@ -384,12 +453,7 @@ nsst_status nsst_level_spectra(int dsize, int dcomp, int H, int W, double* out) 
 
 nsst_status nsst_plan_level_spectra(const nsst_plan* p, int level, double* out) {
   if (!p || !out || level < 0 || level >= p->nlev) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
-  std::vector<double> w = shearing_filters_myer(p->cfg.dsize[level], p->cfg.dcomp[level]);
-  std::vector<cd> S;
-  if (!level_spectra(w, p->ndir[level], p->cfg.dsize[level], p->H, p->W, &S, host_threads()))
-    return fail(NSST_ERR_NUMERIC, "normalisation divides by zero");
-  std::memcpy(out, S.data(), S.size() * sizeof(cd));
-  return NSST_OK;
+  return nsst_level_spectra(p->cfg.dsize[level], p->cfg.dcomp[level], p->H, p->W, out);
 }
 
 nsst_status nsst_plan_set_scalars(nsst_plan* p, const double* s) {
@@ -401,86 +465,149 @@ nsst_status nsst_plan_set_scalars(nsst_plan* p, const double* s) {
   return NSST_OK;
 }
 
+nsst_status nsst_plan_use_graphs(nsst_plan* p, int enable) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (enable && !p->cap_stream) NSST_CUDA(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+  p->use_graphs = enable != 0;
+  return NSST_OK;
+}
+
 }  // extern "C"
 
 // ============================================================ stage helpers
 namespace {
 
-void timer_begin(nsst_plan* p, cudaStream_t st) {
-  p->nstage = 0;
-  if (p->timing) cudaEventRecord(p->ev[0], st);
-}
-void timer_mark(nsst_plan* p, const char* name, cudaStream_t st) {
-  if (!p->timing || p->nstage >= nsst_plan::kMaxStages) return;
-  p->stage_name[p->nstage] = name;
-  cudaEventRecord(p->ev[++p->nstage], st);
-}
-
-// atrousdec.m:19-51 on the device: x -> y[0] lowpass, y[1..nlev] bandpass coarse -> fine.
-nsst_status run_atrousdec(nsst_plan* p, const float* x, float* const* y, cudaStream_t st) {
+// atrousdec.m:19-51 on the device for n items: x[i] -> y(i, 0) lowpass,
+// y(i, 1..nlev) bandpass coarse -> fine; y(i, k) = ybase[i] + k * HW.
+nsst_status run_atrousdec(nsst_plan* p, int n, const float* const* x, float* const* ybase, float* lowpass0,
+                          cudaStream_t st) {
   const int H = p->H, W = p->W, L = p->nlev;
-  const float* cur = x;
+  const size_t HW = (size_t)H * W;
+  static const char* kHi[] = {"atrous_dec_h1_M1",  "atrous_dec_h1_M2",  "atrous_dec_h1_M4",  "atrous_dec_h1_M8",
+                              "atrous_dec_h1_M16", "atrous_dec_h1_M32", "atrous_dec_h1_M64", "atrous_dec_h1_M128"};
+  static const char* kLo[] = {"atrous_dec_h0_M1",  "atrous_dec_h0_M2",  "atrous_dec_h0_M4",  "atrous_dec_h0_M8",
+                              "atrous_dec_h0_M16", "atrous_dec_h0_M32", "atrous_dec_h0_M64", "atrous_dec_h0_M128"};
   for (int i = 0; i < L; i++) {  // i = 0 is the undilated first level
     const int M = 1 << i;
-    float* lo = (i == L - 1) ? y[0] : p->tmp + (size_t)(i & 1) * H * W;
-    AtrousJobs jl{}, jh{};
-    jl.j[0] = AtrousJob{cur, nullptr, lo, H, W};
-    jh.j[0] = AtrousJob{cur, nullptr, y[L - i], H, W};
-    static const char* kHi[] = {"atrous_dec_h1_M1", "atrous_dec_h1_M2", "atrous_dec_h1_M4", "atrous_dec_h1_M8",
-                                "atrous_dec_h1_M16", "atrous_dec_h1_M32", "atrous_dec_h1_M64", "atrous_dec_h1_M128"};
-    static const char* kLo[] = {"atrous_dec_h0_M1", "atrous_dec_h0_M2", "atrous_dec_h0_M4", "atrous_dec_h0_M8",
-                                "atrous_dec_h0_M16", "atrous_dec_h0_M32", "atrous_dec_h0_M64", "atrous_dec_h0_M128"};
-    cudaError_t e = launch_atrous(jh, 1, H, W, M, p->pf.F[1], p->hflip[1].data(), 0, nullptr, st);
-    if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+      const int cn = std::min(kMaxAtrousJobs, n - c0);
+      AtrousJobs jl{}, jh{};
+      for (int t = 0; t < cn; t++) {
+        const int it = c0 + t;
+        const float* cur = (i == 0) ? x[it] : p->tmp + it * p->s_tmp + (size_t)((i - 1) & 1) * HW;
+        float* lo = (i == L - 1) ? (lowpass0 && it == 0 ? lowpass0 : ybase[it])
+                                 : p->tmp + it * p->s_tmp + (size_t)(i & 1) * HW;
+        jl.j[t] = AtrousJob{cur, nullptr, lo, H, W};
+        jh.j[t] = AtrousJob{cur, nullptr, ybase[it] + (size_t)(L - i) * HW, H, W};
+      }
+      cudaError_t e = launch_atrous(jh, cn, H, W, M, p->pf.F[1], p->hflip[1].data(), 0, nullptr, st);
+      if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+      e = launch_atrous(jl, cn, H, W, M, p->pf.F[0], p->hflip[0].data(), 0, nullptr, st);
+      if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+    }
     timer_mark(p, kHi[i], st);
-    e = launch_atrous(jl, 1, H, W, M, p->pf.F[0], p->hflip[0].data(), 0, nullptr, st);
-    if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
     timer_mark(p, kLo[i], st);
-    cur = lo;
   }
   return NSST_OK;
 }
 
-// atrousrec.m:18-41 on the device: y[0..nlev] -> out.
-nsst_status run_atrousrec(nsst_plan* p, const float* const* y, float* out, cudaStream_t st) {
+// atrousrec.m:18-41 on the device for n items: y(i, k) = ybase[i] + k*HW,
+// except that low[i] (if given) replaces y(i, 0).
+nsst_status run_atrousrec(nsst_plan* p, int n, const float* const* ybase, const float* const* low, float* const* out,
+                          cudaStream_t st) {
   const int H = p->H, W = p->W, L = p->nlev;
-  const float* cur = y[0];
+  const size_t HW = (size_t)H * W;
+  static const char* kRec[] = {"atrous_rec_M1",  "atrous_rec_M2",  "atrous_rec_M4",  "atrous_rec_M8",
+                               "atrous_rec_M16", "atrous_rec_M32", "atrous_rec_M64", "atrous_rec_M128"};
   for (int i = L - 1; i >= 0; i--) {
     const int M = 1 << i;
-    float* dst = (i == 0) ? out : p->tmp + (size_t)(i & 1) * H * W;
-    AtrousJobs j{};
-    j.j[0] = AtrousJob{cur, y[L - i], dst, H, W};
-    static const char* kRec[] = {"atrous_rec_M1", "atrous_rec_M2", "atrous_rec_M4", "atrous_rec_M8",
-                                 "atrous_rec_M16", "atrous_rec_M32", "atrous_rec_M64", "atrous_rec_M128"};
-    cudaError_t e = launch_atrous(j, 1, H, W, M, p->pf.F[2], p->hflip[2].data(), p->pf.F[3], p->hflip[3].data(), st);
-    if (e != cudaSuccess) return cuda_fail(e, "atrous synthesis launch");
+    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+      const int cn = std::min(kMaxAtrousJobs, n - c0);
+      AtrousJobs j{};
+      for (int t = 0; t < cn; t++) {
+        const int it = c0 + t;
+        const float* cur = (i == L - 1) ? (low && low[it] ? low[it] : ybase[it])
+                                        : p->tmp + it * p->s_tmp + (size_t)((i + 1) & 1) * HW;
+        float* dst = (i == 0) ? out[it] : p->tmp + it * p->s_tmp + (size_t)(i & 1) * HW;
+        j.j[t] = AtrousJob{cur, ybase[it] + (size_t)(L - i) * HW, dst, H, W};
+      }
+      cudaError_t e =
+          launch_atrous(j, cn, H, W, M, p->pf.F[2], p->hflip[2].data(), p->pf.F[3], p->hflip[3].data(), st);
+      if (e != cudaSuccess) return cuda_fail(e, "atrous synthesis launch");
+    }
     timer_mark(p, kRec[i], st);
-    cur = dst;
   }
   return NSST_OK;
 }
 
-nsst_status upload_thresholds(nsst_plan* p, double sigma, const double* K, const double* scalars,
-                              std::vector<float>* hth, cudaStream_t st) {
-  if (!K) return fail(NSST_ERR_INVALID_ARG, "K is NULL");
+// Thresholds t[i][b] = K[level(b)] * sigma[i] * scalars[b] -> pinned staging -> device.
+nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const double* K, const double* scalars,
+                              cudaStream_t st, float* lowpass_max) {
+  if (!K || !sigma) return fail(NSST_ERR_INVALID_ARG, "K or sigma is NULL");
   if (!scalars) {
     if (!p->has_scalars) return fail(NSST_ERR_INVALID_ARG, "no scalars given and none stored in the plan");
     scalars = p->scalars.data();
   }
-  if (!std::isfinite(sigma) || sigma < 0) return fail(NSST_ERR_INVALID_ARG, "sigma must be finite and >= 0");
-  hth->resize(p->nbands);
-  for (int b = 0; b < p->nbands; b++) {
-    double k = K[p->band_level[b]];
-    double t = k * sigma * scalars[b];
-    if (!std::isfinite(t) || t < 0) return fail(NSST_ERR_INVALID_ARG, "thresholds must be finite and >= 0");
-    (*hth)[b] = (float)t;
+  // the previous call's copy must have consumed the staging buffer
+  NSST_CUDA(cudaEventSynchronize(p->th_done));
+  float lmax = 0.f;
+  for (int i = 0; i < n; i++) {
+    if (!std::isfinite(sigma[i]) || sigma[i] < 0) return fail(NSST_ERR_INVALID_ARG, "sigma must be finite and >= 0");
+    for (int b = 0; b < p->nbands; b++) {
+      double t = K[p->band_level[b]] * sigma[i] * scalars[b];
+      if (!std::isfinite(t) || t < 0) return fail(NSST_ERR_INVALID_ARG, "thresholds must be finite and >= 0");
+      p->th_host[(size_t)i * p->nbands + b] = (float)t;
+    }
+    lmax = std::max(lmax, p->th_host[(size_t)i * p->nbands]);
   }
-  cudaError_t e = cudaMemcpyAsync(p->th, hth->data(), p->nbands * sizeof(float), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(e, "upload thresholds");
+  NSST_CUDA(cudaMemcpyAsync(p->th, p->th_host, sizeof(float) * p->nbands * n, cudaMemcpyHostToDevice, st));
+  NSST_CUDA(cudaEventRecord(p->th_done, st));
+  if (lowpass_max) *lowpass_max = lmax;
   return NSST_OK;
 }
 
-bool aligned16(const void* ptr) { return ((uintptr_t)ptr & 15) == 0; }
+// The fused batched pipeline (no host work, no allocation): capturable.
+nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* const* out, int mode, bool lowpass_th,
+                            cudaStream_t st) {
+  char* A = p->arena;
+  float2* A2 = (float2*)A;
+  const int B = p->B, H = p->H, W = p->W;
+  const size_t HW = (size_t)H * W;
+  std::vector<float*> ys(n);
+  for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
+  NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
+  timer_mark(p, "fft_rows_fwd", st);
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+  timer_mark(p, "fft_cols_fwd", st);
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, p->th,
+                        mode, st));
+  timer_mark(p, "band_rows_threshold", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
+                        p->twH, st));
+  timer_mark(p, "band_synthesis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Inv, p->j_rows_lev_inv, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
+  timer_mark(p, "fft_rows_inv", st);
+  std::vector<const float*> yr(n), low(n, nullptr);
+  for (int i = 0; i < n; i++) {
+    yr[i] = p->rec + i * p->s_rec;
+    low[i] = p->pyr + i * p->s_pyr;
+  }
+  if (lowpass_th) {
+    // lowpass band: copy into rec plane 0 and threshold there (t > 0 only)
+    for (int i = 0; i < n; i++) {
+      NSST_CUDA(cudaMemcpyAsync(p->rec + i * p->s_rec, p->pyr + i * p->s_pyr, HW * sizeof(float),
+                                cudaMemcpyDeviceToDevice, st));
+      NSST_CUDA(launch_thresh_bands(p->rec + i * p->s_rec, HW, 1, p->th + (size_t)i * p->nbands, mode, st));
+      low[i] = p->rec + i * p->s_rec;
+    }
+    timer_mark(p, "lowpass_threshold", st);
+  }
+  return run_atrousrec(p, n, yr.data(), low.data(), out, st);
+}
 
 }  // namespace
 
@@ -489,19 +616,18 @@ extern "C" {
 nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
-  const size_t HW = (size_t)p->H * p->W;
-  std::vector<float*> ys(p->nlev + 1);
-  for (int i = 0; i <= p->nlev; i++) ys[i] = y + i * HW;
-  return run_atrousdec(p, x, ys.data(), (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  float* yb = y;
+  return run_atrousdec(p, 1, &x, &yb, nullptr, st);
 }
 
 nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
-  const size_t HW = (size_t)p->H * p->W;
-  std::vector<const float*> ys(p->nlev + 1);
-  for (int i = 0; i <= p->nlev; i++) ys[i] = y + i * HW;
-  return run_atrousrec(p, ys.data(), x, (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  return run_atrousrec(p, 1, &y, nullptr, &x, st);
 }
 
 nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* stream) {
@@ -509,22 +635,23 @@ nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* 
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t HW = (size_t)p->H * p->W;
-  std::vector<float*> ys(p->nlev + 1);
-  ys[0] = coeffs;  // lowpass goes straight to plane 0
-  for (int i = 1; i <= p->nlev; i++) ys[i] = p->pyr + i * HW;
-  nsst_status s = run_atrousdec(p, x, ys.data(), st);
-  if (s != NSST_OK) return s;
+  timer_begin(p, st);
   char* A = p->arena;
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_levels_fwd, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr,
-                        0, st));
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->jobs_cols_levels, p->nlev, p->H, p->W, (float2*)A, (float2*)A, nullptr, 0,
+  float2* A2 = (float2*)A;
+  float* yb = p->pyr;
+  // the lowpass goes straight to coefficient plane 0
+  NSST_TRY(run_atrousdec(p, 1, &x, &yb, coeffs, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+                        st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
+  // item-0 analysis jobs sit at stride B in the band-major list: use a per-band
+  // launch window of B jobs with n_active = 1
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, p->B * p->ndir_total, 1, p->H, p->W, A2, A2, p->spec, 0,
                         p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->jobs_analysis, p->ndir_total, p->H, p->W, (float2*)A, (float2*)A,
-                        p->spec, 0, p->twH, st));
-  // band scratch -> coefficient planes 1.. of the caller's buffer
-  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_band_to_coeff, p->ndir_total, p->H, p->W, A, coeffs, p->twWh,
-                        p->twW, nullptr, 0, st));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Inv, p->j_band_to_coeff, p->ndir_total, 1, p->H, p->W, A, coeffs, p->twWh, p->twW,
+                        nullptr, 0, st));
+  timer_mark(p, "band_rows_inv", st);
   return NSST_OK;
 }
 
@@ -534,9 +661,7 @@ nsst_status nsst_thresh(nsst_plan* p, float* coeffs, double sigma, const double*
   if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = (cudaStream_t)stream;
-  std::vector<float> hth;
-  nsst_status s = upload_thresholds(p, sigma, K, scalars, &hth, st);
-  if (s != NSST_OK) return s;
+  NSST_TRY(upload_thresholds(p, 1, &sigma, K, scalars, st, nullptr));
   NSST_CUDA(launch_thresh_bands(coeffs, (size_t)p->H * p->W, p->nbands, p->th, mode, st));
   return NSST_OK;
 }
@@ -546,66 +671,77 @@ nsst_status nsst_inverse_shear(nsst_plan* p, const float* coeffs, float* x, void
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
   char* A = p->arena;
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_coeff_fwd, p->ndir_total, p->H, p->W, coeffs, A, p->twWh, p->twW,
+  float2* A2 = (float2*)A;
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_coeff_fwd, p->ndir_total, 1, p->H, p->W, coeffs, A, p->twWh, p->twW,
                         nullptr, 0, st));
-  NSST_CUDA(launch_cols(ColOp::Synthesis, p->jobs_synthesis, p->nlev, p->H, p->W, (float2*)A, (float2*)A, p->spec,
+  timer_mark(p, "band_rows_fwd", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, 1, p->H, p->W, A2, A2, p->spec,
                         (size_t)p->H * p->WH, p->twH, st));
-  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_levels_inv, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+  timer_mark(p, "band_synthesis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Inv, p->j_rows_lev_inv, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
                         st));
-  const size_t HW = (size_t)p->H * p->W;
-  std::vector<const float*> ys(p->nlev + 1);
-  ys[0] = coeffs;
-  for (int i = 1; i <= p->nlev; i++) ys[i] = p->rec + i * HW;
-  return run_atrousrec(p, ys.data(), x, st);
+  timer_mark(p, "fft_rows_inv", st);
+  const float* yr = p->rec;
+  return run_atrousrec(p, 1, &yr, &coeffs, &x, st);
+}
+
+nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const* out, int n, const double* sigma,
+                               const double* K, const double* scalars, int mode, void* stream) {
+  if (!p || !x || !out || !sigma) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  for (int i = 0; i < n; i++)
+    if (!x[i] || !out[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  float lmax = 0.f;
+  NSST_TRY(upload_thresholds(p, n, sigma, K, scalars, st, &lmax));
+  const bool lowpass_th = lmax > 0.f;
+  if (!p->use_graphs || p->timing) {
+    timer_begin(p, st);
+    return enqueue_denoise(p, n, x, out, mode, lowpass_th, st);
+  }
+  // graph replay: the launch sequence depends only on (n, pointers, mode, lowpass_th)
+  std::vector<const void*> key;
+  for (int i = 0; i < n; i++) {
+    key.push_back(x[i]);
+    key.push_back(out[i]);
+  }
+  const int kmode = mode * 2 + (lowpass_th ? 1 : 0);
+  if (!p->gexec || n != p->gkey_n || kmode != p->gkey_mode || key != p->gkey) {
+    if (p->gexec) {
+      cudaGraphExecDestroy(p->gexec);
+      p->gexec = nullptr;
+    }
+    NSST_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+    nsst_status s = enqueue_denoise(p, n, x, out, mode, lowpass_th, p->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(p->cap_stream, &g);
+    if (s != NSST_OK) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&p->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      p->gexec = nullptr;
+      return cuda_fail(ce, "cudaGraphInstantiate");
+    }
+    p->gkey = key;
+    p->gkey_n = n;
+    p->gkey_mode = kmode;
+  }
+  count_launch(0);
+  NSST_CUDA(cudaGraphLaunch(p->gexec, st));
+  return NSST_OK;
 }
 
 nsst_status nsst_denoise(nsst_plan* p, const float* x, float* out, double sigma, const double* K,
                          const double* scalars, int mode, void* stream) {
-  if (!p || !x || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
-  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
-  std::lock_guard<std::mutex> lk(p->mu);
-  cudaStream_t st = (cudaStream_t)stream;
-  std::vector<float> hth;
-  nsst_status s = upload_thresholds(p, sigma, K, scalars, &hth, st);
-  if (s != NSST_OK) return s;
-  timer_begin(p, st);
-  const size_t HW = (size_t)p->H * p->W;
-  std::vector<float*> ys(p->nlev + 1);
-  for (int i = 0; i <= p->nlev; i++) ys[i] = p->pyr + i * HW;
-  s = run_atrousdec(p, x, ys.data(), st);
-  if (s != NSST_OK) return s;
-  char* A = p->arena;
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->jobs_rows_levels_fwd, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr,
-                        0, st));
-  timer_mark(p, "fft_rows_fwd", st);
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->jobs_cols_levels, p->nlev, p->H, p->W, (float2*)A, (float2*)A, nullptr, 0,
-                        p->twH, st));
-  timer_mark(p, "fft_cols_fwd", st);
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->jobs_analysis, p->ndir_total, p->H, p->W, (float2*)A, (float2*)A,
-                        p->spec, 0, p->twH, st));
-  timer_mark(p, "band_analysis_cols", st);
-  NSST_CUDA(launch_rows(RowOp::Thresh, p->jobs_rows_bands, p->ndir_total, p->H, p->W, A, A, p->twWh, p->twW, p->th,
-                        mode, st));
-  timer_mark(p, "band_rows_threshold", st);
-  NSST_CUDA(launch_cols(ColOp::Synthesis, p->jobs_synthesis, p->nlev, p->H, p->W, (float2*)A, (float2*)A, p->spec,
-                        (size_t)p->H * p->WH, p->twH, st));
-  timer_mark(p, "band_synthesis_cols", st);
-  NSST_CUDA(launch_rows(RowOp::Inv, p->jobs_rows_levels_inv, p->nlev, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
-                        st));
-  timer_mark(p, "fft_rows_inv", st);
-  // lowpass band: threshold only when it can change anything (t > 0)
-  const float* low = p->pyr;
-  if (hth[0] > 0.0f) {
-    NSST_CUDA(cudaMemcpyAsync(p->rec, p->pyr, HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    NSST_CUDA(launch_thresh_bands(p->rec, HW, 1, p->th, mode, st));
-    low = p->rec;
-    timer_mark(p, "lowpass_threshold", st);
-  }
-  std::vector<const float*> yr(p->nlev + 1);
-  yr[0] = low;
-  for (int i = 1; i <= p->nlev; i++) yr[i] = p->rec + i * HW;
-  return run_atrousrec(p, yr.data(), out, st);
+  return nsst_denoise_batch(p, &x, &out, 1, &sigma, K, scalars, mode, stream);
 }
 
 nsst_status nsst_timers_enable(nsst_plan* p, int enable) {
@@ -697,6 +833,158 @@ nsst_status nsst_compute_scalars(nsst_plan* p, uint64_t seed, double* out) {
   p->scalars = sc;
   p->has_scalars = true;
   if (out) std::copy(sc.begin(), sc.end(), out);
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+// ============================================================ uneven batches
+struct nsst_multi {
+  std::vector<nsst_plan*> plans;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> done;
+  cudaStream_t cap = nullptr;
+  cudaEvent_t fork = nullptr, finished = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void*> key;
+  int key_mode = -1;
+  std::mutex mu;
+};
+
+extern "C" {
+
+nsst_status nsst_multi_create(nsst_plan* const* plans, int nplans, nsst_multi** out) {
+  if (!plans || nplans < 1 || !out) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
+  *out = nullptr;
+  nsst_multi* m = new (std::nothrow) nsst_multi();
+  if (!m) return fail(NSST_ERR_OUT_OF_MEMORY, "host allocation failed");
+  m->plans.assign(plans, plans + nplans);
+  for (nsst_plan* p : m->plans)
+    if (!p) {
+      delete m;
+      return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+    }
+  cudaError_t e = cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->finished, cudaEventDisableTiming);
+  for (int i = 0; i < nplans && e == cudaSuccess; i++) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t d = nullptr;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d, cudaEventDisableTiming);
+    m->streams.push_back(s);
+    m->done.push_back(d);
+  }
+  if (e != cudaSuccess) {
+    nsst_multi_destroy(m);
+    return cuda_fail(e, "multi streams");
+  }
+  *out = m;
+  return NSST_OK;
+}
+
+nsst_status nsst_multi_destroy(nsst_multi* m) {
+  if (!m) return NSST_OK;
+  cudaDeviceSynchronize();
+  if (m->exec) cudaGraphExecDestroy(m->exec);
+  for (cudaStream_t s : m->streams)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t d : m->done)
+    if (d) cudaEventDestroy(d);
+  if (m->cap) cudaStreamDestroy(m->cap);
+  if (m->fork) cudaEventDestroy(m->fork);
+  if (m->finished) cudaEventDestroy(m->finished);
+  delete m;
+  return NSST_OK;
+}
+
+nsst_status nsst_multi_denoise(nsst_multi* m, const nsst_item* items, int n, const double* K, int mode,
+                               void* stream) {
+  if (!m || !items || n < 1 || !K) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  std::lock_guard<std::mutex> lk(m->mu);
+  const int np = (int)m->plans.size();
+  std::vector<std::vector<int>> groups(np);
+  for (int i = 0; i < n; i++) {
+    if (items[i].plan < 0 || items[i].plan >= np || !items[i].x || !items[i].out)
+      return fail(NSST_ERR_INVALID_ARG, "bad item");
+    groups[items[i].plan].push_back(i);
+  }
+  for (int g = 0; g < np; g++) {
+    if ((int)groups[g].size() > m->plans[g]->B) return fail(NSST_ERR_INVALID_ARG, "group exceeds plan capacity");
+    if (!groups[g].empty() && !m->plans[g]->has_scalars)
+      return fail(NSST_ERR_INVALID_ARG, "plan without stored scalars");
+  }
+  // thresholds into every plan's pinned staging; the previous replay must be done with them
+  NSST_CUDA(cudaEventSynchronize(m->finished));
+  std::vector<char> lowth(np, 0);
+  for (int g = 0; g < np; g++) {
+    nsst_plan* p = m->plans[g];
+    for (size_t t = 0; t < groups[g].size(); t++) {
+      const double sg = items[groups[g][t]].sigma;
+      if (!std::isfinite(sg) || sg < 0) return fail(NSST_ERR_INVALID_ARG, "sigma must be finite and >= 0");
+      for (int b = 0; b < p->nbands; b++) {
+        double th = K[p->band_level[b]] * sg * p->scalars[b];
+        if (!std::isfinite(th) || th < 0) return fail(NSST_ERR_INVALID_ARG, "thresholds must be finite and >= 0");
+        p->th_host[t * p->nbands + b] = (float)th;
+      }
+      if (p->th_host[t * p->nbands] > 0.f) lowth[g] = 1;
+    }
+  }
+  std::vector<const void*> key;
+  for (int i = 0; i < n; i++) {
+    key.push_back(items[i].x);
+    key.push_back(items[i].out);
+    key.push_back((const void*)(intptr_t)items[i].plan);
+  }
+  for (int g = 0; g < np; g++) key.push_back((const void*)(intptr_t)lowth[g]);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!m->exec || key != m->key || mode != m->key_mode) {
+    if (m->exec) {
+      cudaGraphExecDestroy(m->exec);
+      m->exec = nullptr;
+    }
+    NSST_CUDA(cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal));
+    nsst_status s = NSST_OK;
+    cudaError_t ce = cudaEventRecord(m->fork, m->cap);
+    for (int g = 0; g < np && s == NSST_OK && ce == cudaSuccess; g++) {
+      if (groups[g].empty()) continue;
+      nsst_plan* p = m->plans[g];
+      std::lock_guard<std::mutex> plk(p->mu);
+      ce = cudaStreamWaitEvent(m->streams[g], m->fork, 0);
+      if (ce != cudaSuccess) break;
+      const int cnt = (int)groups[g].size();
+      ce = cudaMemcpyAsync(p->th, p->th_host, sizeof(float) * p->nbands * cnt, cudaMemcpyHostToDevice,
+                           m->streams[g]);
+      if (ce != cudaSuccess) break;
+      std::vector<const float*> xs(cnt);
+      std::vector<float*> os(cnt);
+      for (int t = 0; t < cnt; t++) {
+        xs[t] = items[groups[g][t]].x;
+        os[t] = items[groups[g][t]].out;
+      }
+      s = enqueue_denoise(p, cnt, xs.data(), os.data(), mode, lowth[g] != 0, m->streams[g]);
+      if (s == NSST_OK) ce = cudaEventRecord(m->done[g], m->streams[g]);
+      if (ce == cudaSuccess && s == NSST_OK) ce = cudaStreamWaitEvent(m->cap, m->done[g], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce2 = cudaStreamEndCapture(m->cap, &graph);
+    if (s != NSST_OK || ce != cudaSuccess || ce2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      if (s != NSST_OK) return s;
+      return cuda_fail(ce != cudaSuccess ? ce : ce2, "multi capture");
+    }
+    ce = cudaGraphInstantiate(&m->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      m->exec = nullptr;
+      return cuda_fail(ce, "cudaGraphInstantiate");
+    }
+    m->key = key;
+    m->key_mode = mode;
+  }
+  NSST_CUDA(cudaGraphLaunch(m->exec, st));
+  NSST_CUDA(cudaEventRecord(m->finished, st));
   return NSST_OK;
 }
 

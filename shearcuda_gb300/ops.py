@@ -28,11 +28,12 @@ import ctypes
 import numpy as np
 import torch
 
-from ._lib import (NsstConfig, NsstError, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, check, lib)
+from ._lib import (NsstConfig, NsstError, NsstItem, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, check, lib)
 
 __all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters_cuda', 'shear_trans_cuda',
            'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'nsst_scalars',
-           'nsst_denoise', 'pyramid_filters', 'shearing_filters', 'level_spectra', 'launch_count', 'NsstError']
+           'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
+           'level_spectra', 'launch_count', 'NsstError']
 
 
 def _dptr(a):
@@ -59,7 +60,7 @@ class ShearPlan:
     prepare_shearing_filters_cuda returns): filter spectra, pyramid filters
     and work buffers for one image size."""
 
-    def __init__(self, dcomp, dsize, H, W, lpfilt='maxflat', pyramid=PYRAMID_AUTO):
+    def __init__(self, dcomp, dsize, H, W, lpfilt='maxflat', pyramid=PYRAMID_AUTO, batch=1):
         if len(dcomp) != len(dsize):
             raise NsstError(1, 'dcomp and dsize must have the same length')
         cfg = NsstConfig()
@@ -70,7 +71,7 @@ class ShearPlan:
         cfg.lpfilt = lpfilt.encode()
         cfg.pyramid = pyramid
         h = ctypes.c_void_p()
-        check(lib().nsst_plan_create(ctypes.byref(cfg), int(H), int(W), ctypes.byref(h)))
+        check(lib().nsst_plan_create_batch(ctypes.byref(cfg), int(H), int(W), int(batch), ctypes.byref(h)))
         self._h = h
         self.dcomp, self.dsize, self.H, self.W, self.lpfilt = list(dcomp), list(dsize), int(H), int(W), lpfilt
         self.nlevels = len(dcomp)
@@ -78,6 +79,10 @@ class ShearPlan:
         lv = (ctypes.c_int * self.nbands)()
         check(lib().nsst_plan_band_levels(h, lv))
         self.band_levels = list(lv)
+        self.batch = lib().nsst_plan_batch_capacity(h)
+
+    def use_graphs(self, on=True):
+        check(lib().nsst_plan_use_graphs(self.handle, 1 if on else 0))
 
     @property
     def handle(self):
@@ -152,8 +157,8 @@ def _kvec(plan, K):
     return K
 
 
-def prepare_shearing_filters_cuda(dcomp, dsize, H, W=None, lpfilt='maxflat', pyramid=PYRAMID_AUTO):
-    return ShearPlan(dcomp, dsize, H, H if W is None else W, lpfilt, pyramid)
+def prepare_shearing_filters_cuda(dcomp, dsize, H, W=None, lpfilt='maxflat', pyramid=PYRAMID_AUTO, batch=1):
+    return ShearPlan(dcomp, dsize, H, H if W is None else W, lpfilt, pyramid, batch)
 
 
 def clear_shearing_filters_cuda(shear):
@@ -222,6 +227,72 @@ def nsst_denoise(x, shear, sigma, K, scalars=None, mode=THRESH_HARD, out=None, s
     check(lib().nsst_denoise(shear.handle, _dev(x, 'x', (shear.H, shear.W)), _dev(out, 'out', (shear.H, shear.W)),
                              float(sigma), _dptr(K), sp, mode, _stream(stream)))
     return out
+
+
+def _ptr_array(ts, name, shape):
+    arr = (ctypes.c_void_p * len(ts))()
+    for i, t in enumerate(ts):
+        arr[i] = _dev(t, '%s[%d]' % (name, i), shape).value
+    return arr
+
+
+def nsst_denoise_batch(xs, shear, sigmas, K, scalars=None, mode=THRESH_HARD, outs=None, stream=None):
+    """Denoise a list of same-size images in one batched pass."""
+    n = len(xs)
+    if outs is None:
+        outs = [torch.empty_like(x) for x in xs]
+    K = _kvec(shear, K)
+    sg = np.ascontiguousarray(np.broadcast_to(np.asarray(sigmas, np.float64), (n,)))
+    sp = None
+    if scalars is not None:
+        s = np.ascontiguousarray(flatten_scalars(scalars), dtype=np.float64)
+        if s.size != shear.nbands:
+            raise NsstError(1, 'need %d scalars' % shear.nbands)
+        sp = _dptr(s)
+    check(lib().nsst_denoise_batch(shear.handle, _ptr_array(xs, 'x', (shear.H, shear.W)),
+                                   _ptr_array(outs, 'out', (shear.H, shear.W)), n, _dptr(sg), _dptr(K), sp, mode,
+                                   _stream(stream)))
+    return outs
+
+
+class MultiBatch:
+    """Uneven batch over several plans (one per image size), replayed as one CUDA graph."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        arr = (ctypes.c_void_p * len(self.plans))(*[p.handle.value for p in self.plans])
+        h = ctypes.c_void_p()
+        check(lib().nsst_multi_create(arr, len(self.plans), ctypes.byref(h)))
+        self._h = h
+        self._index = {(p.H, p.W): i for i, p in enumerate(self.plans)}
+
+    def denoise(self, xs, sigmas, K, mode=THRESH_HARD, outs=None, stream=None):
+        n = len(xs)
+        if outs is None:
+            outs = [torch.empty_like(x) for x in xs]
+        items = (NsstItem * n)()
+        for i, (x, o, s) in enumerate(zip(xs, outs, sigmas)):
+            pi = self._index.get(tuple(x.shape))
+            if pi is None:
+                raise NsstError(1, 'no plan for image size %s' % (tuple(x.shape),))
+            items[i].x = _dev(x, 'x').value
+            items[i].out = _dev(o, 'out', tuple(x.shape)).value
+            items[i].sigma = float(s)
+            items[i].plan = pi
+        K = _kvec(self.plans[0], K)
+        check(lib().nsst_multi_denoise(self._h, items, n, _dptr(K), mode, _stream(stream)))
+        return outs
+
+    def close(self):
+        if self._h is not None:
+            lib().nsst_multi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def launch_count():
