@@ -492,21 +492,29 @@ nsst_status run_atrousdec(nsst_plan* p, int n, const float* const* x, float* con
     const int M = 1 << i;
     for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
       const int cn = std::min(kMaxAtrousJobs, n - c0);
-      AtrousJobs jl{}, jh{};
+      AtrousJobs jh{};
+      for (int t = 0; t < cn; t++) {
+        const int it = c0 + t;
+        const float* cur = (i == 0) ? x[it] : p->tmp + it * p->s_tmp + (size_t)((i - 1) & 1) * HW;
+        jh.j[t] = AtrousJob{cur, nullptr, ybase[it] + (size_t)(L - i) * HW, H, W};
+      }
+      cudaError_t e = launch_atrous(jh, cn, H, W, M, p->pf.F[1], p->hflip[1].data(), 0, nullptr, st);
+      if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
+    }
+    timer_mark(p, kHi[i], st);
+    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+      const int cn = std::min(kMaxAtrousJobs, n - c0);
+      AtrousJobs jl{};
       for (int t = 0; t < cn; t++) {
         const int it = c0 + t;
         const float* cur = (i == 0) ? x[it] : p->tmp + it * p->s_tmp + (size_t)((i - 1) & 1) * HW;
         float* lo = (i == L - 1) ? (lowpass0 && it == 0 ? lowpass0 : ybase[it])
                                  : p->tmp + it * p->s_tmp + (size_t)(i & 1) * HW;
         jl.j[t] = AtrousJob{cur, nullptr, lo, H, W};
-        jh.j[t] = AtrousJob{cur, nullptr, ybase[it] + (size_t)(L - i) * HW, H, W};
       }
-      cudaError_t e = launch_atrous(jh, cn, H, W, M, p->pf.F[1], p->hflip[1].data(), 0, nullptr, st);
-      if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
-      e = launch_atrous(jl, cn, H, W, M, p->pf.F[0], p->hflip[0].data(), 0, nullptr, st);
+      cudaError_t e = launch_atrous(jl, cn, H, W, M, p->pf.F[0], p->hflip[0].data(), 0, nullptr, st);
       if (e != cudaSuccess) return cuda_fail(e, "atrous analysis launch");
     }
-    timer_mark(p, kHi[i], st);
     timer_mark(p, kLo[i], st);
   }
   return NSST_OK;
