@@ -20,6 +20,8 @@
 // is a neighbouring tile row.  Each thread keeps 16 vertically adjacent
 // outputs in registers and streams one tap column at a time: 16+F-1 shared
 // loads feed 16*F FMAs.
+#include <mutex>
+
 #include "internal.h"
 
 namespace nsst {
@@ -123,10 +125,23 @@ static size_t atrous_smem_pair(int M) {
   return sm;
 }
 
+// The shared-memory opt-in only ever grows: plans (and the no-allocation
+// entry point) with different pyramid depths share these kernels.
 template <int FA, int FB>
 static cudaError_t prepare_atrous_t(int Mmax) {
-  return cudaFuncSetAttribute(k_atrous<FA, FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)atrous_smem_pair<FA, FB>(Mmax));
+  constexpr int kDevs = 64;
+  static std::mutex mu;
+  static size_t configured[kDevs] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const size_t want = atrous_smem_pair<FA, FB>(Mmax);
+  if (want > 227 * 1024) return cudaErrorInvalidValue;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev >= 0 && dev < kDevs && configured[dev] >= want) return cudaSuccess;
+  e = cudaFuncSetAttribute(k_atrous<FA, FB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+  if (e == cudaSuccess && dev >= 0 && dev < kDevs) configured[dev] = want;
+  return e;
 }
 
 template <int FA, int FB>

@@ -137,8 +137,9 @@ int host_threads() {
 
 nsst_status validate_config(const nsst_config* cfg, int H, int W) {
   if (!cfg) return fail(NSST_ERR_INVALID_ARG, "config is NULL");
-  if (cfg->nlevels < 1 || cfg->nlevels > NSST_MAX_LEVELS)
-    return fail(NSST_ERR_INVALID_ARG, "nlevels must be in [1, 8]");
+  // the dilated direct convolution stages a (64 + 2^(L-1)(F-1))-wide halo
+  // tile in shared memory, which bounds the depth at 6 levels
+  if (cfg->nlevels < 1 || cfg->nlevels > 6) return fail(NSST_ERR_INVALID_ARG, "nlevels must be in [1, 6]");
   int nb = 1;
   for (int i = 0; i < cfg->nlevels; i++) {
     if (cfg->dcomp[i] < 0 || cfg->dcomp[i] > 6) return fail(NSST_ERR_INVALID_ARG, "dcomp must be in [0, 6]");
