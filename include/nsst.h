@@ -117,6 +117,25 @@ nsst_status nsst_atrousdec(nsst_plan* plan, const float* x, float* y, void* stre
  * Replaces atrousrec (atrousrec.cpp:42-132; atrousrec.m:18-41). */
 nsst_status nsst_atrousrec(nsst_plan* plan, const float* y, float* x, void* stream);
 
+/* À trous analysis without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc — a MEX host
+ * whose GPU array runtime already owns the device memory, a process under a
+ * fixed device-memory budget, or a real-time loop that cannot pay cudaMalloc's
+ * implicit device synchronisation.  Same result as nsst_atrousdec for the
+ * pyramid filter `lpfilt` (NULL = "maxflat") and `nlevels` (1..6) levels, but
+ * no plan is needed: the caller passes x (H x W) and y ((nlevels+1) x H x W,
+ * plane 0 lowpass, then bandpass coarse -> fine), both device pointers, and
+ * the one scratch image the lowpass chain needs lives in a static device array
+ * of 2048*2048 floats (16 MiB) that every GPU loading the library holds until
+ * exit.  H*W above 2048*2048 is rejected with NSST_ERR_UNSUPPORTED_SIZE.
+ * The first call on a device does a one-time set-up for that device (the
+ * array's device address, kernel shared-memory limits); make that first call
+ * before any stream capture.  All calls share the one array and it keeps the
+ * last call's contents (nothing in it needs to start at zero): calls that
+ * overlap on the GPU — on different streams or threads — race. */
+nsst_status nsst_atrousdec_noalloc(const float* x, float* y, int H, int W, int nlevels, const char* lpfilt,
+                                   void* stream);
+
 /* Forward NSST: x (H x W, device) -> coeffs (nbands x H x W, device).
  * Replaces shear_trans_cuda (shear_trans_cuda.cpp:56-287) and
  * Shearcuda::shearTrans (demo_denoise/shearcuda/shearcuda.cpp:273-318). */

@@ -56,6 +56,7 @@ SIGNATURES = [
     ('nsst_plan_level_spectra', _ci, [_vp, _ci, _dp]),
     ('nsst_atrousdec', _ci, [_vp, _vp, _vp, _vp]),
     ('nsst_atrousrec', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_atrousdec_noalloc', _ci, [_vp, _vp, _ci, _ci, _ci, ctypes.c_char_p, _vp]),
     ('nsst_shear_trans', _ci, [_vp, _vp, _vp, _vp]),
     ('nsst_thresh', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _vp]),
     ('nsst_inverse_shear', _ci, [_vp, _vp, _vp, _vp]),

@@ -31,7 +31,8 @@ import torch
 from ._lib import (NsstConfig, NsstError, NsstItem, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, check, lib)
 
 __all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters_cuda', 'shear_trans_cuda',
-           'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'nsst_scalars',
+           'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'atrousdec_noalloc',
+           'nsst_scalars',
            'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
            'level_spectra', 'launch_count', 'NsstError']
 
@@ -176,6 +177,17 @@ def atrousrec(y, shear, stream=None):
     check(lib().nsst_atrousrec(shear.handle, _dev(y, 'y', (shear.nlevels + 1, shear.H, shear.W)), _dev(x, 'x'),
                                _stream(stream)))
     return x
+
+
+def atrousdec_noalloc(x, nlevels, y, lpfilt='maxflat', stream=None):
+    """À trous analysis through the entry point that allocates no device
+    memory (for callers that cannot call cudaMalloc): ``y`` must be a
+    preallocated (nlevels+1, H, W) CUDA float32 tensor; at most 2048*2048
+    pixels; calls overlapping on the GPU race on the library's one scratch image."""
+    H, W = x.shape
+    check(lib().nsst_atrousdec_noalloc(_dev(x, 'x'), _dev(y, 'y', (nlevels + 1, H, W)), H, W, nlevels,
+                                       lpfilt.encode(), _stream(stream)))
+    return y
 
 
 def shear_trans_cuda(x, lpfilt, shear, coeff=None, stream=None):
