@@ -286,4 +286,103 @@ __device__ __forceinline__ void c2r_pre(float2* buf, const float2* __restrict__ 
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Ping-pong variant: each pass reads buffer `in` and writes buffer `out`, so a
+// thread only holds one butterfly's R values at a time (low register use) and
+// a pass needs a single barrier.  Returns the buffer that holds the result.
+// Both buffers use the [index][sequence] layout with leading dimension LD.
+// ---------------------------------------------------------------------------
+template <int N, int NSEQ, int LD, int T, int R, int NS, int DIR>
+__device__ __forceinline__ void stockham_pp(const float2* __restrict__ in, float2* __restrict__ out,
+                                            const float2* __restrict__ tw) {
+  constexpr int NB = N / R;
+  constexpr int TOTAL = NB * NSEQ;
+  constexpr int STEP = N / (NS * R);
+#pragma unroll 2
+  for (int w = threadIdx.x; w < TOTAL; w += T) {
+    const int s = w % NSEQ;
+    const int j = w / NSEQ;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = in[(j + r * NB) * LD + s];
+    const int k = j % NS;
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        float2 t = __ldg(&tw[r * k * STEP]);
+        v[r] = DIR < 0 ? cmul(v[r], t) : cmulc(v[r], t);
+      }
+    }
+    Dft<R, DIR>::run(v);
+    const int base = (j / NS) * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) out[(base + r * NS) * LD + s] = v[r];
+  }
+  __syncthreads();
+}
+
+template <int N, int NSEQ, int LD, int T, int DIR, int NS>
+__device__ __forceinline__ float2* fft_pp_passes(float2* a, float2* b, const float2* __restrict__ tw, RadixList<>) {
+  return a;
+}
+
+template <int N, int NSEQ, int LD, int T, int DIR, int NS, int R, int... Rest>
+__device__ __forceinline__ float2* fft_pp_passes(float2* a, float2* b, const float2* __restrict__ tw,
+                                                 RadixList<R, Rest...>) {
+  stockham_pp<N, NSEQ, LD, T, R, NS, DIR>(a, b, tw);
+  return fft_pp_passes<N, NSEQ, LD, T, DIR, NS * R>(b, a, tw, RadixList<Rest...>{});
+}
+
+// FFT of the data in `a` using `b` as the second buffer; returns a or b.
+template <int N, int NSEQ, int LD, int T, int DIR>
+__device__ __forceinline__ float2* block_fft_pp(float2* a, float2* b, const float2* __restrict__ tw) {
+  return fft_pp_passes<N, NSEQ, LD, T, DIR, 1>(a, b, tw, typename FftPlan<N>::type{});
+}
+
+// Out-of-place packed-real post-processing (after a forward FFT of the
+// W/2-point complex view); see r2c_post for the formulas.
+template <int WH, int NSEQ, int LD, int T>
+__device__ __forceinline__ void r2c_post_pp(const float2* __restrict__ in, float2* __restrict__ out,
+                                            const float2* __restrict__ twW) {
+  constexpr int TOTAL = (WH / 2 + 1) * NSEQ;
+  for (int w = threadIdx.x; w < TOTAL; w += T) {
+    const int s = w % NSEQ, k = w / NSEQ;
+    const float2 zk = in[k * LD + s];
+    if (k == 0) {
+      out[s] = make_float2(zk.x + zk.y, zk.x - zk.y);
+    } else {
+      const float2 zmc = cconj(in[(WH - k) * LD + s]);
+      const float2 E = cscale(cadd(zk, zmc), 0.5f);
+      const float2 d = cscale(csub(zk, zmc), 0.5f);
+      const float2 O = make_float2(d.y, -d.x);
+      const float2 To = cmul(__ldg(&twW[k]), O);
+      out[k * LD + s] = cadd(E, To);
+      if (k != WH - k) out[(WH - k) * LD + s] = cconj(csub(E, To));
+    }
+  }
+  __syncthreads();
+}
+
+// Out-of-place packed-real pre-processing (before an inverse FFT); see c2r_pre.
+template <int WH, int NSEQ, int LD, int T>
+__device__ __forceinline__ void c2r_pre_pp(const float2* __restrict__ in, float2* __restrict__ out,
+                                           const float2* __restrict__ twW) {
+  constexpr int TOTAL = (WH / 2 + 1) * NSEQ;
+  for (int w = threadIdx.x; w < TOTAL; w += T) {
+    const int s = w % NSEQ, k = w / NSEQ;
+    const float2 xk = in[k * LD + s];
+    if (k == 0) {
+      out[s] = make_float2(xk.x + xk.y, xk.x - xk.y);
+    } else {
+      const float2 xmc = cconj(in[(WH - k) * LD + s]);
+      const float2 E = cadd(xk, xmc);
+      const float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));
+      const float2 iO = make_float2(-O.y, O.x);
+      out[k * LD + s] = cadd(E, iO);
+      if (k != WH - k) out[(WH - k) * LD + s] = cconj(csub(E, iO));
+    }
+  }
+  __syncthreads();
+}
+
 }  // namespace nsst

@@ -27,17 +27,31 @@
 
 namespace nsst {
 
-constexpr int kThreads = 256;
-
+// Tile shapes: a row CTA owns RS rows, a column CTA owns CS columns, each as two
+// ping-pong shared buffers [index][sequence] with one float2 of padding per
+// index.  They keep a thread's share of a tile at <= 16 complex values and the
+// shared memory low enough for 2-3 resident CTAs per SM: the kernels are bound
+// by global-memory latency, so resident CTAs are what hides it.
 template <int N>
 struct RowCfg {  // N = W/2 complex points per row
-  static constexpr int RS = N >= 1024 ? 8 : 16;
-  static constexpr size_t smem() { return (size_t)N * (RS + 1) * sizeof(float2); }
+  static constexpr int RS = N >= 1024 ? 4 : 8;
+  static constexpr int T = 256;
+  static constexpr int LD = RS + 1;
+  static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 template <int N>
 struct ColCfg {  // N = H points per column
-  static constexpr int CS = N >= 2048 ? 4 : (N >= 768 ? 8 : 16);
-  static constexpr size_t smem() { return (size_t)N * (CS + 1) * sizeof(float2); }
+  static constexpr int CS = N >= 1024 ? 4 : 8;
+  static constexpr int T = N >= 2048 ? 512 : 256;
+  static constexpr int LD = CS + 1;
+  static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
+};
+
+// The synthesis CTA keeps its running band sum in registers: more threads per
+// CTA keep that share at 8 complex values per thread.
+template <int N>
+struct SynCfg : ColCfg<N> {
+  static constexpr int T = N >= 2048 ? 1024 : 512;
 };
 
 __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
@@ -46,210 +60,219 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
   return a > 0.0f ? copysignf(a, v) : 0.0f;
 }
 
+// global rows [row0, row0+RS) of a packed/real-as-complex H x WH array -> smem [i][s]
+template <int WH, int RS, int LD, int T>
+__device__ __forceinline__ void load_rows(float2* buf, const float2* __restrict__ src) {
+#pragma unroll 4
+  for (int e = threadIdx.x; e < WH * RS; e += T) {
+    const int s = e / WH, i = e % WH;
+    buf[i * LD + s] = src[(size_t)s * WH + i];
+  }
+}
+template <int WH, int RS, int LD, int T>
+__device__ __forceinline__ void store_rows(float2* __restrict__ dst, const float2* buf) {
+#pragma unroll 4
+  for (int e = threadIdx.x; e < WH * RS; e += T) {
+    const int s = e / WH, i = e % WH;
+    dst[(size_t)s * WH + i] = buf[i * LD + s];
+  }
+}
+
 // ---------------------------------------------------------------------------
-// Row kernels.  grid = (H / RS, njobs), block = kThreads.
+// Row kernels.  grid = (H / RS, njobs).
 // ---------------------------------------------------------------------------
 
 // real rows -> packed half-spectrum rows (forward R2C along W)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_fwd(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
-                                                        float2* dst_base, const float2* __restrict__ twWh,
-                                                        const float2* __restrict__ twW) {
-  constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
+__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_fwd(const RowJob* __restrict__ jobs, int n_active,
+                                                             const float2* src_base, float2* dst_base,
+                                                             const float2* __restrict__ twWh,
+                                                             const float2* __restrict__ twW) {
+  using C = RowCfg<WH>;
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)WH * C::LD;
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
-  const int row0 = blockIdx.x * RS;
-  const float2* src = src_base + job.src + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    smem[i * LD + s] = src[(size_t)s * WH + i];
-  }
+  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  block_fft<WH, RS, kThreads, -1>(smem, twWh);
-  r2c_post<WH, RS, kThreads>(smem, twW);
-  float2* dst = dst_base + job.dst + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    dst[(size_t)s * WH + i] = smem[i * LD + s];
-  }
+  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, -1>(A, B, twWh);
+  float2* Y = (X == A) ? B : A;
+  r2c_post_pp<WH, C::RS, C::LD, C::T>(X, Y, twW);
+  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, Y);
 }
 
 // packed rows -> real rows (inverse C2R along W, unnormalised: x W)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_inv(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
-                                                        float2* dst_base, const float2* __restrict__ twWh,
-                                                        const float2* __restrict__ twW) {
-  constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
+__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_inv(const RowJob* __restrict__ jobs, int n_active,
+                                                             const float2* src_base, float2* dst_base,
+                                                             const float2* __restrict__ twWh,
+                                                             const float2* __restrict__ twW) {
+  using C = RowCfg<WH>;
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)WH * C::LD;
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
-  const int row0 = blockIdx.x * RS;
-  const float2* src = src_base + job.src + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    smem[i * LD + s] = src[(size_t)s * WH + i];
-  }
+  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  c2r_pre<WH, RS, kThreads>(smem, twW);
-  block_fft<WH, RS, kThreads, +1>(smem, twWh);
-  float2* dst = dst_base + job.dst + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    dst[(size_t)s * WH + i] = smem[i * LD + s];
-  }
+  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
+  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, +1>(B, A, twWh);
+  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, X);
 }
 
 // packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
 template <int WH>
-__global__ void __launch_bounds__(kThreads) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active, const float2* src_base,
-                                                           float2* dst_base, const float2* __restrict__ twWh,
-                                                           const float2* __restrict__ twW,
-                                                           const float* __restrict__ thr, int mode) {
-  constexpr int RS = RowCfg<WH>::RS, LD = RS + 1;
+__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active,
+                                                                const float2* src_base, float2* dst_base,
+                                                                const float2* __restrict__ twWh,
+                                                                const float2* __restrict__ twW,
+                                                                const float* __restrict__ thr, int mode) {
+  using C = RowCfg<WH>;
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)WH * C::LD;
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const float th = thr[job.th_index];
-  const int row0 = blockIdx.x * RS;
-  const float2* src = src_base + job.src + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    smem[i * LD + s] = src[(size_t)s * WH + i];
-  }
+  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  c2r_pre<WH, RS, kThreads>(smem, twW);
-  block_fft<WH, RS, kThreads, +1>(smem, twWh);
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int i = e / RS, s = e % RS;
-    float2 v = smem[i * LD + s];
+  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
+  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, +1>(B, A, twWh);
+  for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
+    const int i = e / C::RS, s = e % C::RS;
+    float2 v = X[i * C::LD + s];
     v.x = apply_thresh(v.x, th, mode);
     v.y = apply_thresh(v.y, th, mode);
-    smem[i * LD + s] = v;
+    X[i * C::LD + s] = v;
   }
   __syncthreads();
-  block_fft<WH, RS, kThreads, -1>(smem, twWh);
-  r2c_post<WH, RS, kThreads>(smem, twW);
-  float2* dst = dst_base + job.dst + (size_t)row0 * WH;
-  for (int e = threadIdx.x; e < WH * RS; e += kThreads) {
-    int s = e / WH, i = e % WH;
-    dst[(size_t)s * WH + i] = smem[i * LD + s];
-  }
+  float2* Y = (X == A) ? B : A;
+  float2* Z = block_fft_pp<WH, C::RS, C::LD, C::T, -1>(X, Y, twWh);
+  float2* O = (Z == A) ? B : A;
+  r2c_post_pp<WH, C::RS, C::LD, C::T>(Z, O, twW);
+  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, O);
 }
 
 // ---------------------------------------------------------------------------
-// Column kernels.  grid = (WH / CS, njobs), block = kThreads.
+// Column kernels.  grid = (WH / CS, njobs).
 // ---------------------------------------------------------------------------
 
 // plain column FFT (forward or inverse) src -> dst
 template <int H, int DIR>
-__global__ void __launch_bounds__(kThreads) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base,
-                                                    float2* dst_base, const float2* __restrict__ twH) {
-  constexpr int CS = ColCfg<H>::CS, LD = CS + 1;
+__global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH,
+                                                        const float2* src_base, float2* dst_base,
+                                                        const float2* __restrict__ twH) {
+  using C = ColCfg<H>;
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)H * C::LD;
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
-  for (int e = threadIdx.x; e < H * CS; e += kThreads) {
-    int i = e / CS, s = e % CS;
-    smem[i * LD + s] = src_base[job.src + (size_t)i * WH + col0 + s];
+  const int col0 = blockIdx.x * C::CS;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int i = e / C::CS, s = e % C::CS;
+    A[i * C::LD + s] = src_base[job.src + (size_t)i * WH + col0 + s];
   }
   __syncthreads();
-  block_fft<H, CS, kThreads, DIR>(smem, twH);
-  for (int e = threadIdx.x; e < H * CS; e += kThreads) {
-    int i = e / CS, s = e % CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = smem[i * LD + s];
+  float2* X = block_fft_pp<H, C::CS, C::LD, C::T, DIR>(A, B, twH);
+#pragma unroll 4
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int i = e / C::CS, s = e % C::CS;
+    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
   }
 }
 
 // analysis band: dst = colIFFT( Wk .* src ), src = fully transformed level spectrum
 template <int H>
-__global__ void __launch_bounds__(kThreads) k_band_analysis(const ColJob* __restrict__ jobs, int n_active, int WH,
-                                                             const float2* src_base, float2* dst_base,
-                                                             const float2* __restrict__ spec_base,
-                                                             const float2* __restrict__ twH) {
-  constexpr int CS = ColCfg<H>::CS, LD = CS + 1;
+__global__ void __launch_bounds__(ColCfg<H>::T) k_band_analysis(const ColJob* __restrict__ jobs, int n_active,
+                                                                 int WH, const float2* src_base, float2* dst_base,
+                                                                 const float2* __restrict__ spec_base,
+                                                                 const float2* __restrict__ twH) {
+  using C = ColCfg<H>;
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)H * C::LD;
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
-  for (int e = threadIdx.x; e < H * CS; e += kThreads) {
-    int i = e / CS, s = e % CS;
-    size_t g = (size_t)i * WH + col0 + s;
-    float2 z = src_base[job.src + g];
-    float2 p = __ldg(&spec_base[job.spec + g]);
-    float2 r = cmul(p, z);
+  const int col0 = blockIdx.x * C::CS;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int i = e / C::CS, s = e % C::CS;
+    const size_t g = (size_t)i * WH + col0 + s;
+    const float2 z = src_base[job.src + g];
+    float2 r = cmul(__ldg(&spec_base[job.spec + g]), z);
     if (col0 + s == 0) {  // packed DC/Nyquist column
-      float2 zm = src_base[job.src + (size_t)((H - i) % H) * WH];
+      const float2 zm = src_base[job.src + (size_t)((H - i) % H) * WH];
       r = cadd(r, cmul(__ldg(&spec_base[job.m0 + i]), cconj(zm)));
     }
-    smem[i * LD + s] = r;
+    A[i * C::LD + s] = r;
   }
   __syncthreads();
-  block_fft<H, CS, kThreads, +1>(smem, twH);
-  for (int e = threadIdx.x; e < H * CS; e += kThreads) {
-    int i = e / CS, s = e % CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = smem[i * LD + s];
+  float2* X = block_fft_pp<H, C::CS, C::LD, C::T, +1>(A, B, twH);
+#pragma unroll 4
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int i = e / C::CS, s = e % C::CS;
+    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
   }
 }
 
 // synthesis: dst = colIFFT( sum_k conj(Wk) .* colFFT(src_k) ) over job.nbands
 // bands stored at src + k * band_stride, spectra at spec + k * band_stride,
-// side arrays at m0 + k * H.
+// side arrays at m0 + k * H.  The running sum stays in registers.
 template <int H>
-__global__ void __launch_bounds__(kThreads) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active, int WH,
-                                                              const float2* src_base, float2* dst_base,
-                                                              const float2* __restrict__ spec_base,
-                                                              size_t band_stride,
-                                                              const float2* __restrict__ twH) {
-  constexpr int CS = ColCfg<H>::CS, LD = CS + 1;
-  constexpr int EPT = H * CS / kThreads;
-  static_assert(H * CS % kThreads == 0, "tile must divide evenly");
+__global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active,
+                                                                  int WH, const float2* src_base, float2* dst_base,
+                                                                  const float2* __restrict__ spec_base,
+                                                                  size_t band_stride,
+                                                                  const float2* __restrict__ twH) {
+  using C = SynCfg<H>;
+  constexpr int EPT = H * C::CS / C::T;
+  static_assert(H * C::CS % C::T == 0, "tile must divide evenly");
   extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)H * C::LD;
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = blockIdx.x * C::CS;
   float2 acc[EPT];
 #pragma unroll
   for (int it = 0; it < EPT; it++) acc[it] = make_float2(0.f, 0.f);
   for (int k = 0; k < job.nbands; k++) {
     const float2* src = src_base + job.src + k * band_stride;
     const float2* spec = spec_base + job.spec + k * band_stride;
-#pragma unroll 4
-    for (int it = 0; it < EPT; it++) {
-      int e = threadIdx.x + it * kThreads;
-      int i = e / CS, s = e % CS;
-      smem[i * LD + s] = src[(size_t)i * WH + col0 + s];
-    }
-    __syncthreads();
-    block_fft<H, CS, kThreads, -1>(smem, twH);
 #pragma unroll
     for (int it = 0; it < EPT; it++) {
-      int e = threadIdx.x + it * kThreads;
-      int i = e / CS, s = e % CS;
-      float2 z = smem[i * LD + s];
-      float2 p = __ldg(&spec[(size_t)i * WH + col0 + s]);
-      acc[it] = cadd(acc[it], cmulc(z, p));
+      const int e = threadIdx.x + it * C::T;
+      const int i = e / C::CS, s = e % C::CS;
+      A[i * C::LD + s] = src[(size_t)i * WH + col0 + s];
+    }
+    __syncthreads();
+    const float2* X = block_fft_pp<H, C::CS, C::LD, C::T, -1>(A, B, twH);
+#pragma unroll
+    for (int it = 0; it < EPT; it++) {
+      const int e = threadIdx.x + it * C::T;
+      const int i = e / C::CS, s = e % C::CS;
+      const float2 z = X[i * C::LD + s];
+      acc[it] = cadd(acc[it], cmulc(z, __ldg(&spec[(size_t)i * WH + col0 + s])));
       if (col0 + s == 0) {
-        float2 zm = smem[((H - i) % H) * LD];
-        float2 m = __ldg(&spec_base[job.m0 + (size_t)k * H + i]);
-        // conj(M) * conj(z[-u]) = conj(M * z[-u])
-        acc[it] = cadd(acc[it], cconj(cmul(m, zm)));
+        const float2 zm = X[((H - i) % H) * C::LD];
+        const float2 m = __ldg(&spec_base[job.m0 + (size_t)k * H + i]);
+        acc[it] = cadd(acc[it], cconj(cmul(m, zm)));  // conj(M) conj(z[-u])
       }
     }
     __syncthreads();
   }
 #pragma unroll
   for (int it = 0; it < EPT; it++) {
-    int e = threadIdx.x + it * kThreads;
-    int i = e / CS, s = e % CS;
-    smem[i * LD + s] = acc[it];
+    const int e = threadIdx.x + it * C::T;
+    const int i = e / C::CS, s = e % C::CS;
+    A[i * C::LD + s] = acc[it];
   }
   __syncthreads();
-  block_fft<H, CS, kThreads, +1>(smem, twH);
-  for (int e = threadIdx.x; e < H * CS; e += kThreads) {
-    int i = e / CS, s = e % CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = smem[i * LD + s];
+  const float2* X = block_fft_pp<H, C::CS, C::LD, C::T, +1>(A, B, twH);
+#pragma unroll 4
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int i = e / C::CS, s = e % C::CS;
+    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
   }
 }
 
@@ -281,12 +304,15 @@ bool col_len_supported(int h) {
       return false;
   }
 }
-int row_tile(int wh) { return wh >= 1024 ? 8 : 16; }
-int col_tile(int h) { return h >= 2048 ? 4 : (h >= 768 ? 8 : 16); }
+int row_tile(int wh) { return wh >= 1024 ? 4 : 8; }
+int col_tile(int h) { return h >= 1024 ? 4 : 8; }
 
 template <typename KernelT>
 static cudaError_t opt_in(KernelT k, size_t bytes) {
-  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  return e;
 }
 
 cudaError_t prepare_row_kernels(int wh) {
@@ -338,11 +364,11 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
     constexpr size_t sm = RowCfg<n>::smem();                                           \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                               \
     if (op == RowOp::Fwd)                                                              \
-      k_rows_fwd<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
+      k_rows_fwd<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
     else if (op == RowOp::Inv)                                                         \
-      k_rows_inv<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
+      k_rows_inv<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
     else                                                                               \
-      k_rows_thresh<n><<<grid, kThreads, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
+      k_rows_thresh<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
   }
     NSST_ROW_SIZES(CASE)
@@ -364,13 +390,13 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
     constexpr size_t sm = ColCfg<n>::smem();                                                          \
     dim3 grid(WH / ColCfg<n>::CS, njobs);                                                             \
     if (op == ColOp::Fwd)                                                                             \
-      k_cols<n, -1><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                   \
+      k_cols<n, -1><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                   \
     else if (op == ColOp::Inv)                                                                        \
-      k_cols<n, 1><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                    \
+      k_cols<n, 1><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                    \
     else if (op == ColOp::Analysis)                                                                   \
-      k_band_analysis<n><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base, twH);   \
+      k_band_analysis<n><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base, twH);   \
     else                                                                                              \
-      k_band_synthesis<n><<<grid, kThreads, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,        \
+      k_band_synthesis<n><<<grid, SynCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,        \
                                                       band_stride, twH);                              \
     return cudaGetLastError();                                                                        \
   }
