@@ -314,3 +314,116 @@ def denoise(x, sigma, K, scalars, dcomp, dsize, mode='hard', shear_f=None, fname
 def psnr(ref, x, peak=255.0):
     mse = np.mean((np.asarray(ref, np.float64) - np.asarray(x, np.float64)) ** 2)
     return 10 * math.log10(peak * peak / mse)
+
+
+# ----------------------------------------------------------------------------
+# Adjoints and the gradient of the denoising loss (FP64).  The reference has no
+# adjoint; these are the exact transposes of the operators above, used to
+# check the GPU adjoint kernels.
+# ----------------------------------------------------------------------------
+def _reflect_index(t, n):
+    """Single mirror reflection with the edge sample repeated (symext.m)."""
+    t = np.where(t < 0, -1 - t, t)
+    return np.where(t >= n, 2 * n - 1 - t, t)
+
+
+def _filter_step_matrix_apply(x, F, M, transpose=False):
+    """One centred dilated filtering step y[r,c] = sum_ab hf[a,b] xe[r-M c0+M a, c-M c0+M b]
+    (the atrousc(symext(...)) call, see _filter_step) or its transpose."""
+    n, m = x.shape
+    Fs = F.shape[0]
+    c0 = (Fs - 1) // 2
+    hf = F[::-1, ::-1]
+    out = np.zeros_like(x)
+    rows = np.arange(n)
+    cols = np.arange(m)
+    for a in range(Fs):
+        ri = _reflect_index(rows - M * c0 + M * a, n)
+        for b in range(Fs):
+            w = hf[a, b]
+            if w == 0.0:
+                continue
+            ci = _reflect_index(cols - M * c0 + M * b, m)
+            if not transpose:
+                out += w * x[np.ix_(ri, ci)]
+            else:
+                np.add.at(out, np.ix_(ri, ci), w * x)
+    return out
+
+
+def atrousdec_adjoint(gy, fname='maxflat'):
+    """Transpose of atrousdec: gradients of the (nlev+1) outputs -> gradient of x."""
+    h0, h1, _, _ = atrousfilters(fname)
+    n = len(gy) - 1
+    g_lo = gy[0].copy()  # gradient of the last lowpass
+    for i in range(n - 1, 0, -1):
+        M = 2 ** i
+        g_lo = _filter_step_matrix_apply(g_lo, h0, M, True) + _filter_step_matrix_apply(gy[n - i], h1, M, True)
+    return _filter_step_matrix_apply(g_lo, h0, 1, True) + _filter_step_matrix_apply(gy[n], h1, 1, True)
+
+
+def atrousrec_adjoint(gx, nlevels, fname='maxflat'):
+    """Transpose of atrousrec: gradient of the output -> gradients of y[0..nlev]."""
+    _, _, g0, g1 = atrousfilters(fname)
+    gy = [None] * (nlevels + 1)
+    gy[nlevels] = _filter_step_matrix_apply(gx, g1, 1, True)
+    g = _filter_step_matrix_apply(gx, g0, 1, True)
+    for i in range(1, nlevels):
+        M = 2 ** i
+        gy[nlevels - i] = _filter_step_matrix_apply(g, g1, M, True)
+        g = _filter_step_matrix_apply(g, g0, M, True)
+    gy[0] = g
+    return gy
+
+
+def soft(c, t):
+    return np.sign(c) * np.maximum(np.abs(c) - t, 0.0)
+
+
+def denoise_tau(x, tau, shear_f, fname='maxflat', mode='soft', nthreads=1):
+    """Forward of the differentiable pipeline with explicit per-band thresholds
+    tau = [t_lowpass, level0 (ndir0,), level1 (ndir1,), ...]."""
+    dst, _ = _dec_with(x, shear_f, fname, nthreads)
+    thr = lambda c, t: soft(c, t) if mode == 'soft' else c * (np.abs(c) > t)
+    dt = [thr(dst[0], tau[0])] + [thr(dst[i], np.asarray(tau[i])[:, None, None]) for i in range(1, len(dst))]
+    return nsst_rec2(dt, shear_f, fname, nthreads=max(nthreads, 1)), dst
+
+
+def _dec_with(x, shear_f, fname, nthreads):
+    y = atrousdec(x, fname, len(shear_f), nthreads=max(nthreads, 1))
+    dst = [y[0]]
+    for i in range(len(shear_f)):
+        Y = sfft.fft2(y[i + 1], workers=max(nthreads, 1))
+        dst.append(np.real(sfft.ifft2(shear_f[i] * Y[None], axes=(-2, -1), workers=max(nthreads, 1))))
+    return dst, shear_f
+
+
+def denoise_tau_grad(x, tau, clean, shear_f, fname='maxflat', mode='soft', nthreads=1):
+    """loss = ||rec(T(dec(x), tau)) - clean||^2 and its gradients w.r.t. x and tau."""
+    w = max(nthreads, 1)
+    xr, dst = denoise_tau(x, tau, shear_f, fname, mode, nthreads)
+    r = xr - clean
+    loss = float(np.sum(r * r))
+    gxr = 2.0 * r
+    L = len(shear_f)
+    gyp = atrousrec_adjoint(gxr, L, fname)         # d loss / d y' (synthesis inputs)
+    gct = [gyp[0]]                                  # d loss / d thresholded coefficients
+    for i in range(L):
+        G = sfft.fft2(gyp[i + 1], workers=w)
+        gct.append(np.real(sfft.ifft2(shear_f[i] * G[None], axes=(-2, -1), workers=w)))
+    gc, gtau = [], []
+    for i, (c, g) in enumerate(zip(dst, gct)):
+        t = tau[0] if i == 0 else np.asarray(tau[i])[:, None, None]
+        keep = np.abs(c) > t
+        gc.append(g * keep)
+        if mode == 'soft':
+            gt = -np.sum(g * np.sign(c) * keep, axis=(-2, -1))
+        else:
+            gt = np.zeros_like(np.asarray(t, float).reshape(-1)) if i else 0.0
+        gtau.append(float(gt) if i == 0 else np.asarray(gt).reshape(-1))
+    gy = [gc[0]]
+    for i in range(L):
+        C = sfft.fft2(gc[i + 1], axes=(-2, -1), workers=w)
+        gy.append(np.real(sfft.ifft2(np.sum(np.conj(shear_f[i]) * C, axis=0), workers=w)))
+    gx = atrousdec_adjoint(gy, fname)
+    return loss, gx, gtau

@@ -125,7 +125,7 @@ template <> struct FftPlan<256> { using type = RadixList<4, 8, 8>; };
 template <> struct FftPlan<384> { using type = RadixList<3, 2, 8, 8>; };
 template <> struct FftPlan<512> { using type = RadixList<8, 8, 8>; };
 template <> struct FftPlan<768> { using type = RadixList<3, 4, 8, 8>; };
-template <> struct FftPlan<1024> { using type = RadixList<2, 8, 8, 8>; };
+template <> struct FftPlan<1024> { using type = RadixList<8, 8, 8, 2>; };
 template <> struct FftPlan<2048> { using type = RadixList<4, 8, 8, 8>; };
 
 // One Stockham pass of radix R over NSEQ sequences of length N, in place.
@@ -290,9 +290,22 @@ __device__ __forceinline__ void c2r_pre(float2* buf, const float2* __restrict__ 
 // Ping-pong variant: each pass reads buffer `in` and writes buffer `out`, so a
 // thread only holds one butterfly's R values at a time (low register use) and
 // a pass needs a single barrier.  Returns the buffer that holds the result.
-// Both buffers use the [index][sequence] layout with leading dimension LD.
+//
+// Layout: element (index i, sequence s) at [phi(i) * NSEQ + s] with no padding.
+// A warp covers 32/NSEQ consecutive butterflies of NSEQ sequences each, so the
+// rows it touches in one access are consecutive (-> alternating bank groups,
+// conflict-free) in every pass except where the first pass (NS == 1) writes
+// rows R apart; that pass's output is row-swizzled, phi(i) = i ^ ((i / R) & m)
+// with m = 16/NSEQ - 1, and the second pass reads it back through the same phi.
 // ---------------------------------------------------------------------------
-template <int N, int NSEQ, int LD, int T, int R, int NS, int DIR>
+template <int NSEQ, int SWZ>
+__device__ __forceinline__ int swz_row(int i) {
+  constexpr int M = 16 / NSEQ - 1;
+  if (SWZ == 0 || M <= 0) return i;
+  return i ^ ((i / SWZ) & M);
+}
+
+template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT>
 __device__ __forceinline__ void stockham_pp(const float2* __restrict__ in, float2* __restrict__ out,
                                             const float2* __restrict__ tw) {
   constexpr int NB = N / R;
@@ -304,7 +317,7 @@ __device__ __forceinline__ void stockham_pp(const float2* __restrict__ in, float
     const int j = w / NSEQ;
     float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) v[r] = in[(j + r * NB) * LD + s];
+    for (int r = 0; r < R; r++) v[r] = in[swz_row<NSEQ, SWZ_IN>(j + r * NB) * NSEQ + s];
     const int k = j % NS;
     if (NS > 1) {
 #pragma unroll
@@ -316,27 +329,30 @@ __device__ __forceinline__ void stockham_pp(const float2* __restrict__ in, float
     Dft<R, DIR>::run(v);
     const int base = (j / NS) * NS * R + k;
 #pragma unroll
-    for (int r = 0; r < R; r++) out[(base + r * NS) * LD + s] = v[r];
+    for (int r = 0; r < R; r++) out[swz_row<NSEQ, SWZ_OUT>(base + r * NS) * NSEQ + s] = v[r];
   }
   __syncthreads();
 }
 
-template <int N, int NSEQ, int LD, int T, int DIR, int NS>
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN>
 __device__ __forceinline__ float2* fft_pp_passes(float2* a, float2* b, const float2* __restrict__ tw, RadixList<>) {
   return a;
 }
 
-template <int N, int NSEQ, int LD, int T, int DIR, int NS, int R, int... Rest>
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, int R, int... Rest>
 __device__ __forceinline__ float2* fft_pp_passes(float2* a, float2* b, const float2* __restrict__ tw,
                                                  RadixList<R, Rest...>) {
-  stockham_pp<N, NSEQ, LD, T, R, NS, DIR>(a, b, tw);
-  return fft_pp_passes<N, NSEQ, LD, T, DIR, NS * R>(b, a, tw, RadixList<Rest...>{});
+  // only the first pass (NS == 1, even radix) writes rows R apart
+  constexpr int SWZ_OUT = (NS == 1 && R % 2 == 0 && sizeof...(Rest) > 0) ? R : 0;
+  stockham_pp<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(a, b, tw);
+  return fft_pp_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(b, a, tw, RadixList<Rest...>{});
 }
 
-// FFT of the data in `a` using `b` as the second buffer; returns a or b.
-template <int N, int NSEQ, int LD, int T, int DIR>
+// FFT of the data in `a` (layout [i * NSEQ + s]) using `b` as the second
+// buffer; returns a or b, holding the result in the same unswizzled layout.
+template <int N, int NSEQ, int T, int DIR>
 __device__ __forceinline__ float2* block_fft_pp(float2* a, float2* b, const float2* __restrict__ tw) {
-  return fft_pp_passes<N, NSEQ, LD, T, DIR, 1>(a, b, tw, typename FftPlan<N>::type{});
+  return fft_pp_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, typename FftPlan<N>::type{});
 }
 
 // Out-of-place packed-real post-processing (after a forward FFT of the

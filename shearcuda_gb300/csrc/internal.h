@@ -39,11 +39,23 @@ struct AtrousJob {
   const float* xa;
   const float* xb;  // optional second input (synthesis)
   float* out;
-  int H, W;
+  int H, W;         // input image size
+  int Ho, Wo;       // output size (0 = same as the input) for the forward
+                    // step; the extended domain H + M(F-1) x W + M(F-1) for
+                    // the adjoint step
 };
 constexpr int kMaxAtrousJobs = 64;
 struct AtrousJobs {  // passed by value
   AtrousJob j[kMaxAtrousJobs];
+};
+
+struct FoldJob {
+  const float* z1;  // first source (extended domain) / or c for the lowpass mask
+  const float* z2;  // optional second source / or g for the lowpass mask
+  float* out;
+};
+struct FoldJobs {  // passed by value
+  FoldJob j[kMaxAtrousJobs];
 };
 
 template <int F>
@@ -73,7 +85,7 @@ inline void fill_taps(AtrousTaps<F>& t, const float* hflip) {
 }
 inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
 
-enum class RowOp { Fwd, Inv, Thresh };
+enum class RowOp { Fwd, Inv, Thresh, Backward };
 enum class ColOp { Fwd, Inv, Analysis, Synthesis };
 
 bool row_len_supported(int wh);
@@ -92,7 +104,24 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
                         cudaStream_t st);
 cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,
                           int FB, const float* hb, cudaStream_t st);
+// Adjoint helper: out (Ho x Wo, extended domain) = zero-extended full
+// correlation of x with the *unflipped* filter h, Ho = H + M(F-1).
+cudaError_t launch_atrous_full(const AtrousJobs& jobs, int njobs, int maxHo, int maxWo, int M, int F, const float* h,
+                               cudaStream_t st);
 bool atrous_pair_supported(int FA, int FB);
+cudaError_t launch_fold(const FoldJobs& jobs, int njobs, int H, int W, int E1, int E2, bool accumulate,
+                        cudaStream_t st);
+cudaError_t launch_lowpass_backward(const FoldJobs& jobs, int njobs, size_t n, const float* tau, int mode,
+                                    float* partials, int slot0, int nblk, cudaStream_t st);
+cudaError_t launch_reduce_tau(const float* partials, int count, size_t stride, int nbands, float* grad_tau,
+                              bool accumulate, cudaStream_t st);
+cudaError_t launch_broadcast_tau(const float* tau, float* th, int nbands, int n, cudaStream_t st);
+// Backward band row pass: Qc (coefficients' packed rows, src) and Qg (gradient
+// packed rows, dst, in place) -> R2C(C2R(Qg) * 1[|C2R(Qc)| > t]); per-CTA soft
+// threshold gradient partials at partials[th_index * pstride + item * (H/RS) + tile].
+cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                                 void* dst_base, const float2* twWh, const float2* twW, const float* tau, int mode,
+                                 float* partials, size_t pstride, cudaStream_t st);
 cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
 
 // ------------------------------------------------------- host-side FP64 math

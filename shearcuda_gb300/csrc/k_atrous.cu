@@ -39,20 +39,29 @@ __device__ __forceinline__ int mirror_index(int i, int n) {
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
 
-template <int F>
+// out[r][c] += sum_{a,b} taps[a][b] * X[r + M(a - ORG)][c + M(b - ORG)] for this
+// thread's 16 rows.  Forward steps: ORG = (F-1)/2 and X mirror-extended;
+// adjoint steps (ZERO): ORG = F-1 and X zero-extended.
+template <int F, bool ZERO>
 __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
                                                   int prow0, int col0, const float* __restrict__ taps,
                                                   const int* __restrict__ tapcols, int ntapcols, float* tile,
                                                   float (&acc)[kAtP]) {
-  constexpr int C0 = (F - 1) / 2;
+  constexpr int C0 = ZERO ? F - 1 : (F - 1) / 2;
   constexpr int TR = kAtRows + F - 1;
   const int TC = kAtTX + M * (F - 1);
   const int tid = threadIdx.x;
   for (int e = tid; e < TR * TC; e += kAtThreads) {
     int tr = e / TC, tc = e - tr * TC;
-    int r = mirror_index(phase + M * (prow0 + tr - C0), H);
-    int c = mirror_index(col0 - M * C0 + tc, W);
-    tile[e] = __ldg(&x[(size_t)r * W + c]);
+    int r = phase + M * (prow0 + tr - C0);
+    int c = col0 - M * C0 + tc;
+    if (ZERO) {
+      tile[e] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(&x[(size_t)r * W + c]) : 0.0f;
+    } else {
+      r = mirror_index(r, H);
+      c = mirror_index(c, W);
+      tile[e] = __ldg(&x[(size_t)r * W + c]);
+    }
   }
   __syncthreads();
   const int tx = tid % kAtTX, ty = tid / kAtTX;
@@ -73,7 +82,7 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
 }
 
 // out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/64), njobs)
-template <int FA, int FB>
+template <int FA, int FB, bool ZERO = false>
 __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
                                                         const __grid_constant__ AtrousTaps<FA> ta,
                                                         const __grid_constant__ AtrousTaps<FB> tb) {
@@ -82,11 +91,12 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
   __shared__ int s_cols[(FA > FB ? FA : FB)];
   const AtrousJob& job = jobs.j[blockIdx.z];
   const int H = job.H, W = job.W;
+  const int Ho = job.Ho > 0 ? job.Ho : H, Wo = job.Wo > 0 ? job.Wo : W;  // 0: same as the input
   const int col0 = blockIdx.x * kAtTX;
   const int phase = blockIdx.y % M;
   const int prow0 = (blockIdx.y / M) * kAtRows;
-  const int nprow = (H - phase + M - 1) / M;  // poly rows of this phase
-  if (col0 >= W || prow0 >= nprow) return;
+  const int nprow = (Ho - phase + M - 1) / M;  // output poly rows of this phase
+  if (col0 >= Wo || prow0 >= nprow) return;
   float acc[kAtP];
 #pragma unroll
   for (int p = 0; p < kAtP; p++) acc[p] = 0.f;
@@ -94,21 +104,21 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
   for (int e = threadIdx.x; e < FA * FA; e += kAtThreads) s_taps[e] = ta.w[e];
   for (int e = threadIdx.x; e < ta.ncols; e += kAtThreads) s_cols[e] = ta.cols[e];
   __syncthreads();
-  atrous_accumulate<FA>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
+  atrous_accumulate<FA, ZERO>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
   if (FB > 0 && job.xb != nullptr) {
     for (int e = threadIdx.x; e < FB * FB; e += kAtThreads) s_taps[e] = tb.w[e];
     for (int e = threadIdx.x; e < tb.ncols; e += kAtThreads) s_cols[e] = tb.cols[e];
     __syncthreads();
-    atrous_accumulate<(FB > 0 ? FB : 1)>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
-                                          at_smem, acc);
+    atrous_accumulate<(FB > 0 ? FB : 1), ZERO>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
+                                                at_smem, acc);
   }
   const int tx = threadIdx.x % kAtTX, ty = threadIdx.x / kAtTX;
   const int c = col0 + tx;
-  if (c < W) {
+  if (c < Wo) {
 #pragma unroll
     for (int p = 0; p < kAtP; p++) {
       int pr = prow0 + ty * kAtP + p;
-      if (pr < nprow) job.out[(size_t)(phase + M * pr) * W + c] = acc[p];
+      if (pr < nprow) job.out[(size_t)(phase + M * pr) * Wo + c] = acc[p];
     }
   }
 }
@@ -139,7 +149,9 @@ static cudaError_t prepare_atrous_t(int Mmax) {
   if (want > 227 * 1024) return cudaErrorInvalidValue;
   std::lock_guard<std::mutex> lk(mu);
   if (dev >= 0 && dev < kDevs && configured[dev] >= want) return cudaSuccess;
-  e = cudaFuncSetAttribute(k_atrous<FA, FB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+  e = cudaFuncSetAttribute(k_atrous<FA, FB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+  if (e == cudaSuccess && FB == 0)
+    e = cudaFuncSetAttribute(k_atrous<FA, FB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
   if (e == cudaSuccess && dev >= 0 && dev < kDevs) configured[dev] = want;
   return e;
 }
@@ -155,7 +167,22 @@ static cudaError_t launch_atrous_t(const AtrousJobs& jobs, int njobs, int maxH, 
   const int nprow_max = (maxH + M - 1) / M;
   dim3 grid((maxW + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
   count_launch();
-  k_atrous<FA, FB><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  k_atrous<FA, FB, false><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  return cudaGetLastError();
+}
+
+template <int F>
+static cudaError_t launch_atrous_full_t(const AtrousJobs& jobs, int njobs, int maxHo, int maxWo, int M,
+                                        const float* h, cudaStream_t st) {
+  AtrousTaps<F> ta;
+  AtrousTaps<0> tb;
+  fill_taps(ta, h);
+  fill_taps(tb, nullptr);
+  const size_t sm = atrous_smem<F>(M);
+  const int nprow_max = (maxHo + M - 1) / M;
+  dim3 grid((maxWo + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
+  count_launch();
+  k_atrous<F, 0, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
   return cudaGetLastError();
 }
 
@@ -178,6 +205,20 @@ cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW,
   NSST_AT_PAIRS(NSST_AT)
 #undef NSST_AT
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_atrous_full(const AtrousJobs& jobs, int njobs, int maxHo, int maxWo, int M, int F, const float* h,
+                               cudaStream_t st) {
+  if (njobs == 0) return cudaSuccess;
+  if (njobs > kMaxAtrousJobs) return cudaErrorInvalidValue;
+  switch (F) {
+    case 5: return launch_atrous_full_t<5>(jobs, njobs, maxHo, maxWo, M, h, st);
+    case 7: return launch_atrous_full_t<7>(jobs, njobs, maxHo, maxWo, M, h, st);
+    case 9: return launch_atrous_full_t<9>(jobs, njobs, maxHo, maxWo, M, h, st);
+    case 13: return launch_atrous_full_t<13>(jobs, njobs, maxHo, maxWo, M, h, st);
+    case 19: return launch_atrous_full_t<19>(jobs, njobs, maxHo, maxWo, M, h, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 bool atrous_pair_supported(int FA, int FB) {

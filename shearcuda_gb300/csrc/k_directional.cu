@@ -28,22 +28,21 @@
 namespace nsst {
 
 // Tile shapes: a row CTA owns RS rows, a column CTA owns CS columns, each as two
-// ping-pong shared buffers [index][sequence] with one float2 of padding per
-// index.  They keep a thread's share of a tile at <= 16 complex values and the
+// ping-pong shared buffers [index][sequence] (dense, see block_fft_pp).  They keep a thread's share of a tile at <= 16 complex values and the
 // shared memory low enough for 2-3 resident CTAs per SM: the kernels are bound
 // by global-memory latency, so resident CTAs are what hides it.
 template <int N>
 struct RowCfg {  // N = W/2 complex points per row
   static constexpr int RS = N >= 1024 ? 4 : 8;
   static constexpr int T = 256;
-  static constexpr int LD = RS + 1;
+  static constexpr int LD = RS;
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 template <int N>
 struct ColCfg {  // N = H points per column
   static constexpr int CS = N >= 1024 ? 4 : 8;
   static constexpr int T = N >= 2048 ? 512 : 256;
-  static constexpr int LD = CS + 1;
+  static constexpr int LD = CS;
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 
@@ -61,11 +60,13 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
 }
 
 // global rows [row0, row0+RS) of a packed/real-as-complex H x WH array -> smem [i][s]
+// Sequence-fastest staging: a warp reads 32/RS consecutive elements of each of
+// its RS rows (full 32-byte sectors) and writes consecutive shared rows.
 template <int WH, int RS, int LD, int T>
 __device__ __forceinline__ void load_rows(float2* buf, const float2* __restrict__ src) {
 #pragma unroll 4
   for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int s = e / WH, i = e % WH;
+    const int s = e % RS, i = e / RS;
     buf[i * LD + s] = src[(size_t)s * WH + i];
   }
 }
@@ -73,7 +74,7 @@ template <int WH, int RS, int LD, int T>
 __device__ __forceinline__ void store_rows(float2* __restrict__ dst, const float2* buf) {
 #pragma unroll 4
   for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int s = e / WH, i = e % WH;
+    const int s = e % RS, i = e / RS;
     dst[(size_t)s * WH + i] = buf[i * LD + s];
   }
 }
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_fwd(const RowJob* __rest
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, -1>(A, B, twWh);
+  float2* X = block_fft_pp<WH, C::RS, C::T, -1>(A, B, twWh);
   float2* Y = (X == A) ? B : A;
   r2c_post_pp<WH, C::RS, C::LD, C::T>(X, Y, twW);
   store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, Y);
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_inv(const RowJob* __rest
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
   c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
-  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, +1>(B, A, twWh);
+  float2* X = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
   store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, X);
 }
 
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __r
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
   c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
-  float2* X = block_fft_pp<WH, C::RS, C::LD, C::T, +1>(B, A, twWh);
+  float2* X = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
   for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
     const int i = e / C::RS, s = e % C::RS;
     float2 v = X[i * C::LD + s];
@@ -148,8 +149,66 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __r
   }
   __syncthreads();
   float2* Y = (X == A) ? B : A;
-  float2* Z = block_fft_pp<WH, C::RS, C::LD, C::T, -1>(X, Y, twWh);
+  float2* Z = block_fft_pp<WH, C::RS, C::T, -1>(X, Y, twWh);
   float2* O = (Z == A) ? B : A;
+  r2c_post_pp<WH, C::RS, C::LD, C::T>(Z, O, twW);
+  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, O);
+}
+
+
+// Backward band row pass (adjoint of the threshold step, rows of one band):
+// coefficients c = C2R(Qc) are recomputed, g = C2R(Qg) is the gradient w.r.t.
+// the thresholded coefficients; out = R2C(g * 1[|c| > t]) replaces Qg, and
+// each CTA writes its share of d loss / d t = -sum g sign(c) 1[|c| > t] (soft).
+template <int WH>
+__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* __restrict__ jobs, int n_active,
+                                                                  const float2* src_base, float2* dst_base,
+                                                                  const float2* __restrict__ twWh,
+                                                                  const float2* __restrict__ twW,
+                                                                  const float* __restrict__ tau, int mode,
+                                                                  float* __restrict__ partials, size_t pstride) {
+  using C = RowCfg<WH>;
+  extern __shared__ float2 smem[];
+  float2 *A = smem, *B = smem + (size_t)WH * C::LD, *Cb = smem + 2 * (size_t)WH * C::LD,
+         *D = smem + 3 * (size_t)WH * C::LD;
+  __shared__ float red[32];
+  const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const float th = tau[job.th_index];
+  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  load_rows<WH, C::RS, C::LD, C::T>(Cb, dst_base + job.dst + off);
+  __syncthreads();
+  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
+  c2r_pre_pp<WH, C::RS, C::LD, C::T>(Cb, D, twW);
+  float2* Xc = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
+  float2* Xg = block_fft_pp<WH, C::RS, C::T, +1>(D, Cb, twWh);
+  float part = 0.0f;
+  for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
+    const int i = e / C::RS, s = e % C::RS;
+    const float2 c = Xc[i * C::LD + s];
+    float2 g = Xg[i * C::LD + s];
+    const bool kx = fabsf(c.x) > th, ky = fabsf(c.y) > th;
+    if (mode == THRESH_SOFT) {
+      if (kx) part -= copysignf(g.x, c.x);
+      if (ky) part -= copysignf(g.y, c.y);
+    }
+    g.x = kx ? g.x : 0.0f;
+    g.y = ky ? g.y : 0.0f;
+    Xg[i * C::LD + s] = g;
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (C::T >> 5) ? red[threadIdx.x] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0)
+      partials[(size_t)job.th_index * pstride + (size_t)job.item * gridDim.x + blockIdx.x] = v;
+  }
+  float2* Y = (Xg == Cb) ? D : Cb;
+  float2* Z = block_fft_pp<WH, C::RS, C::T, -1>(Xg, Y, twWh);
+  float2* O = (Z == Cb) ? D : Cb;
   r2c_post_pp<WH, C::RS, C::LD, C::T>(Z, O, twW);
   store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, O);
 }
@@ -175,7 +234,7 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict_
     A[i * C::LD + s] = src_base[job.src + (size_t)i * WH + col0 + s];
   }
   __syncthreads();
-  float2* X = block_fft_pp<H, C::CS, C::LD, C::T, DIR>(A, B, twH);
+  float2* X = block_fft_pp<H, C::CS, C::T, DIR>(A, B, twH);
 #pragma unroll 4
   for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
     const int i = e / C::CS, s = e % C::CS;
@@ -208,7 +267,7 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_band_analysis(const ColJob* __
     A[i * C::LD + s] = r;
   }
   __syncthreads();
-  float2* X = block_fft_pp<H, C::CS, C::LD, C::T, +1>(A, B, twH);
+  float2* X = block_fft_pp<H, C::CS, C::T, +1>(A, B, twH);
 #pragma unroll 4
   for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
     const int i = e / C::CS, s = e % C::CS;
@@ -246,7 +305,7 @@ __global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synt
       A[i * C::LD + s] = src[(size_t)i * WH + col0 + s];
     }
     __syncthreads();
-    const float2* X = block_fft_pp<H, C::CS, C::LD, C::T, -1>(A, B, twH);
+    const float2* X = block_fft_pp<H, C::CS, C::T, -1>(A, B, twH);
 #pragma unroll
     for (int it = 0; it < EPT; it++) {
       const int e = threadIdx.x + it * C::T;
@@ -268,7 +327,7 @@ __global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synt
     A[i * C::LD + s] = acc[it];
   }
   __syncthreads();
-  const float2* X = block_fft_pp<H, C::CS, C::LD, C::T, +1>(A, B, twH);
+  const float2* X = block_fft_pp<H, C::CS, C::T, +1>(A, B, twH);
 #pragma unroll 4
   for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
     const int i = e / C::CS, s = e % C::CS;
@@ -323,6 +382,7 @@ cudaError_t prepare_row_kernels(int wh) {
     cudaError_t e = opt_in(k_rows_fwd<n>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
+    if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 2 * sm);             \
     return e;                                                                 \
   }
     NSST_ROW_SIZES(CASE)
@@ -370,6 +430,30 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
     else                                                                               \
       k_rows_thresh<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
+  }
+    NSST_ROW_SIZES(CASE)
+#undef CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                                 void* dst_base, const float2* twWh, const float2* twW, const float* tau, int mode,
+                                 float* partials, size_t pstride, cudaStream_t st) {
+  const int WH = W / 2;
+  if (njobs == 0) return cudaSuccess;
+  count_launch();
+  const float2* sb = static_cast<const float2*>(src_base);
+  float2* db = static_cast<float2*>(dst_base);
+  switch (WH) {
+#define CASE(n)                                                                                      \
+  case n: {                                                                                          \
+    constexpr size_t sm = 2 * RowCfg<n>::smem();                                                     \
+    dim3 grid(H / RowCfg<n>::RS, njobs);                                                             \
+    k_rows_backward<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, tau, mode, \
+                                                      partials, pstride);                           \
+    return cudaGetLastError();                                                                       \
   }
     NSST_ROW_SIZES(CASE)
 #undef CASE
