@@ -186,6 +186,35 @@ nsst_status nsst_multi_create(nsst_plan* const* plans, int nplans, nsst_multi** 
 nsst_status nsst_multi_denoise(nsst_multi* m, const nsst_item* items, int n, const double* K, int mode, void* stream);
 nsst_status nsst_multi_destroy(nsst_multi* m);
 
+/* ---- Differentiation (no counterpart in the reference).  The adjoint of
+ * every stage is hand-written: transposed pyramid steps (zero-extended
+ * correlation with the unflipped filter, then the mirrored margins folded
+ * back), conjugate-spectrum directional synthesis/analysis, and the threshold
+ * subgradient 1[|c| > t] (soft rule: d/dt = -sign(c) 1[|c| > t]). */
+
+/* Allocate the gradient workspace of a plan (once; about twice the plan's
+ * own work buffers).  Required by the calls below. */
+nsst_status nsst_plan_enable_grad(nsst_plan* plan);
+
+/* x = A^T c, the adjoint of nsst_shear_trans (coeffs: nbands x H x W). */
+nsst_status nsst_shear_trans_adjoint(nsst_plan* plan, const float* coeffs, float* x, void* stream);
+
+/* c = R^T x, the adjoint of nsst_inverse_shear. */
+nsst_status nsst_inverse_shear_adjoint(nsst_plan* plan, const float* x, float* coeffs, void* stream);
+
+/* Fused denoise with explicit per-band thresholds tau (device, nbands floats,
+ * shared by the n images): out_i = R(T(A x_i, tau)). */
+nsst_status nsst_denoise_tau_batch(nsst_plan* plan, const float* const* x, float* const* out, int n,
+                                   const float* tau, int mode, void* stream);
+
+/* Backward of nsst_denoise_tau_batch: given grad_out_i = d loss / d out_i,
+ * writes grad_x_i = d loss / d x_i and grad_tau (device, nbands floats;
+ * added to when accumulate_tau != 0) = d loss / d tau summed over the images.
+ * Band coefficients are recomputed from x, not stored. */
+nsst_status nsst_denoise_tau_backward(nsst_plan* plan, const float* const* x, const float* const* grad_out,
+                                      float* const* grad_x, int n, const float* tau, float* grad_tau,
+                                      int accumulate_tau, int mode, void* stream);
+
 /* Store per-band noise scalars in the plan (nbands doubles). */
 nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
 

@@ -65,6 +65,12 @@ SIGNATURES = [
     ('nsst_multi_create', _ci, [ctypes.POINTER(_vp), _ci, ctypes.POINTER(_vp)]),
     ('nsst_multi_denoise', _ci, [_vp, ctypes.POINTER(NsstItem), _ci, _dp, _ci, _vp]),
     ('nsst_multi_destroy', _ci, [_vp]),
+    ('nsst_plan_enable_grad', _ci, [_vp]),
+    ('nsst_shear_trans_adjoint', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_inverse_shear_adjoint', _ci, [_vp, _vp, _vp, _vp]),
+    ('nsst_denoise_tau_batch', _ci, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _ci, _vp, _ci, _vp]),
+    ('nsst_denoise_tau_backward', _ci, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _ci,
+                                        _vp, _vp, _ci, _ci, _vp]),
     ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
     ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst_timers_enable', _ci, [_vp, _ci]),

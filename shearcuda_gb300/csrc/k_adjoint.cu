@@ -67,7 +67,7 @@ __global__ void k_lowpass_backward(const __grid_constant__ FoldJobs jobs, size_t
     const float c = job.z1[idx], g = job.z2[idx];
     const bool keep = fabsf(c) > t;
     job.out[idx] = keep ? g : 0.0f;
-    if (mode == THRESH_SOFT && keep) part -= copysignf(g, c);
+    if (mode == THRESH_SOFT && keep) part -= (c > 0.0f ? g : -g);  // -g sign(c)
   }
   __shared__ float red[32];
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);

@@ -190,8 +190,8 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
     float2 g = Xg[i * C::LD + s];
     const bool kx = fabsf(c.x) > th, ky = fabsf(c.y) > th;
     if (mode == THRESH_SOFT) {
-      if (kx) part -= copysignf(g.x, c.x);
-      if (ky) part -= copysignf(g.y, c.y);
+      if (kx) part -= (c.x > 0.0f ? g.x : -g.x);  // -g sign(c)
+      if (ky) part -= (c.y > 0.0f ? g.y : -g.y);
     }
     g.x = kx ? g.x : 0.0f;
     g.y = ky ? g.y : 0.0f;

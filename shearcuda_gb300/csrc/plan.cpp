@@ -49,7 +49,8 @@ struct nsst_plan {
   int H = 0, W = 0, WH = 0, nlev = 0, nbands = 0, ndir_total = 0, B = 1;
   std::vector<int> ndir, first_band, band_level;  // per level / per band
   PyramidFilters pf;
-  std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1
+  std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1 (forward steps)
+  std::vector<float> h32[4];    // FP32 unflipped h0, h1, g0, g1 (adjoint steps)
   int device = 0;
 
   // one device arena
@@ -88,6 +89,29 @@ struct nsst_plan {
   cudaGraphExec_t gexec = nullptr;
   std::vector<const void*> gkey;
   int gkey_n = -1, gkey_mode = -1;
+
+  // gradient workspace (nsst_plan_enable_grad), one allocation
+  char* garena = nullptr;
+  size_t garena_bytes = 0;
+  float* gyp = nullptr;     // B x (nlev+1) x HW   d loss / d synthesis inputs
+  float* gy = nullptr;      // B x (nlev+1) x HW   d loss / d analysis outputs
+  float* gtmp = nullptr;    // B x 2 x HW          adjoint pyramid chains
+  float* zext = nullptr;    // B x 2 x HWext       extended correlations
+  size_t s_zext = 0;        // floats per item (2 slots)
+  size_t hwext = 0;         // floats per slot
+  float2* lev2 = nullptr;   // B x nlev x HWh
+  float2* band2 = nullptr;  // B x ndir_total x HWh
+  float2* sum2 = nullptr;   // B x nlev x HWh
+  float* partials = nullptr;  // nbands x (B x ntiles)
+  int ntiles = 0;             // row tiles per band
+  RowJob* gj_rows_lev_fwd = nullptr;   // gyp[1..] -> lev2
+  ColJob* gj_cols_lev = nullptr;       // lev2 in place
+  ColJob* gj_analysis = nullptr;       // lev2 -> band2
+  RowJob* gj_rows_backward = nullptr;  // band (plan arena) + band2 -> band2
+  ColJob* gj_synthesis = nullptr;      // band2 -> sum2
+  RowJob* gj_rows_lev_inv = nullptr;   // sum2 -> gy[1..]
+  RowJob* gj_coeff_fwd = nullptr;      // caller coeffs -> band2 (item 0)
+  RowJob* gj_band_to_coeff = nullptr;  // band2 -> caller coeffs (item 0)
 
   // stage timers
   bool timing = false;
@@ -238,7 +262,10 @@ nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, 
   if (!atrous_pair_supported(p->pf.F[0], 0) || !atrous_pair_supported(p->pf.F[1], 0) ||
       !atrous_pair_supported(p->pf.F[2], p->pf.F[3]))
     return destroy(fail(NSST_ERR_INVALID_ARG, "pyramid filter sizes not compiled"));
-  for (int k = 0; k < 4; k++) p->hflip[k] = flip_to_float(p->pf.h[k], p->pf.F[k]);
+  for (int k = 0; k < 4; k++) {
+    p->hflip[k] = flip_to_float(p->pf.h[k], p->pf.F[k]);
+    p->h32[k].assign(p->pf.h[k].begin(), p->pf.h[k].end());
+  }
   // One reflection must cover the widest dilated filter (symext.m needs
   // p + shift <= image size; the coarsest level dilates by 2^(nlevels-1)).
   const int Mmax = 1 << (p->nlev - 1);
@@ -425,6 +452,7 @@ nsst_status nsst_plan_destroy(nsst_plan* p) {
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->th_done) cudaEventDestroy(p->th_done);
   if (p->th_host) cudaFreeHost(p->th_host);
+  if (p->garena) cudaFree(p->garena);
   if (p->arena) cudaFree(p->arena);
   delete p;
   return NSST_OK;
@@ -842,6 +870,323 @@ nsst_status nsst_compute_scalars(nsst_plan* p, uint64_t seed, double* out) {
   p->scalars = sc;
   p->has_scalars = true;
   if (out) std::copy(sc.begin(), sc.end(), out);
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+
+// ============================================================ adjoint / gradients
+namespace {
+
+// zext slot k of item i
+float* zslot(nsst_plan* p, int item, int k) { return p->zext + item * p->s_zext + (size_t)k * p->hwext; }
+
+// g_out = K^T g_in for one dilated filtering step (filter F, dilation M):
+// full zero-extended correlation with the unflipped filter, then fold.
+nsst_status adjoint_step(nsst_plan* p, int n, const float* const* gin, const std::vector<float>& h, int F, int M,
+                         float* const* gout, int slot, cudaStream_t st) {
+  const int H = p->H, W = p->W, E = M * (F - 1) / 2;
+  const int Ho = H + 2 * E, Wo = W + 2 * E;
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    AtrousJobs jz{};
+    FoldJobs jf{};
+    for (int t = 0; t < cn; t++) {
+      jz.j[t] = AtrousJob{gin[c0 + t], nullptr, zslot(p, c0 + t, slot), H, W, Ho, Wo};
+      jf.j[t] = FoldJob{zslot(p, c0 + t, slot), nullptr, gout[c0 + t]};
+    }
+    NSST_CUDA(launch_atrous_full(jz, cn, Ho, Wo, M, F, h.data(), st));
+    NSST_CUDA(launch_fold(jf, cn, H, W, E, 0, false, st));
+  }
+  return NSST_OK;
+}
+
+// transpose of atrousrec (atrousrec.m:18-41): g (H x W) -> gyp planes (nlev+1)
+nsst_status run_atrousrec_adjoint(nsst_plan* p, int n, const float* const* gout, float* const* gyp_base,
+                                  cudaStream_t st) {
+  const int L = p->nlev;
+  const size_t HW = (size_t)p->H * p->W;
+  const std::vector<float>& g0 = p->h32[2];
+  const std::vector<float>& g1 = p->h32[3];
+  std::vector<const float*> cur(gout, gout + n);
+  std::vector<float*> dst_hi(n), dst_lo(n);
+  for (int i = 0; i < L; i++) {  // i = 0 is the undilated last synthesis level
+    const int M = 1 << i;
+    for (int t = 0; t < n; t++) {
+      dst_hi[t] = gyp_base[t] + (size_t)(L - i) * HW;
+      dst_lo[t] = (i == L - 1) ? gyp_base[t] : p->gtmp + t * 2 * HW + (size_t)(i & 1) * HW;
+    }
+    NSST_TRY(adjoint_step(p, n, cur.data(), g1, p->pf.F[3], M, dst_hi.data(), 1, st));
+    NSST_TRY(adjoint_step(p, n, cur.data(), g0, p->pf.F[2], M, dst_lo.data(), 0, st));
+    for (int t = 0; t < n; t++) cur[t] = dst_lo[t];
+  }
+  timer_mark(p, "adjoint_atrous_rec", st);
+  return NSST_OK;
+}
+
+// transpose of atrousdec (atrousdec.m:19-51): gy planes -> gx
+nsst_status run_atrousdec_adjoint(nsst_plan* p, int n, const float* const* gy_base, float* const* gx,
+                                  cudaStream_t st) {
+  const int H = p->H, W = p->W, L = p->nlev;
+  const size_t HW = (size_t)H * W;
+  const std::vector<float>& h0 = p->h32[0];
+  const std::vector<float>& h1 = p->h32[1];
+  std::vector<const float*> glo(n);
+  for (int t = 0; t < n; t++) glo[t] = gy_base[t];  // plane 0: gradient of the final lowpass
+  for (int i = L - 1; i >= 0; i--) {
+    const int M = 1 << i;
+    const int E0 = M * (p->pf.F[0] - 1) / 2, E1 = M * (p->pf.F[1] - 1) / 2;
+    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+      const int cn = std::min(kMaxAtrousJobs, n - c0);
+      AtrousJobs ja{}, jb{};
+      FoldJobs jf{};
+      for (int t = 0; t < cn; t++) {
+        const int it = c0 + t;
+        float* out = (i == 0) ? gx[it] : p->gtmp + it * 2 * HW + (size_t)(i & 1) * HW;
+        ja.j[t] = AtrousJob{glo[it], nullptr, zslot(p, it, 0), H, W, H + 2 * E0, W + 2 * E0};
+        jb.j[t] = AtrousJob{gy_base[it] + (size_t)(L - i) * HW, nullptr, zslot(p, it, 1), H, W, H + 2 * E1,
+                            W + 2 * E1};
+        jf.j[t] = FoldJob{zslot(p, it, 0), zslot(p, it, 1), out};
+      }
+      NSST_CUDA(launch_atrous_full(ja, cn, H + 2 * E0, W + 2 * E0, M, p->pf.F[0], h0.data(), st));
+      NSST_CUDA(launch_atrous_full(jb, cn, H + 2 * E1, W + 2 * E1, M, p->pf.F[1], h1.data(), st));
+      NSST_CUDA(launch_fold(jf, cn, H, W, E0, E1, false, st));
+    }
+    for (int t = 0; t < n; t++) glo[t] = (i == 0) ? gx[t] : p->gtmp + t * 2 * HW + (size_t)(i & 1) * HW;
+  }
+  timer_mark(p, "adjoint_atrous_dec", st);
+  return NSST_OK;
+}
+
+nsst_status need_grad(nsst_plan* p) {
+  if (!p->garena) return fail(NSST_ERR_INVALID_ARG, "gradient workspace not enabled (nsst_plan_enable_grad)");
+  return NSST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_plan_enable_grad(nsst_plan* p) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->garena) return NSST_OK;
+  const int H = p->H, W = p->W, B = p->B;
+  const size_t HW = (size_t)H * W, HWh = (size_t)H * p->WH, NB = (size_t)B;
+  const int Mmax = 1 << (p->nlev - 1);
+  const int Fmax = *std::max_element(p->pf.F, p->pf.F + 4);
+  const int Emax = Mmax * (Fmax - 1) / 2;
+  p->hwext = (size_t)(H + 2 * Emax) * (W + 2 * Emax);
+  p->s_zext = 2 * p->hwext;
+  p->ntiles = H / row_tile(p->WH);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  size_t o_gyp = take(sizeof(float) * NB * (p->nlev + 1) * HW), o_gy = take(sizeof(float) * NB * (p->nlev + 1) * HW);
+  size_t o_gtmp = take(sizeof(float) * NB * 2 * HW), o_z = take(sizeof(float) * NB * p->s_zext);
+  size_t o_lev2 = take(sizeof(float2) * NB * p->nlev * HWh), o_band2 = take(sizeof(float2) * NB * p->ndir_total * HWh);
+  size_t o_sum2 = take(sizeof(float2) * NB * p->nlev * HWh);
+  size_t o_part = take(sizeof(float) * p->nbands * NB * p->ntiles);
+  const size_t nL = NB * p->nlev, nD = NB * p->ndir_total;
+  size_t o_j1 = take(sizeof(RowJob) * nL), o_j2 = take(sizeof(ColJob) * nL), o_j3 = take(sizeof(ColJob) * nD);
+  size_t o_j4 = take(sizeof(RowJob) * nD), o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
+  size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
+  cudaError_t ce = dev_alloc((void**)&p->garena, off);
+  if (ce != cudaSuccess) {
+    p->garena = nullptr;
+    return cuda_fail(ce, "gradient workspace allocation");
+  }
+  p->garena_bytes = off;
+  char* G = p->garena;
+  p->gyp = (float*)(G + o_gyp);
+  p->gy = (float*)(G + o_gy);
+  p->gtmp = (float*)(G + o_gtmp);
+  p->zext = (float*)(G + o_z);
+  p->lev2 = (float2*)(G + o_lev2);
+  p->band2 = (float2*)(G + o_band2);
+  p->sum2 = (float2*)(G + o_sum2);
+  p->partials = (float*)(G + o_part);
+  p->gj_rows_lev_fwd = (RowJob*)(G + o_j1);
+  p->gj_cols_lev = (ColJob*)(G + o_j2);
+  p->gj_analysis = (ColJob*)(G + o_j3);
+  p->gj_rows_backward = (RowJob*)(G + o_j4);
+  p->gj_synthesis = (ColJob*)(G + o_j5);
+  p->gj_rows_lev_inv = (RowJob*)(G + o_j6);
+  p->gj_coeff_fwd = (RowJob*)(G + o_j7);
+  p->gj_band_to_coeff = (RowJob*)(G + o_j8);
+  auto g2 = [&](const void* ptr) { return (size_t)((const char*)ptr - G) / sizeof(float2); };
+  auto a2 = [&](const void* ptr) { return (size_t)((const char*)ptr - p->arena) / sizeof(float2); };
+  std::vector<RowJob> j1, j4, j6, j7, j8;
+  std::vector<ColJob> j2, j3, j5;
+  for (int i = 0; i < B; i++) {
+    const size_t gyp = g2(p->gyp + i * (p->nlev + 1) * HW), gy = g2(p->gy + i * (p->nlev + 1) * HW);
+    const size_t lev = g2(p->lev2 + i * p->s_lev), sum = g2(p->sum2 + i * p->s_sum);
+    for (int l = 0; l < p->nlev; l++) {
+      j1.push_back(RowJob{gyp + (size_t)(l + 1) * HWh, lev + (size_t)l * HWh, 0, i});
+      j2.push_back(ColJob{lev + (size_t)l * HWh, lev + (size_t)l * HWh, 0, 0, 0, i});
+      j6.push_back(RowJob{sum + (size_t)l * HWh, gy + (size_t)(l + 1) * HWh, 0, i});
+    }
+  }
+  for (int b = 0; b < p->ndir_total; b++) {
+    const int l = p->band_level[1 + b] - 1;
+    for (int i = 0; i < B; i++) {
+      const size_t lev = g2(p->lev2 + i * p->s_lev), band2 = g2(p->band2 + i * p->s_band);
+      const size_t band = a2(p->band + i * p->s_band);
+      j3.push_back(ColJob{lev + (size_t)l * HWh, band2 + (size_t)b * HWh, (size_t)b * HWh, p->m0_off + (size_t)b * H,
+                          1, i});
+      j4.push_back(RowJob{band + (size_t)b * HWh, band2 + (size_t)b * HWh, 1 + b, i});
+    }
+  }
+  for (int l = 0; l < p->nlev; l++)
+    for (int i = 0; i < B; i++) {
+      const size_t band2 = g2(p->band2 + i * p->s_band), sum = g2(p->sum2 + i * p->s_sum);
+      j5.push_back(ColJob{band2 + (size_t)p->first_band[l] * HWh, sum + (size_t)l * HWh,
+                          (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], i});
+    }
+  for (int b = 0; b < p->ndir_total; b++) {
+    const size_t band20 = g2(p->band2);
+    j7.push_back(RowJob{(size_t)(1 + b) * HWh, band20 + (size_t)b * HWh, 1 + b, 0});
+    j8.push_back(RowJob{band20 + (size_t)b * HWh, (size_t)(1 + b) * HWh, 1 + b, 0});
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) { return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice); };
+  ce = up(p->gj_rows_lev_fwd, j1.data(), j1.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_cols_lev, j2.data(), j2.size() * sizeof(ColJob));
+  if (ce == cudaSuccess) ce = up(p->gj_analysis, j3.data(), j3.size() * sizeof(ColJob));
+  if (ce == cudaSuccess) ce = up(p->gj_rows_backward, j4.data(), j4.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_synthesis, j5.data(), j5.size() * sizeof(ColJob));
+  if (ce == cudaSuccess) ce = up(p->gj_rows_lev_inv, j6.data(), j6.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_coeff_fwd, j7.data(), j7.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
+  if (ce != cudaSuccess) return cuda_fail(ce, "upload gradient job lists");
+  for (int F : {p->pf.F[0], p->pf.F[1], p->pf.F[2], p->pf.F[3]}) {
+    ce = prepare_atrous_kernels(F, 0, Mmax);
+    if (ce != cudaSuccess) return cuda_fail(ce, "adjoint kernel set-up");
+  }
+  return NSST_OK;
+}
+
+// x = A^T c: adjoint of nsst_shear_trans (directional synthesis with conj
+// spectra, then the transpose of the analysis pyramid).
+nsst_status nsst_shear_trans_adjoint(nsst_plan* p, const float* coeffs, float* x, void* stream) {
+  if (!p || !coeffs || !x) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(need_grad(p));
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  char* G = p->garena;
+  float2* G2 = (float2*)G;
+  const size_t HW = (size_t)p->H * p->W;
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_coeff_fwd, p->ndir_total, 1, p->H, p->W, coeffs, G, p->twWh, p->twW,
+                        nullptr, 0, st));
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synthesis, p->B * p->nlev, 1, p->H, p->W, G2, G2, p->spec,
+                        (size_t)p->H * p->WH, p->twH, st));
+  NSST_CUDA(launch_rows(RowOp::Inv, p->gj_rows_lev_inv, p->nlev, 1, p->H, p->W, G, G, p->twWh, p->twW, nullptr, 0,
+                        st));
+  NSST_CUDA(cudaMemcpyAsync(p->gy, coeffs, HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  const float* gyb = p->gy;
+  return run_atrousdec_adjoint(p, 1, &gyb, &x, st);
+}
+
+// c = R^T x: adjoint of nsst_inverse_shear (transpose of the synthesis pyramid,
+// then the directional analysis).
+nsst_status nsst_inverse_shear_adjoint(nsst_plan* p, const float* x, float* coeffs, void* stream) {
+  if (!p || !coeffs || !x) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
+  NSST_TRY(need_grad(p));
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  char* G = p->garena;
+  float2* G2 = (float2*)G;
+  const size_t HW = (size_t)p->H * p->W;
+  float* gypb = p->gyp;
+  NSST_TRY(run_atrousrec_adjoint(p, 1, &x, &gypb, st));
+  NSST_CUDA(cudaMemcpyAsync(coeffs, p->gyp, HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_rows_lev_fwd, p->nlev, 1, p->H, p->W, G, G, p->twWh, p->twW, nullptr, 0,
+                        st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->gj_cols_lev, p->nlev, 1, p->H, p->W, G2, G2, nullptr, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->gj_analysis, p->B * p->ndir_total, 1, p->H, p->W, G2, G2, p->spec, 0,
+                        p->twH, st));
+  NSST_CUDA(launch_rows(RowOp::Inv, p->gj_band_to_coeff, p->ndir_total, 1, p->H, p->W, G, coeffs, p->twWh, p->twW,
+                        nullptr, 0, st));
+  return NSST_OK;
+}
+
+nsst_status nsst_denoise_tau_batch(nsst_plan* p, const float* const* x, float* const* out, int n, const float* tau,
+                                   int mode, void* stream) {
+  if (!p || !x || !out || !tau) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  for (int i = 0; i < n; i++)
+    if (!x[i] || !out[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  NSST_CUDA(launch_broadcast_tau(tau, p->th, p->nbands, n, st));
+  return enqueue_denoise(p, n, x, out, mode, true, st);
+}
+
+nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const float* const* grad_out,
+                                      float* const* grad_x, int n, const float* tau, float* grad_tau,
+                                      int accumulate_tau, int mode, void* stream) {
+  if (!p || !x || !grad_out || !grad_x || !tau || !grad_tau) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  NSST_TRY(need_grad(p));
+  for (int i = 0; i < n; i++)
+    if (!x[i] || !grad_out[i] || !grad_x[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  char* A = p->arena;
+  float2* A2 = (float2*)A;
+  char* G = p->garena;
+  float2* G2 = (float2*)G;
+  const int H = p->H, W = p->W, B = p->B;
+  const size_t HW = (size_t)H * W;
+  // 1. recompute the coefficient spectra of x (they are not stored)
+  std::vector<float*> ys(n), gyp(n), gy(n);
+  for (int i = 0; i < n; i++) {
+    ys[i] = p->pyr + i * p->s_pyr;
+    gyp[i] = p->gyp + i * (p->nlev + 1) * HW;
+    gy[i] = p->gy + i * (p->nlev + 1) * HW;
+  }
+  NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
+  timer_mark(p, "recompute_coefficients", st);
+  // 2. d loss / d thresholded coefficients = D P_s^T grad_out
+  NSST_TRY(run_atrousrec_adjoint(p, n, grad_out, gyp.data(), st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_rows_lev_fwd, B * p->nlev, n, H, W, G, G, p->twWh, p->twW, nullptr, 0, st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->gj_cols_lev, B * p->nlev, n, H, W, G2, G2, nullptr, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->gj_analysis, B * p->ndir_total, n, H, W, G2, G2, p->spec, 0, p->twH, st));
+  timer_mark(p, "gradient_analysis", st);
+  // 3. threshold subgradient per band (+ tau partials), then D^T
+  const size_t pstride = (size_t)B * p->ntiles;
+  NSST_CUDA(launch_rows_backward(p->gj_rows_backward, B * p->ndir_total, n, H, W, A, G, p->twWh, p->twW, tau, mode,
+                                 p->partials, pstride, st));
+  timer_mark(p, "band_rows_backward", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synthesis, B * p->nlev, n, H, W, G2, G2, p->spec, (size_t)H * p->WH,
+                        p->twH, st));
+  NSST_CUDA(launch_rows(RowOp::Inv, p->gj_rows_lev_inv, B * p->nlev, n, H, W, G, G, p->twWh, p->twW, nullptr, 0, st));
+  timer_mark(p, "gradient_synthesis", st);
+  // lowpass band
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    FoldJobs jl{};
+    for (int t = 0; t < cn; t++) jl.j[t] = FoldJob{ys[c0 + t], gyp[c0 + t], gy[c0 + t]};
+    NSST_CUDA(launch_lowpass_backward(jl, cn, HW, tau, mode, p->partials, c0 * p->ntiles, p->ntiles, st));
+  }
+  // 4. d loss / d x = P^T g_y
+  std::vector<const float*> gyc(gy.begin(), gy.end());
+  NSST_TRY(run_atrousdec_adjoint(p, n, gyc.data(), grad_x, st));
+  NSST_CUDA(launch_reduce_tau(p->partials, n * p->ntiles, pstride, p->nbands, grad_tau, accumulate_tau != 0, st));
+  timer_mark(p, "reduce_tau", st);
   return NSST_OK;
 }
 

@@ -83,3 +83,45 @@ def test_threshold_rules():
     np.testing.assert_array_equal(ht[1], [[[0.0, -2.5], [0.0, -4.0]]])  # strict >
     st = nsst2d.nsst_ST(d, 1.0, [0, 2], [1.0, np.array([1.0])])
     np.testing.assert_allclose(st[1], [[[0.0, -0.5], [0.0, -2.0]]])
+
+
+def test_oracle_pyramid_adjoints_dot_product():
+    rng = np.random.default_rng(11)
+    H = W = 192
+    x = rng.standard_normal((H, W))
+    gy = [rng.standard_normal((H, W)) for _ in range(5)]
+    y = nsst2d.atrousdec(x, nlevels=4, conv='numpy')
+    lhs = sum(np.sum(a * b) for a, b in zip(y, gy))
+    rhs = np.sum(x * nsst2d.atrousdec_adjoint(gy))
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+    xr = nsst2d.atrousrec(gy, conv='numpy')
+    g = rng.standard_normal((H, W))
+    lhs = np.sum(xr * g)
+    rhs = sum(np.sum(a * b) for a, b in zip(gy, nsst2d.atrousrec_adjoint(g, 4)))
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+
+
+def test_oracle_loss_gradient_finite_differences():
+    from shearcuda_gb300.synth import noisy_image
+    H = W = 160
+    sf = nsst2d.shear_spectra(H, W, [2, 3], [16, 16])
+    clean, noisy = noisy_image(H, W, 20.0, 3)
+    tau = [10.0, np.full(4, 20.0), np.full(8, 15.0)]
+    loss, gx, gt = nsst2d.denoise_tau_grad(noisy, tau, clean, sf, nthreads=4)
+    rng = np.random.default_rng(2)
+    h = 1e-4
+    for _ in range(4):
+        i, j = int(rng.integers(0, H)), int(rng.integers(0, W))
+        xp, xm = noisy.copy(), noisy.copy()
+        xp[i, j] += h
+        xm[i, j] -= h
+        fd = (np.sum((nsst2d.denoise_tau(xp, tau, sf, nthreads=4)[0] - clean) ** 2) -
+              np.sum((nsst2d.denoise_tau(xm, tau, sf, nthreads=4)[0] - clean) ** 2)) / (2 * h)
+        assert abs(fd - gx[i, j]) <= 1e-3 * max(1.0, abs(fd))
+    tp = [tau[0], tau[1].copy(), tau[2].copy()]
+    tm = [tau[0], tau[1].copy(), tau[2].copy()]
+    tp[2][3] += h
+    tm[2][3] -= h
+    fd = (np.sum((nsst2d.denoise_tau(noisy, tp, sf, nthreads=4)[0] - clean) ** 2) -
+          np.sum((nsst2d.denoise_tau(noisy, tm, sf, nthreads=4)[0] - clean) ** 2)) / (2 * h)
+    assert abs(fd - gt[2][3]) <= 1e-3 * max(1.0, abs(fd))
