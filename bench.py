@@ -374,6 +374,44 @@ def run_gpu(args):
         m.close()
         del plans
 
+        # ---- differentiable config: 16 x 512^2, forward vs forward + hand-written adjoint
+        pd = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=16)
+        sc.autograd.enable_grad(pd)
+        sd = sc.nsst_scalars(pd, seed=100)
+        lv = pd.band_levels
+        tau = torch.tensor([3.0 * SIGMA * sd[b] for b in range(pd.nbands)], dtype=torch.float32, device=dev)
+        xd = torch.stack(xs[:16]).contiguous()
+        cd = torch.stack([torch.tensor(noisy_image(H, W, 0.0, 1000 * rank + i)[0].astype(np.float32), device=dev)
+                          for i in range(16)])
+        def fwd():
+            with torch.no_grad():
+                return sc.nsst_denoise_diff(xd, tau, pd)
+        def fwd_bwd():
+            xg = xd.clone().requires_grad_(True)
+            tg = tau.clone().requires_grad_(True)
+            loss = torch.sum((sc.nsst_denoise_diff(xg, tg, pd) - cd) ** 2)
+            loss.backward()
+            return xg.grad, tg.grad
+        for f in (fwd, fwd_bwd):
+            for _ in range(3):
+                f()
+        torch.cuda.synchronize()
+        res = {}
+        for name, f in (('forward_ms', fwd), ('forward_adjoint_ms', fwd_bwd)):
+            tt = 0.0
+            for _ in range(5):
+                flush.fill_(1.0)
+                e0.record(stream)
+                f()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tt += e0.elapsed_time(e1)
+            res[name] = tt / 5
+        res['ratio'] = res['forward_adjoint_ms'] / res['forward_ms']
+        res['images'] = 16
+        line['differentiable_d16'] = res
+        del pd
+
     if rank == 0:
         cb = cpu_baseline()
         line['cpu_baseline'] = cb

@@ -242,6 +242,88 @@ uint64_t nsst_launch_count(void);
  * NSST_ERR_OUT_OF_MEMORY (n <= 0 disarms).  Host-side fault injection only. */
 void nsst_debug_fail_next_alloc(int n);
 
+/* ------------------------------------------------------------------------
+ * 3-D path: Fourier-domain band-pass pyramid (shearcuda3d/3DBP, Pyr_mode 1.5)
+ * and 24^3 pseudo-polar Meyer directional filters applied by linear 'same'
+ * convolution (shearcuda3d/3DShearTrans, CONVNFFT_Folder/convnfft.m).
+ *
+ * Volumes are float32 n0 x n1 x n2, index (x*n1 + y)*n2 + z (axis 2 fastest);
+ * axis k plays the role of MATLAB dimension k+1, and the pyramid's half
+ * spectrum lies along axis 2 as ccsym(X, 3, 'c') does.  The plan pads each
+ * dimension by edge replication (MarshalData.m:3-22) to a grid of 96, 144 or
+ * 192 so that every level size is a 2^a 3^b transform length, and crops the
+ * reconstruction back.
+ *
+ * Sub-band layout ("bp", per volume): level 0 (finest) band-pass of
+ * m_0 = grid dims, level 1 of 2/3 of it, level 2 of 1/3, ..., then the lowpass;
+ * concatenated, nsst3_subband_floats() floats per volume.  Directional bands
+ * are ordered level-major, then cone (after the swap of cones 1 and 2 of
+ * GetMeyerBasedFilter.m:148-150), then l2, then l1.
+ * ------------------------------------------------------------------------ */
+typedef struct nsst3_plan nsst3_plan;
+
+typedef struct nsst3_config {
+  int nlevels;                   /* pyramid levels, 1..4 (the demo uses 3) */
+  int num_dirs[NSST_MAX_LEVELS]; /* numDir per level, finest first; 3*numDir^2 bands per level (numDir | 24) */
+  double pyr_mode;               /* 1, 1.5 or 2 (PyrNDDec_mm.m:58-74); 1.5 in the demo */
+} nsst3_config;
+
+/* Plan for batches of up to `batch` volumes of n0 x n1 x n2 (each <= 192).
+ * Builds the FP64 Meyer filters, their convolution spectra (FP32 on the
+ * device) and the pyramid windows; allocates every work buffer.
+ * Replaces GetMeyerBasedFilter.m + the per-call cuFFT plans and filter FFTs
+ * of ShDecThRec_cuda.cpp:178-335. */
+nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, int batch, nsst3_plan** plan);
+nsst_status nsst3_plan_destroy(nsst3_plan* plan);
+int nsst3_num_bands(const nsst3_plan* plan);           /* directional bands over all levels */
+size_t nsst3_subband_floats(const nsst3_plan* plan);   /* floats per volume of the sub-band layout */
+size_t nsst3_plan_device_bytes(const nsst3_plan* plan);
+/* level -1: dims[0..2] = the padded grid; level l in [0, nlevels]: dims of band-pass l
+ * (l = nlevels: lowpass) and conv[0..2] = its convolution FFT lengths. */
+nsst_status nsst3_level_dims(const nsst3_plan* plan, int level, int* dims, int* conv);
+/* level, cone, l2, l1 of directional band b. */
+nsst_status nsst3_band_info(const nsst3_plan* plan, int band, int* info4);
+
+/* FP64 Meyer filters of GetMeyerBasedFilter.m:12-150 (cube 24): writes
+ * sum_l 3*num_dirs[l]^2 filters of 24^3 doubles in band order when out is not
+ * NULL; returns the filter count (or -1 on a bad argument).  Host only. */
+int nsst3_meyer_filters(int nlevels, const int* num_dirs, double* out);
+
+/* Band-pass pyramid of n volumes (device x, n*n0*n1*n2 floats contiguous) into
+ * bp (device, n * nsst3_subband_floats).  Replaces MarshalData.m + DoPyrDec.m
+ * (PyrNDDec_mm.m:20-109). */
+nsst_status nsst3_pyr_dec(nsst3_plan* plan, const float* x, float* bp, int n, void* stream);
+/* Inverse: bp -> x (n0 x n1 x n2, the grid cropped).  Replaces DoPyrRec.m
+ * (PyrNDRec_mm.m:20-95). */
+nsst_status nsst3_pyr_rec(nsst3_plan* plan, const float* bp, float* x, int n, void* stream);
+
+/* Directional coefficients of one pyramid level (ShDec.m:18-34, one level,
+ * every cone): coeffs (device) receives, per volume, 3*numDir^2 volumes of
+ * that level's band-pass size in band order. */
+nsst_status nsst3_sh_dec(nsst3_plan* plan, const float* bp, int level, float* coeffs, int n, void* stream);
+
+/* ShDecThRec_cuda (ShDecThRec_cuda.cpp:57-335): for each level, sum over all
+ * bands of the directional coefficients hard-thresholded at
+ * T[level] * sigma[i] * scalars[band] (ThresholdShCoeff.m:7 zeroes
+ * |c| <= t); the lowpass is copied unchanged.  bp -> rec_bp, same layout.
+ * sigma: n doubles (host), T: nlevels doubles, scalars: nsst3_num_bands
+ * doubles (NULL = the plan's stored scalars). */
+nsst_status nsst3_sh_dec_thresh_rec(nsst3_plan* plan, const float* bp, float* rec_bp, int n, const double* sigma,
+                                    const double* T, const double* scalars, void* stream);
+
+/* The whole 3-D denoise of DenoiseDemo/main.m:80-145 for n volumes: pad,
+ * pyramid, directional hard threshold + band sum, pyramid reconstruction,
+ * crop.  x, out: device, n*n0*n1*n2 floats. */
+nsst_status nsst3_denoise_batch(nsst3_plan* plan, const float* x, float* out, int n, const double* sigma,
+                                const double* T, const double* scalars, void* stream);
+
+/* NsstScalars.m:1-19: a seeded N(0,1) grid-sized volume (FP64 on the host)
+ * is decomposed on the GPU and each band's MAD/0.6745 is taken on the host in
+ * FP64.  Writes nsst3_num_bands doubles to out and stores them in the plan.
+ * Synchronous. */
+nsst_status nsst3_compute_scalars(nsst3_plan* plan, uint64_t seed, double* out);
+nsst_status nsst3_plan_set_scalars(nsst3_plan* plan, const double* scalars);
+
 #ifdef __cplusplus
 }
 #endif

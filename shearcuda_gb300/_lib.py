@@ -28,6 +28,10 @@ class NsstItem(ctypes.Structure):
     _fields_ = [('x', ctypes.c_void_p), ('out', ctypes.c_void_p), ('sigma', ctypes.c_double), ('plan', ctypes.c_int)]
 
 
+class Nsst3Config(ctypes.Structure):
+    _fields_ = [('nlevels', ctypes.c_int), ('num_dirs', ctypes.c_int * MAX_LEVELS), ('pyr_mode', ctypes.c_double)]
+
+
 class NsstError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__('%s: %s' % (STATUS_NAMES.get(status, status), msg))
@@ -77,6 +81,21 @@ SIGNATURES = [
     ('nsst_timers_read', _ci, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_float), _ci]),
     ('nsst_launch_count', ctypes.c_uint64, []),
     ('nsst_debug_fail_next_alloc', None, [_ci]),
+    ('nsst3_plan_create', _ci, [ctypes.POINTER(Nsst3Config), _ci, _ci, _ci, _ci, ctypes.POINTER(_vp)]),
+    ('nsst3_plan_destroy', _ci, [_vp]),
+    ('nsst3_num_bands', _ci, [_vp]),
+    ('nsst3_subband_floats', _sz, [_vp]),
+    ('nsst3_plan_device_bytes', _sz, [_vp]),
+    ('nsst3_level_dims', _ci, [_vp, _ci, _ip, _ip]),
+    ('nsst3_band_info', _ci, [_vp, _ci, _ip]),
+    ('nsst3_meyer_filters', _ci, [_ci, _ip, _dp]),
+    ('nsst3_pyr_dec', _ci, [_vp, _vp, _vp, _ci, _vp]),
+    ('nsst3_pyr_rec', _ci, [_vp, _vp, _vp, _ci, _vp]),
+    ('nsst3_sh_dec', _ci, [_vp, _vp, _ci, _vp, _ci, _vp]),
+    ('nsst3_sh_dec_thresh_rec', _ci, [_vp, _vp, _vp, _ci, _dp, _dp, _dp, _vp]),
+    ('nsst3_denoise_batch', _ci, [_vp, _vp, _vp, _ci, _dp, _dp, _dp, _vp]),
+    ('nsst3_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
+    ('nsst3_plan_set_scalars', _ci, [_vp, _dp]),
 ]
 
 _lib = None

@@ -117,7 +117,13 @@ struct RadixList {};
 
 template <int N>
 struct FftPlan;
+template <> struct FftPlan<16> { using type = RadixList<4, 4>; };
+template <> struct FftPlan<24> { using type = RadixList<3, 8>; };
+template <> struct FftPlan<32> { using type = RadixList<4, 8>; };
+template <> struct FftPlan<48> { using type = RadixList<3, 4, 4>; };
 template <> struct FftPlan<64> { using type = RadixList<8, 8>; };
+template <> struct FftPlan<72> { using type = RadixList<3, 3, 8>; };
+template <> struct FftPlan<144> { using type = RadixList<3, 3, 4, 4>; };
 template <> struct FftPlan<96> { using type = RadixList<3, 4, 8>; };
 template <> struct FftPlan<128> { using type = RadixList<8, 4, 4>; };
 template <> struct FftPlan<192> { using type = RadixList<3, 8, 8>; };

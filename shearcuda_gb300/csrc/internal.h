@@ -124,6 +124,48 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
                                  float* partials, size_t pstride, cudaStream_t st);
 cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
 
+// ------------------------------------------------------------------- 3-D path
+struct V3Axis {  // one axis of a batched 3-D FFT
+  int axis, d2;
+  long long nseq, si, ss;
+  size_t item_stride;
+};
+struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)
+  int K[3];
+  int nr[3];
+  const float* v0;
+  const float* v1;
+  const float* v2;
+};
+bool fft3_len_supported(int n);
+cudaError_t prepare_fft3(int n);
+cudaError_t launch_fft3_axis(float2* vol, int nitems, size_t item_stride, int d0, int d1, int d2, int axis, int dir,
+                             const float2* tw, cudaStream_t st);
+cudaError_t launch_pad_real(const float* in, size_t in_stride, float2* out, size_t out_stride, int n, int m0, int m1,
+                            int m2, int L0, int L1, int L2, cudaStream_t st);
+cudaError_t launch_pad_edge(const float* in, size_t in_stride, float2* out, size_t out_stride, int n, int n0, int n1,
+                            int n2, int d0, int d1, int d2, cudaStream_t st);
+cudaError_t launch_crop_real(const float2* in, size_t in_stride, float* out, size_t out_stride, int n, int m0, int m1,
+                             int m2, int L1, int L2, int o0, int o1, int o2, float scale, cudaStream_t st);
+cudaError_t launch_half(const float2* in, size_t in_stride, float2* out, size_t out_stride, int n, int d0, int d1,
+                        int d2, cudaStream_t st);
+cudaError_t launch_conj_extend(const float2* in, size_t in_stride, float2* out, size_t out_stride, int n, int d0,
+                               int d1, int d2, cudaStream_t st);
+cudaError_t launch_pyr_dec(float2* Xh, size_t stride, float2* Lp, size_t lp_stride, int n, int d0, int d1, int d2,
+                           int s0, int s1, int s2, const PyrWin& w, float invDN, cudaStream_t st);
+cudaError_t launch_pyr_rec(float2* Hh, size_t stride, const float2* Lp, size_t lp_stride, int n, int d0, int d1,
+                           int d2, int s0, int s1, int s2, const PyrWin& w, float DN, cudaStream_t st);
+cudaError_t launch_band_pair(const float2* Y, size_t y_stride, const float2* Fa, const float2* Fb, float2* W,
+                             size_t w_stride, int n, size_t total, cudaStream_t st);
+cudaError_t launch_crop_pair(const float2* W, size_t w_stride, float* out_a, float* out_b, size_t o_stride, int n,
+                            int m0, int m1, int m2, int L1, int L2, int off, float scale, cudaStream_t st);
+cudaError_t launch_crop_thresh_acc(const float2* W, size_t w_stride, float* acc, size_t a_stride, int n, int m0,
+                                   int m1, int m2, int L1, int L2, int off, const float* th, int ia, int ib,
+                                   int nb_item, float scale, cudaStream_t st);
+std::vector<double> meyer_filters_3d(int cube, int nlevels, const int* num_dirs);
+void filter_spectrum_3d(const double* f, int cube, int L0, int L1, int L2, std::vector<std::complex<double>>* out);
+void pyr_window_1d(int nr, double w, double tbw, int* K, std::vector<double>* v);
+
 // ------------------------------------------------------- host-side FP64 math
 using cd = std::complex<double>;
 
@@ -154,6 +196,9 @@ std::vector<float2> half_twiddle_table(int n);       // exp(-2 pi i k / n), k < 
 
 // error reporting
 void set_error(const std::string& msg);
+
+// cudaMalloc behind the allocation fault-injection hook
+cudaError_t dev_alloc(void** p, size_t bytes);
 
 // launch accounting (every kernel launch site calls this once per launch)
 void count_launch(int n = 1);

@@ -29,7 +29,7 @@ static std::atomic<int> g_fail_alloc_countdown{0};
 static std::atomic<uint64_t> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
-static cudaError_t dev_alloc(void** p, size_t bytes) {
+cudaError_t dev_alloc(void** p, size_t bytes) {
   int c = g_fail_alloc_countdown.load();
   if (c > 0) {
     if (g_fail_alloc_countdown.fetch_sub(1) == 1) {

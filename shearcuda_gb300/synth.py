@@ -51,3 +51,34 @@ def uneven_batch(n, seed, sizes=BATCH_SIZES, sigma_range=(10.0, 40.0)):
         clean, noisy = noisy_image(H, W, sigma, seed * 100003 + i)
         out.append((clean, noisy, sigma))
     return out
+
+
+def clean_volume(shape, rng, n_ellipsoids=None):
+    """A sequence-like volume: 1-12 random ellipsoids (centre uniform,
+    semi-axes U[0.05, 0.3] * min(shape), intensity U[0, 255]) whose centres
+    move linearly along axis 2 (the time axis of a video volume) at a random
+    velocity of up to 0.3 voxel per plane, over a constant background U[0, 64]."""
+    n0, n1, n2 = shape
+    x0 = np.arange(n0, dtype=np.float64)[:, None, None]
+    x1 = np.arange(n1, dtype=np.float64)[None, :, None]
+    t = np.arange(n2, dtype=np.float64)[None, None, :]
+    vol = np.full(shape, rng.uniform(0, 64))
+    m = min(shape)
+    for _ in range(int(n_ellipsoids or rng.integers(1, 13))):
+        c = rng.uniform(0, 1, size=3) * np.array(shape)
+        ax = rng.uniform(0.05, 0.3, size=3) * m
+        vel = rng.uniform(-0.3, 0.3, size=2)
+        val = rng.uniform(0, 255)
+        d0 = (x0 - c[0] - vel[0] * t) / ax[0]
+        d1 = (x1 - c[1] - vel[1] * t) / ax[1]
+        d2 = (t - c[2]) / ax[2]
+        vol[d0 * d0 + d1 * d1 + d2 * d2 <= 1.0] = val
+    return vol
+
+
+def noisy_volume(shape, sigma, seed):
+    """(clean, noisy) FP64 volume pair for one seed."""
+    rng = np.random.default_rng(seed)
+    clean = clean_volume(tuple(shape), rng)
+    noisy = clean + sigma * rng.standard_normal(tuple(shape))
+    return clean, noisy

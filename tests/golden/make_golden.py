@@ -17,6 +17,12 @@ It writes two kinds of fixtures, both small enough to commit:
   ``oracle/mex_shim``; see ``oracle/build_oracle.py``) on seeded random
   signals, for every (filter size, dilation) pair the 4-level pyramid uses,
   plus odd-sized ragged cases.  These pin the C and NumPy restatements.
+* ``nsst3_scalar_tables.json``: the 3-D noise scalars the reference ships
+  (``shearcuda3d/DenoiseDemo/nsstScalarsData*.mat``, written by
+  NsstScalars.m:1-19 — Monte-Carlo MAD/0.6745 per band of N(0,1) noise for
+  the demo's data size), flattened to the band order level, cone, l2, l1.
+  They pin the 3-D pyramid windows, the Meyer filters and the band order to
+  within the Monte-Carlo and data-size spread.
 """
 import argparse
 import json
@@ -112,6 +118,31 @@ def atrousc_cases(seed=1234):
     return cases
 
 
+def scalar_tables3(reference):
+    """nsstScalarsData<level><dBand digits>.mat -> {name: {num_dirs, lowpass, bands}}."""
+    import scipy.io as sio
+    out = {}
+    demo = os.path.join(reference, 'shearcuda3d', 'DenoiseDemo')
+    for fn in sorted(os.listdir(demo)):
+        m = re.match(r'nsstScalarsData(\d+)\.mat$', fn)
+        if not m:
+            continue
+        digits = m.group(1)
+        level = int(digits[0])
+        if len(digits) != 1 + 2 * level:
+            continue
+        num_dirs = [int(digits[1 + 2 * l]) for l in range(level)]
+        s = sio.loadmat(os.path.join(demo, fn), squeeze_me=True, struct_as_record=False)['nsstScalars']
+        be = np.asarray(s.bandEst, dtype=object).reshape(3, level)
+        bands = []
+        for l in range(level):
+            for c in range(3):
+                tab = np.asarray(be[c, l], dtype=np.float64).reshape(num_dirs[l], num_dirs[l])
+                bands.extend(float(v) for v in tab.ravel())  # (l2, l1) row-major
+        out[digits] = {'num_dirs': num_dirs, 'lowpass': float(s.lowPassEst), 'bands': bands}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference')
@@ -120,6 +151,8 @@ def main():
     with open(os.path.join(HERE, 'pyramid_filter_tables.json'), 'w') as f:
         json.dump(tables, f, indent=1)
     np.savez_compressed(os.path.join(HERE, 'atrousc_ref_cases.npz'), **atrousc_cases())
+    with open(os.path.join(HERE, 'nsst3_scalar_tables.json'), 'w') as f:
+        json.dump(scalar_tables3(args.reference), f, indent=1)
     print('wrote', os.listdir(HERE))
 
 
