@@ -324,6 +324,20 @@ nsst_status nsst3_denoise_batch(nsst3_plan* plan, const float* x, float* out, in
 nsst_status nsst3_compute_scalars(nsst3_plan* plan, uint64_t seed, double* out);
 nsst_status nsst3_plan_set_scalars(nsst3_plan* plan, const double* scalars);
 
+/* Differentiation of nsst3_denoise_batch (no counterpart in the reference).
+ * nsst3_plan_enable_grad allocates one keep bit per directional coefficient
+ * and batch item; from then on nsst3_denoise_batch records the masks
+ * |c| > t of its hard threshold.  nsst3_denoise_backward then maps
+ * gy = d loss / d out (device, n volumes) to gx = d loss / d x (device, n
+ * volumes) for the n volumes of the most recent nsst3_denoise_batch on this
+ * plan (the threshold's subgradient keeps that call's masks).  The adjoint
+ * steps: zero-padding of gy, the pyramid decomposition (the band-pass pyramid
+ * is a Parseval frame, so it is the reconstruction's adjoint), per band the
+ * masked gradient correlated with the filter (conjugate spectrum), the
+ * pyramid reconstruction, and the fold of the edge padding. */
+nsst_status nsst3_plan_enable_grad(nsst3_plan* plan);
+nsst_status nsst3_denoise_backward(nsst3_plan* plan, const float* gy, float* gx, int n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

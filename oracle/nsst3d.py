@@ -340,14 +340,36 @@ def denoise3(x, F, sigma, T, band_scalars, L=3, mode=1.5):
     return pyr_rec(rec, mode)
 
 
-PAD_GRIDS = (96, 144, 192)
+FFT_LENS = (16, 24, 32, 48, 64, 72, 96, 128, 144, 192, 256)
 
 
-def pad_size(n):
-    """Smallest supported grid (96, 144, 192) >= n."""
-    for d in PAD_GRIDS:
-        if d >= n:
-            return d
+def level_sizes(g, L=3, mode=1.5):
+    """Level sizes g, g/D0, g/D0/D1, ... of a grid, or None when one of them
+    is not a supported transform length (2^a 3^b, multiple of 8) or has no
+    supported linear-convolution length (>= m + 23)."""
+    D = pyr_params(mode, L)[2]
+    conv = lambda m: next((v for v in FFT_LENS if v >= m + 23), None)
+    out = [g]
+    if g not in FFT_LENS or conv(g) is None:
+        return None
+    v = float(g)
+    for l in range(L):
+        v /= D[l]
+        iv = int(round(v))
+        if abs(v - iv) > 1e-9 or iv not in FFT_LENS or iv % 8:
+            return None
+        if l + 1 < L and conv(iv) is None:
+            return None
+        out.append(iv)
+    return out
+
+
+def pad_size(n, L=3, mode=1.5):
+    """Smallest grid >= n (at most 192) whose level sizes all work; for the
+    3-level Pyr_mode 1.5 pyramid these are 96, 144 and 192."""
+    for g in FFT_LENS:
+        if n <= g <= 192 and level_sizes(g, L, mode):
+            return g
     raise ValueError('volume dimension %d larger than 192' % n)
 
 
@@ -366,3 +388,73 @@ def psnr3(ref, x):
 def pad_volume_to(x, grid):
     """Edge replication of x up to the given grid dims."""
     return np.pad(x, [(0, g - s) for s, g in zip(x.shape, grid)], mode='edge')
+
+
+# ----------------------------------------------------------------------------
+# Adjoint of the 3-D denoise (hard threshold: the subgradient keeps the mask of
+# the forward pass fixed).  The band-pass pyramid is a Parseval frame, so
+# pyr_rec is the exact adjoint of pyr_dec and vice versa (checked by
+# test_oracle3d.py); the adjoint of convnfft 'same' is the correlation
+# corr_same below; the adjoint of edge padding folds the padded planes back.
+# ----------------------------------------------------------------------------
+def corr_same(G, B):
+    """Adjoint of convnfft_same(., B) for an output G of A's shape: place G at
+    offset ceil((n-1)/2) of the linear-convolution domain, correlate with B and
+    keep the first A.shape samples."""
+    sl = []
+    L = []
+    for dim in range(G.ndim):
+        m, n = G.shape[dim], B.shape[dim]
+        L.append(2 ** math.ceil(math.log2(m + n - 1)))
+        s0 = math.ceil((n - 1) / 2)
+        sl.append(slice(s0, s0 + m))
+    Z = np.zeros(L)
+    Z[tuple(sl)] = G
+    Bp = np.zeros(L)
+    Bp[tuple(slice(0, n) for n in B.shape)] = B
+    out = np.real(sfft.ifftn(sfft.fftn(Z) * np.conj(sfft.fftn(Bp))))
+    return out[tuple(slice(0, m) for m in G.shape)]
+
+
+def fold_edge(g, shape):
+    """Adjoint of pad_volume_to(x, g.shape): sums the replicated planes back."""
+    out = g
+    for ax, n in enumerate(shape):
+        head = np.take(out, np.arange(n - 1), axis=ax)
+        tail = np.take(out, np.arange(n - 1, out.shape[ax]), axis=ax).sum(axis=ax, keepdims=True)
+        out = np.concatenate([head, tail], axis=ax)
+    return out
+
+
+def denoise3_masks(x, F, sigma, T, band_scalars, L=3, mode=1.5, grid=None):
+    """Forward pass with the keep-masks of every band (|c| > t)."""
+    grid = grid or tuple(pad_size(s, L, mode) for s in x.shape)
+    bp = pyr_dec(pad_volume_to(x, grid), L, mode)
+    masks = []
+    for b, (c, l, l2, l1, f) in enumerate(band_list(F)):
+        coef = convnfft_same(bp[l], f)
+        masks.append(np.abs(coef) > T[l] * sigma * band_scalars[b])
+    return masks, grid
+
+
+def denoise3_jvp(dx, masks, F, grid, L=3, mode=1.5):
+    """J dx of the denoise linearised at fixed masks (crop of the grid)."""
+    bp = pyr_dec(pad_volume_to(dx, grid), L, mode)
+    rec = [np.zeros_like(b) for b in bp[:L]] + [bp[L]]
+    for b, (c, l, l2, l1, f) in enumerate(band_list(F)):
+        rec[l] += np.where(masks[b], convnfft_same(bp[l], f), 0.0)
+    n = dx.shape
+    return pyr_rec(rec, mode)[:n[0], :n[1], :n[2]]
+
+
+def denoise3_vjp(gy, masks, F, grid, L=3, mode=1.5):
+    """J^T gy: zero-pad, pyr_dec (= pyr_rec^T), masked correlations,
+    pyr_rec (= pyr_dec^T), fold of the edge padding."""
+    n = gy.shape
+    g = np.zeros(grid)
+    g[:n[0], :n[1], :n[2]] = gy
+    u = pyr_dec(g, L, mode)
+    gb = [np.zeros_like(b) for b in u[:L]] + [u[L]]
+    for b, (c, l, l2, l1, f) in enumerate(band_list(F)):
+        gb[l] += corr_same(np.where(masks[b], u[l], 0.0), f)
+    return fold_edge(pyr_rec(gb, mode), n)

@@ -96,6 +96,8 @@ SIGNATURES = [
     ('nsst3_denoise_batch', _ci, [_vp, _vp, _vp, _ci, _dp, _dp, _dp, _vp]),
     ('nsst3_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst3_plan_set_scalars', _ci, [_vp, _dp]),
+    ('nsst3_plan_enable_grad', _ci, [_vp]),
+    ('nsst3_denoise_backward', _ci, [_vp, _vp, _vp, _ci, _vp]),
 ]
 
 _lib = None

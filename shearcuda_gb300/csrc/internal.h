@@ -161,7 +161,15 @@ cudaError_t launch_crop_pair(const float2* W, size_t w_stride, float* out_a, flo
                             int m0, int m1, int m2, int L1, int L2, int off, float scale, cudaStream_t st);
 cudaError_t launch_crop_thresh_acc(const float2* W, size_t w_stride, float* acc, size_t a_stride, int n, int m0,
                                    int m1, int m2, int L1, int L2, int off, const float* th, int ia, int ib,
-                                   int nb_item, float scale, cudaStream_t st);
+                                   int nb_item, float scale, uint32_t* ma, uint32_t* mb, size_t mask_stride,
+                                   cudaStream_t st);
+cudaError_t launch_place_masked(const float* u, size_t u_stride, const uint32_t* ma, const uint32_t* mb,
+                                size_t mask_stride, float2* W, size_t w_stride, int n, int m0, int m1, int m2, int L0,
+                                int L1, int L2, int off, cudaStream_t st);
+cudaError_t launch_spec_acc(const float2* Z, size_t z_stride, const float2* Fa, const float2* Fb, float2* S,
+                            size_t s_stride, int n, size_t total, bool first, cudaStream_t st);
+cudaError_t launch_fold_edge(const float* g, size_t g_stride, float* out, size_t o_stride, int n, int n0, int n1,
+                             int n2, int d0, int d1, int d2, cudaStream_t st);
 std::vector<double> meyer_filters_3d(int cube, int nlevels, const int* num_dirs);
 void filter_spectrum_3d(const double* f, int cube, int L0, int L1, int L2, std::vector<std::complex<double>>* out);
 void pyr_window_1d(int nr, double w, double tbw, int* K, std::vector<double>* v);

@@ -316,13 +316,19 @@ __global__ void k_band_pair(const float2* __restrict__ Y, size_t y_stride, const
 
 // acc (m^3) += T(real(W[crop]) * s, ta) + T(imag(W[crop]) * s, tb);
 // T zeroes |c| <= t (ThresholdShCoeff.m:7); t = -1 disables the threshold.
+// With ma (and mb) set, the keep bits |c| > t of the pair are stored, one
+// 32-bit word per 32 consecutive voxels (m^3 is a multiple of 32, so every
+// warp of the grid-stride loop is full).
 __global__ void k_crop_thresh_acc(const float2* __restrict__ W, size_t w_stride, float* __restrict__ acc,
                                   size_t a_stride, int m0, int m1, int m2, int L1, int L2, int off,
-                                  const float* __restrict__ th, int ia, int ib, int nb_item, float scale) {
+                                  const float* __restrict__ th, int ia, int ib, int nb_item, float scale,
+                                  uint32_t* __restrict__ ma, uint32_t* __restrict__ mb, size_t mask_stride) {
   const float2* w = W + blockIdx.y * w_stride;
   float* a = acc + blockIdx.y * a_stride;
   const float ta = th ? th[blockIdx.y * nb_item + ia] : -1.0f;
   const float tb = (th && ib >= 0) ? th[blockIdx.y * nb_item + ib] : -1.0f;
+  uint32_t* mka = ma ? ma + blockIdx.y * mask_stride : nullptr;
+  uint32_t* mkb = mb ? mb + blockIdx.y * mask_stride : nullptr;
   const size_t total = (size_t)m0 * m1 * m2;
   V3_LOOP(total) {
     const int z = (int)(idx % m2);
@@ -330,10 +336,92 @@ __global__ void k_crop_thresh_acc(const float2* __restrict__ W, size_t w_stride,
     const int y = (int)(r % m1), x = (int)(r / m1);
     const float2 v = w[((size_t)(x + off) * L1 + (y + off)) * L2 + (z + off)];
     const float ca = v.x * scale, cb = v.y * scale;
+    const bool ka = !(fabsf(ca) <= ta), kb = !(fabsf(cb) <= tb);
     float sum = a[idx];
-    sum += (fabsf(ca) <= ta) ? 0.0f : ca;
-    if (ib >= 0) sum += (fabsf(cb) <= tb) ? 0.0f : cb;
+    sum += ka ? ca : 0.0f;
+    if (ib >= 0) sum += kb ? cb : 0.0f;
     a[idx] = sum;
+    if (mka) {
+      const uint32_t bits_a = __ballot_sync(0xffffffffu, ka);
+      const uint32_t bits_b = __ballot_sync(0xffffffffu, kb);
+      if ((threadIdx.x & 31) == 0) {
+        mka[idx >> 5] = bits_a;
+        if (mkb) mkb[idx >> 5] = bits_b;
+      }
+    }
+  }
+}
+
+// Adjoint of the pair's crop + threshold: W (L0 x L1 x L2) = zero except the
+// crop box at offset `off`, where it holds keep_a * u + i keep_b * u.
+__global__ void k_place_masked(const float* __restrict__ u, size_t u_stride, const uint32_t* __restrict__ ma,
+                               const uint32_t* __restrict__ mb, size_t mask_stride, float2* __restrict__ W,
+                               size_t w_stride, int m0, int m1, int m2, int L0, int L1, int L2, int off) {
+  const float* src = u + blockIdx.y * u_stride;
+  const uint32_t* mka = ma + blockIdx.y * mask_stride;
+  const uint32_t* mkb = mb ? mb + blockIdx.y * mask_stride : nullptr;
+  float2* dst = W + blockIdx.y * w_stride;
+  const size_t total = (size_t)L0 * L1 * L2;
+  V3_LOOP(total) {
+    const int z = (int)(idx % L2) - off;
+    const size_t r = idx / L2;
+    const int y = (int)(r % L1) - off, x = (int)(r / L1) - off;
+    float2 o = make_float2(0.f, 0.f);
+    if (x >= 0 && x < m0 && y >= 0 && y < m1 && z >= 0 && z < m2) {
+      const size_t j = ((size_t)x * m1 + y) * m2 + z;
+      const float v = src[j];
+      const uint32_t bit = 1u << (j & 31);
+      o.x = (mka[j >> 5] & bit) ? v : 0.0f;
+      if (mkb) o.y = (mkb[j >> 5] & bit) ? v : 0.0f;
+    }
+    dst[idx] = o;
+  }
+}
+
+// S (=, or += unless first) (conj(Fa) - i conj(Fb)) Z: the real part of the
+// inverse transform of the sum is the correlation of the real part of Z's
+// source with filter a plus that of its imaginary part with filter b.
+__global__ void k_spec_acc(const float2* __restrict__ Z, size_t z_stride, const float2* __restrict__ Fa,
+                           const float2* __restrict__ Fb, float2* __restrict__ S, size_t s_stride, size_t n,
+                           int first) {
+  const float2* z = Z + blockIdx.y * z_stride;
+  float2* s = S + blockIdx.y * s_stride;
+  V3_LOOP(n) {
+    const float2 fa = Fa[idx];
+    float2 k = make_float2(fa.x, -fa.y);
+    if (Fb) {
+      const float2 fb = Fb[idx];
+      k.x -= fb.y;
+      k.y -= fb.x;
+    }
+    const float2 v = z[idx];
+    const float2 prod = make_float2(k.x * v.x - k.y * v.y, k.x * v.y + k.y * v.x);
+    if (first) {
+      s[idx] = prod;
+    } else {
+      const float2 o = s[idx];
+      s[idx] = make_float2(o.x + prod.x, o.y + prod.y);
+    }
+  }
+}
+
+// Adjoint of k_pad_edge: out (n0 x n1 x n2) gathers the grid voxels that
+// replicate it (the last plane of each axis collects the padded planes).
+__global__ void k_fold_edge(const float* __restrict__ g, size_t g_stride, float* __restrict__ out, size_t o_stride,
+                            int n0, int n1, int n2, int d0, int d1, int d2) {
+  const float* src = g + blockIdx.y * g_stride;
+  float* dst = out + blockIdx.y * o_stride;
+  const size_t total = (size_t)n0 * n1 * n2;
+  V3_LOOP(total) {
+    const int z = (int)(idx % n2);
+    const size_t r = idx / n2;
+    const int y = (int)(r % n1), x = (int)(r / n1);
+    const int x1 = x == n0 - 1 ? d0 : x + 1, y1 = y == n1 - 1 ? d1 : y + 1, z1 = z == n2 - 1 ? d2 : z + 1;
+    float sum = 0.f;
+    for (int a = x; a < x1; a++)
+      for (int b = y; b < y1; b++)
+        for (int c = z; c < z1; c++) sum += src[((size_t)a * d1 + b) * d2 + c];
+    dst[idx] = sum;
   }
 }
 
@@ -421,10 +509,33 @@ cudaError_t launch_crop_pair(const float2* W, size_t w_stride, float* out_a, flo
 }
 cudaError_t launch_crop_thresh_acc(const float2* W, size_t w_stride, float* acc, size_t a_stride, int n, int m0,
                                    int m1, int m2, int L1, int L2, int off, const float* th, int ia, int ib,
-                                   int nb_item, float scale, cudaStream_t st) {
+                                   int nb_item, float scale, uint32_t* ma, uint32_t* mb, size_t mask_stride,
+                                   cudaStream_t st) {
+  if (ma && ((size_t)m0 * m1 * m2) % 32) return cudaErrorInvalidValue;
   count_launch();
   k_crop_thresh_acc<<<v3grid((size_t)m0 * m1 * m2, n), 256, 0, st>>>(W, w_stride, acc, a_stride, m0, m1, m2, L1, L2,
-                                                                      off, th, ia, ib, nb_item, scale);
+                                                                      off, th, ia, ib, nb_item, scale, ma, mb,
+                                                                      mask_stride);
+  return cudaGetLastError();
+}
+cudaError_t launch_place_masked(const float* u, size_t u_stride, const uint32_t* ma, const uint32_t* mb,
+                                size_t mask_stride, float2* W, size_t w_stride, int n, int m0, int m1, int m2, int L0,
+                                int L1, int L2, int off, cudaStream_t st) {
+  count_launch();
+  k_place_masked<<<v3grid((size_t)L0 * L1 * L2, n), 256, 0, st>>>(u, u_stride, ma, mb, mask_stride, W, w_stride, m0,
+                                                                   m1, m2, L0, L1, L2, off);
+  return cudaGetLastError();
+}
+cudaError_t launch_spec_acc(const float2* Z, size_t z_stride, const float2* Fa, const float2* Fb, float2* S,
+                            size_t s_stride, int n, size_t total, bool first, cudaStream_t st) {
+  count_launch();
+  k_spec_acc<<<v3grid(total, n), 256, 0, st>>>(Z, z_stride, Fa, Fb, S, s_stride, total, first ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_fold_edge(const float* g, size_t g_stride, float* out, size_t o_stride, int n, int n0, int n1,
+                             int n2, int d0, int d1, int d2, cudaStream_t st) {
+  count_launch();
+  k_fold_edge<<<v3grid((size_t)n0 * n1 * n2, n), 256, 0, st>>>(g, g_stride, out, o_stride, n0, n1, n2, d0, d1, d2);
   return cudaGetLastError();
 }
 

@@ -160,6 +160,12 @@ struct nsst3_plan {
   float* rbp = nullptr;
   float* th = nullptr;
 
+  // differentiation: keep bits of every band of the last thresholded forward
+  uint32_t* mask = nullptr;
+  size_t mask_words = 0;            // per item
+  std::vector<size_t> mask_off;     // per band, in words
+  int masks_valid_n = 0;            // items covered by the stored masks (0 = none)
+
   std::vector<double> scalars;
   bool has_scalars = false;
   std::vector<float> th_host;
@@ -193,10 +199,14 @@ PyrWin level_window(const nsst3_plan* p, int l) {
 
 // PyrNDDec_mm.m:20-109 (OutD 'S') for n volumes x (dims in[3], padded to the
 // grid by edge replication) into the sub-band layout bp (item stride bp_floats).
-nsst_status run_pyr_dec(nsst3_plan* p, const float* x, const int* in, float* bp, int n, cudaStream_t st) {
+nsst_status run_pyr_dec(nsst3_plan* p, const float* x, const int* in, float* bp, int n, cudaStream_t st,
+                        bool zero_pad = false) {
   const size_t xs = (size_t)in[0] * in[1] * in[2];
   const nsst3_plan::Level& l0 = p->lev[0];
-  V3_CUDA(launch_pad_edge(x, xs, p->vol, p->vol_elems, n, in[0], in[1], in[2], p->g[0], p->g[1], p->g[2], st));
+  if (zero_pad)
+    V3_CUDA(launch_pad_real(x, xs, p->vol, p->vol_elems, n, in[0], in[1], in[2], p->g[0], p->g[1], p->g[2], st));
+  else
+    V3_CUDA(launch_pad_edge(x, xs, p->vol, p->vol_elems, n, in[0], in[1], in[2], p->g[0], p->g[1], p->g[2], st));
   V3_TRY(fft3(p, p->vol, p->vol_elems, n, p->g, -1, st));
   V3_CUDA(launch_half(p->vol, p->vol_elems, p->xh + l0.xh_off, p->xh_elems, n, p->g[0], p->g[1], p->g[2], st));
   for (int l = 0; l <= p->L; l++) {
@@ -245,7 +255,7 @@ nsst_status run_pyr_rec(nsst3_plan* p, const float* bp, float* x, const int* out
 // item stride bp_floats).  acc == NULL: band coefficients into coeffs
 // (nb volumes of the level per item, item stride nb * vol).
 nsst_status run_sh_level(nsst3_plan* p, const float* bp, int l, float* acc, const float* th, float* coeffs, int n,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool record_masks = false) {
   const nsst3_plan::Level& a = p->lev[l];
   const size_t cv = a.conv();
   V3_CUDA(launch_pad_real(bp + a.bp_off, p->bp_floats, p->Y, p->conv_elems, n, a.m[0], a.m[1], a.m[2], a.lc[0],
@@ -260,8 +270,11 @@ nsst_status run_sh_level(nsst3_plan* p, const float* bp, int l, float* acc, cons
     V3_CUDA(launch_band_pair(p->Y, p->conv_elems, Fa, Fb, p->Wk, p->conv_elems, n, cv, st));
     V3_TRY(fft3(p, p->Wk, p->conv_elems, n, a.lc, +1, st));
     if (acc) {
+      uint32_t* ma = record_masks ? p->mask + p->mask_off[ba] : nullptr;
+      uint32_t* mb = (record_masks && bb >= 0) ? p->mask + p->mask_off[bb] : nullptr;
       V3_CUDA(launch_crop_thresh_acc(p->Wk, p->conv_elems, acc + a.bp_off, p->bp_floats, n, a.m[0], a.m[1], a.m[2],
-                                     a.lc[1], a.lc[2], kSameOff, th, ba, bb, p->nbands, scale, st));
+                                     a.lc[1], a.lc[2], kSameOff, th, ba, bb, p->nbands, scale, ma, mb, p->mask_words,
+                                     st));
     } else {
       float* oa = coeffs + (size_t)k * a.vol();
       float* ob = bb >= 0 ? oa + a.vol() : nullptr;
@@ -291,9 +304,10 @@ nsst_status upload_th(nsst3_plan* p, int n, const double* sigma, const double* T
 
 // ShDecThRec_cuda: rec (sub-band layout) = per level sum of thresholded
 // bands; lowpass copied from bp.
-nsst_status run_dec_thresh_rec(nsst3_plan* p, const float* bp, float* rec, int n, const float* th, cudaStream_t st) {
+nsst_status run_dec_thresh_rec(nsst3_plan* p, const float* bp, float* rec, int n, const float* th, cudaStream_t st,
+                               bool record_masks = false) {
   V3_CUDA(cudaMemsetAsync(rec, 0, (size_t)n * p->bp_floats * sizeof(float), st));
-  for (int l = 0; l < p->L; l++) V3_TRY(run_sh_level(p, bp, l, rec, th, nullptr, n, st));
+  for (int l = 0; l < p->L; l++) V3_TRY(run_sh_level(p, bp, l, rec, th, nullptr, n, st, record_masks));
   const nsst3_plan::Level& lp = p->lev[p->L];
   V3_CUDA(cudaMemcpy2DAsync(rec + lp.bp_off, p->bp_floats * sizeof(float), bp + lp.bp_off,
                             p->bp_floats * sizeof(float), lp.vol() * sizeof(float), n, cudaMemcpyDeviceToDevice, st));
@@ -506,7 +520,9 @@ nsst_status nsst3_plan_destroy(nsst3_plan* p) {
     std::lock_guard<std::mutex> lk(p->mu);
     cudaSetDevice(p->device);
     if (p->arena) cudaFree(p->arena);
+    if (p->mask) cudaFree(p->mask);
     p->arena = nullptr;
+    p->mask = nullptr;
   }
   delete p;
   return NSST_OK;
@@ -583,7 +599,9 @@ nsst_status nsst3_denoise_batch(nsst3_plan* p, const float* x, float* out, int n
   const cudaStream_t st = (cudaStream_t)stream;
   V3_TRY(upload_th(p, n, sigma, T, scalars, st));
   V3_TRY(run_pyr_dec(p, x, p->n, p->bp, n, st));
-  V3_TRY(run_dec_thresh_rec(p, p->bp, p->rbp, n, p->th, st));
+  p->masks_valid_n = 0;
+  V3_TRY(run_dec_thresh_rec(p, p->bp, p->rbp, n, p->th, st, p->mask != nullptr));
+  if (p->mask) p->masks_valid_n = n;
   return run_pyr_rec(p, p->rbp, out, p->n, n, st);
 }
 
@@ -654,6 +672,76 @@ nsst_status nsst3_compute_scalars(nsst3_plan* p, uint64_t seed, double* out) {
   p->scalars = sc;
   p->has_scalars = true;
   if (out) std::copy(sc.begin(), sc.end(), out);
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiation of the 3-D denoise.  The hard threshold's subgradient keeps
+// the forward pass's masks; the band-pass pyramid is a Parseval frame, so the
+// adjoint of the decomposition is the reconstruction and vice versa; the
+// adjoint of each 'same' convolution is a correlation (the conjugate filter
+// spectrum) of the masked gradient placed back at offset 12.
+// ---------------------------------------------------------------------------
+extern "C" {
+
+nsst_status nsst3_plan_enable_grad(nsst3_plan* p) {
+  if (!p) return fail3(NSST_ERR_INVALID_ARG, "NULL plan");
+  if (p->mask) return NSST_OK;
+  if (cudaSetDevice(p->device) != cudaSuccess) return fail3(NSST_ERR_CUDA, "cudaSetDevice failed");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->mask_off.assign(p->nbands, 0);
+  size_t words = 0;
+  for (int b = 0; b < p->nbands; b++) {
+    p->mask_off[b] = words;
+    words += align_up3(p->lev[p->band_level[b]].vol() / 32, 8);
+  }
+  p->mask_words = words;
+  void* m = nullptr;
+  cudaError_t e = dev_alloc(&m, (size_t)p->B * words * sizeof(uint32_t));
+  if (e != cudaSuccess) return cuda_fail3(e, "mask buffer");
+  p->mask = (uint32_t*)m;
+  p->masks_valid_n = 0;
+  return NSST_OK;
+}
+
+nsst_status nsst3_denoise_backward(nsst3_plan* p, const float* gy, float* gx, int n, void* stream) {
+  V3_TRY(check_call(p, n, gy, gx));
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (!p->mask) return fail3(NSST_ERR_INVALID_ARG, "gradients are not enabled on this plan");
+  if (p->masks_valid_n != n)
+    return fail3(NSST_ERR_INVALID_ARG, "no forward nsst3_denoise_batch of these n volumes since grad was enabled");
+  const cudaStream_t st = (cudaStream_t)stream;
+  // u = pyr_dec(zero-pad(gy)): the adjoint of crop + pyr_rec
+  V3_TRY(run_pyr_dec(p, gy, p->n, p->rbp, n, st, true));
+  // per level: bp_bar_l = sum_b corr(mask_b * u_l, f_b)
+  for (int l = 0; l < p->L; l++) {
+    const nsst3_plan::Level& a = p->lev[l];
+    const size_t cv = a.conv();
+    for (int k = 0; k < a.nb; k += 2) {
+      const int ba = a.first_band + k;
+      const int bb = k + 1 < a.nb ? ba + 1 : -1;
+      const float2* Fa = p->spec + a.spec_off + (size_t)k * cv;
+      const float2* Fb = bb >= 0 ? Fa + cv : nullptr;
+      V3_CUDA(launch_place_masked(p->rbp + a.bp_off, p->bp_floats, p->mask + p->mask_off[ba],
+                                  bb >= 0 ? p->mask + p->mask_off[bb] : nullptr, p->mask_words, p->Wk, p->conv_elems,
+                                  n, a.m[0], a.m[1], a.m[2], a.lc[0], a.lc[1], a.lc[2], kSameOff, st));
+      V3_TRY(fft3(p, p->Wk, p->conv_elems, n, a.lc, -1, st));
+      V3_CUDA(launch_spec_acc(p->Wk, p->conv_elems, Fa, Fb, p->Y, p->conv_elems, n, cv, k == 0, st));
+    }
+    V3_TRY(fft3(p, p->Y, p->conv_elems, n, a.lc, +1, st));
+    V3_CUDA(launch_crop_real(p->Y, p->conv_elems, p->bp + a.bp_off, p->bp_floats, n, a.m[0], a.m[1], a.m[2], a.lc[1],
+                             a.lc[2], 0, 0, 0, (float)(1.0 / (double)cv), st));
+  }
+  // the lowpass passes through unchanged
+  const nsst3_plan::Level& lp = p->lev[p->L];
+  V3_CUDA(cudaMemcpy2DAsync(p->bp + lp.bp_off, p->bp_floats * sizeof(float), p->rbp + lp.bp_off,
+                            p->bp_floats * sizeof(float), lp.vol() * sizeof(float), n, cudaMemcpyDeviceToDevice, st));
+  // pyr_rec (the adjoint of pyr_dec) to the full grid, then fold the edge padding
+  V3_TRY(run_pyr_rec(p, p->bp, p->rbp, p->g, n, st));
+  V3_CUDA(launch_fold_edge(p->rbp, p->vol_elems, gx, p->in_elems, n, p->n[0], p->n[1], p->n[2], p->g[0], p->g[1],
+                           p->g[2], st));
   return NSST_OK;
 }
 

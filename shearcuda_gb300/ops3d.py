@@ -11,6 +11,8 @@ here                           reference (ShearCuda tree)
 ``sh_dec_th_rec_cuda``         shearcuda3d/3DShearTrans/src_cuda/ShDecThRec_cuda.cpp:57-335
 ``nsst_scalars3``              shearcuda3d/DenoiseDemo/NsstScalars.m:1-19
 ``denoise3``                   shearcuda3d/DenoiseDemo/main.m:80-145 (fused, batched)
+``denoise3_backward``          (no reference counterpart) adjoint of ``denoise3`` at its threshold masks
+``Denoise3Fn``                 ``torch.autograd.Function`` over ``denoise3`` / ``denoise3_backward``
 =============================  ==========================================================================
 
 Volumes are CUDA float32 tensors (n0, n1, n2) or batches (B, n0, n1, n2);
@@ -27,7 +29,8 @@ from ._lib import Nsst3Config, NsstError, check, lib
 from .ops import _dev, _dptr, _stream
 
 __all__ = ['VolumePlan', 'get_meyer_based_filter', 'do_pyr_dec', 'do_pyr_rec', 'sh_dec', 'sh_dec_th_rec_cuda',
-           'nsst_scalars3', 'denoise3', 'DEMO_T', 'DEMO_NUM_DIRS', 'V3_NUM_DIRS']
+           'nsst_scalars3', 'denoise3', 'denoise3_backward', 'Denoise3Fn', 'denoise3_diff', 'DEMO_T',
+           'DEMO_NUM_DIRS', 'V3_NUM_DIRS']
 
 DEMO_T = (3.3, 3.0, 3.0, 3.0)     # DenoiseDemo/main.m:18
 DEMO_NUM_DIRS = (8, 4, 4)         # dBand{3} of DenoiseDemo/main.m:44-47 (numDir per level, finest first)
@@ -79,6 +82,8 @@ class VolumePlan:
             check(lib().nsst3_band_info(h, b, info))
             self.band_info.append(tuple(info))
         self.band_level = [i[0] for i in self.band_info]
+        self._grad = False
+        self._fwd_token = 0   # bumped by every denoise3 call (the masks it leaves)
         # offsets of each level in the sub-band layout (64-float aligned)
         self.level_offsets = []
         off = 0
@@ -112,6 +117,12 @@ class VolumePlan:
         if s.size != self.nbands:
             raise NsstError(1, 'need %d scalars' % self.nbands)
         check(lib().nsst3_plan_set_scalars(self.handle, _dptr(s)))
+
+    def enable_grad(self):
+        """Record the threshold masks in every later denoise3 call."""
+        if not self._grad:
+            check(lib().nsst3_plan_enable_grad(self.handle))
+            self._grad = True
 
     def empty_subbands(self, n=1, device=None):
         return torch.zeros((n, self.subband_floats), dtype=torch.float32, device=device or 'cuda')
@@ -211,4 +222,45 @@ def denoise3(x, plan, sigma, T=DEMO_T, scalars=None, out=None, stream=None):
     ob = out.unsqueeze(0) if out.dim() == 3 else out
     check(lib().nsst3_denoise_batch(plan.handle, _dev(xb, 'x'), _dev(ob, 'out'), n, _dptr(sig), _dptr(t),
                                     None if sc is None else _dptr(sc), _stream(stream)))
+    plan._fwd_token += 1
     return ob[0] if squeeze else ob
+
+
+def denoise3_backward(gy, plan, out=None, stream=None):
+    """d loss / d x for the volumes of the plan's most recent denoise3 call,
+    given gy = d loss / d out (same shape as that call's input)."""
+    squeeze = gy.dim() == 3
+    gb = plan._batch(gy, 'gy')
+    if out is None:
+        out = torch.empty_like(gb)
+    ob = out.unsqueeze(0) if out.dim() == 3 else out
+    check(lib().nsst3_denoise_backward(plan.handle, _dev(gb, 'gy'), _dev(ob, 'gx'), gb.shape[0], _stream(stream)))
+    return ob[0] if squeeze else ob
+
+
+class Denoise3Fn(torch.autograd.Function):
+    """out = denoise3(x); backward through the hand-written adjoint.  The
+    plan keeps only the masks of its latest forward call, so a backward
+    whose masks were overwritten first re-runs its own forward."""
+
+    @staticmethod
+    def forward(ctx, x, plan, sigma, T, scalars):
+        plan.enable_grad()
+        out = denoise3(x.detach().contiguous(), plan, sigma, T, scalars)
+        ctx.plan, ctx.args, ctx.token = plan, (sigma, T, scalars), plan._fwd_token
+        ctx.save_for_backward(x)
+        return out
+
+    @staticmethod
+    def backward(ctx, gy):
+        plan = ctx.plan
+        (x,) = ctx.saved_tensors
+        if plan._fwd_token != ctx.token:
+            denoise3(x.detach().contiguous(), plan, *ctx.args)
+        gx = denoise3_backward(gy.contiguous(), plan)
+        return gx, None, None, None, None
+
+
+def denoise3_diff(x, plan, sigma, T=DEMO_T, scalars=None):
+    """Differentiable 3-D denoise (gradient with respect to the volumes)."""
+    return Denoise3Fn.apply(x, plan, sigma, T, scalars)

@@ -213,3 +213,80 @@ def test_vol3d_launch_count_and_determinism(s3):
     assert s3.launch_count() > n0
     assert torch.equal(a, b)
     assert math.isfinite(float(a.abs().max()))
+
+
+def _dot(a, b):
+    return float(np.vdot(np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()))
+
+
+def test_denoise3_backward_dot_product(s3):
+    # the hard-threshold denoise is linear at fixed masks and f(x0) = J(x0) x0,
+    # so <gy, f(x0)> = <J^T gy, x0> with the masks of the same forward call
+    import torch
+    shape = (80, 96, 100)  # padded to (96, 96, 144): the fold of the edge padding is exercised
+    _, x = s3.synth.noisy_volume(shape, 30.0, 31)
+    p = s3.VolumePlan(*shape, num_dirs=(2, 2, 4), batch=2)
+    s3.nsst_scalars3(p, seed=2)
+    p.enable_grad()
+    xb = torch.stack([_t(x), _t(x[::-1].copy())])
+    out = s3.denoise3(xb, p, [30.0, 20.0])
+    gy = torch.randn_like(out)
+    gx = s3.denoise3_backward(gy, p)
+    for i in range(2):
+        lhs, rhs = _dot(_np(gy[i]), _np(out[i])), _dot(_np(gx[i]), _np(xb[i]))
+        assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (i, lhs, rhs)
+
+
+def test_denoise3_backward_identity_without_threshold(s3):
+    # T = 0 keeps every coefficient: the denoise is the identity, so is its adjoint
+    import torch
+    shape = (80, 96, 100)
+    _, x = s3.synth.noisy_volume(shape, 30.0, 32)
+    p = s3.VolumePlan(*shape, num_dirs=(2, 2, 4))
+    p.set_scalars(np.ones(p.nbands))
+    p.enable_grad()
+    out = s3.denoise3(_t(x), p, 30.0, [0, 0, 0])
+    assert rel_l2(_np(out), x) < TOL
+    gy = torch.randn((1,) + shape, device='cuda')
+    gx = s3.denoise3_backward(gy, p)
+    assert rel_l2(_np(gx), _np(gy)) < TOL
+
+
+def test_denoise3_backward_matches_oracle(s3):
+    from oracle import nsst3d
+    import torch
+    shape = (40, 44, 36)
+    sigma = 30.0
+    _, x = s3.synth.noisy_volume(shape, sigma, 33)
+    p = s3.VolumePlan(*shape, num_dirs=(2, 2))
+    assert p.grid == (48, 48, 48)
+    scal = s3.nsst_scalars3(p, seed=4)
+    p.enable_grad()
+    T = [3.0, 3.0]
+    s3.denoise3(_t(x), p, sigma, T)
+    gy = np.random.default_rng(34).standard_normal(shape)
+    gx = _np(s3.denoise3_backward(_t(gy), p))
+    F = nsst3d.meyer_filters_3d([2, 2])
+    th = [np.float32(T[l] * sigma * scal[b]) / (T[l] * sigma) for b, (c, l, l2, l1, f) in
+          enumerate(nsst3d.band_list(F))]
+    masks, grid = nsst3d.denoise3_masks(x.astype(np.float32).astype(np.float64), F, sigma, T, np.asarray(th), L=2)
+    ref = nsst3d.denoise3_vjp(gy, masks, F, grid, L=2)
+    # masks can differ only where a coefficient sits within FP32 rounding of its threshold
+    assert rel_l2(gx, ref) < 1e-4
+
+
+def test_denoise3_autograd_function(s3):
+    import torch
+    shape = (48, 48, 48)
+    clean, x = s3.synth.noisy_volume(shape, 30.0, 35)
+    p = s3.VolumePlan(*shape, num_dirs=(2, 2, 4), batch=1)
+    s3.nsst_scalars3(p, seed=6)
+    xt = _t(x).requires_grad_(True)
+    out = s3.denoise3_diff(xt, p, 30.0)
+    loss = ((out - _t(clean)) ** 2).sum()
+    # another forward on the plan overwrites its masks; backward must redo its own
+    s3.denoise3(_t(np.zeros(shape)), p, 30.0)
+    loss.backward()
+    s3.denoise3(xt.detach(), p, 30.0)
+    ref = s3.denoise3_backward((2 * (out.detach() - _t(clean))), p)
+    assert torch.equal(xt.grad, ref)

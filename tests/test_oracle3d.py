@@ -132,3 +132,40 @@ def test_host_meyer_filters_reject_bad_num_dirs(built_lib):
     for bad in [(5,), (1,), (16,), ()]:
         with pytest.raises(NsstError):
             get_meyer_based_filter(bad)
+
+
+def test_pyramid_is_parseval():
+    # <pyr_dec x, s> = <x, pyr_rec s>: the reconstruction is the exact adjoint
+    rng = np.random.default_rng(21)
+    for mode, L, shape in [(1.5, 3, (96, 96, 96)), (1.5, 3, (96, 144, 96)), (1, 2, (48, 48, 64))]:
+        x = rng.standard_normal(shape)
+        subs = nsst3d.pyr_dec(x, L, mode)
+        s = [rng.standard_normal(b.shape) for b in subs]
+        lhs = sum(np.vdot(a, b) for a, b in zip(subs, s))
+        rhs = np.vdot(x, nsst3d.pyr_rec(s, mode))
+        assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+
+
+def test_corr_same_and_fold_are_adjoints():
+    rng = np.random.default_rng(22)
+    A, B, G = rng.standard_normal((20, 17, 15)), rng.standard_normal((24, 24, 24)), rng.standard_normal((20, 17, 15))
+    assert abs(np.vdot(nsst3d.convnfft_same(A, B), G) - np.vdot(A, nsst3d.corr_same(G, B))) < 1e-10
+    x, y = rng.standard_normal((5, 6, 7)), rng.standard_normal((8, 9, 12))
+    assert abs(np.vdot(nsst3d.pad_volume_to(x, y.shape), y) - np.vdot(x, nsst3d.fold_edge(y, x.shape))) < 1e-10
+
+
+def test_denoise3_adjoint_dot_product_and_fd():
+    rng = np.random.default_rng(23)
+    shape = (40, 44, 36)
+    F = nsst3d.meyer_filters_3d([2, 2])
+    x = rng.standard_normal(shape) * 30 + 100
+    sc = np.full(12 * 2, 0.2)
+    masks, grid = nsst3d.denoise3_masks(x, F, 30.0, [3.0, 3.0], sc, L=2)
+    assert grid == (48, 48, 48)
+    dx, gy = rng.standard_normal(shape), rng.standard_normal(shape)
+    lhs = np.vdot(nsst3d.denoise3_jvp(dx, masks, F, grid, L=2), gy)
+    rhs = np.vdot(dx, nsst3d.denoise3_vjp(gy, masks, F, grid, L=2))
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+    # the denoise is linear where the masks hold: J x = denoise(x)
+    full = nsst3d.denoise3(nsst3d.pad_volume_to(x, grid), F, 30.0, [3.0, 3.0], sc, L=2)[:40, :44, :36]
+    assert np.abs(nsst3d.denoise3_jvp(x, masks, F, grid, L=2) - full).max() < 1e-9 * np.abs(full).max()
