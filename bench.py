@@ -197,6 +197,56 @@ def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
     return b
 
 
+def volume_bench(sc, torch, dev, stream, flush, rank, reps=3):
+    """3-D denoise of seeded ellipsoid sequences (sigma 30, T = [3.3 3 3]):
+    volumes/s of the batched forward and of forward + adjoint (gradient with
+    respect to the volumes at the forward's threshold masks)."""
+    from shearcuda_gb300.synth import noisy_volume
+    out = {'num_dirs': list(sc.V3_NUM_DIRS), 'T': list(sc.DEMO_T[:3]), 'sigma': 30.0}
+    for n in (128, 192):
+        p = sc.VolumePlan(n, n, n, num_dirs=sc.V3_NUM_DIRS, batch=4)
+        sc.nsst_scalars3(p, seed=9)
+        p.enable_grad()
+        xb = torch.stack([torch.tensor(noisy_volume((n, n, n), 30.0, 500 * rank + i)[1].astype(np.float32),
+                                       device=dev) for i in range(4)])
+        ob = torch.empty_like(xb)
+        gy = torch.randn_like(xb)
+        gx = torch.empty_like(xb)
+
+        def fwd():
+            sc.denoise3(xb, p, 30.0, sc.DEMO_T, out=ob)
+
+        def fwd_bwd():
+            fwd()
+            sc.denoise3_backward(gy, p, out=gx)
+
+        res = {'grid': p.grid[0], 'conv_lengths': [c[0] for c in p.conv_dims[:3]],
+               'device_bytes': p.device_bytes()}
+        c0 = sc.launch_count()
+        fwd()
+        res['kernels_forward'] = sc.launch_count() - c0
+        for name, f in (('forward_ms', fwd), ('forward_adjoint_ms', fwd_bwd)):
+            for _ in range(2):
+                f()
+            torch.cuda.synchronize()
+            tt = 0.0
+            for _ in range(reps):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                f()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tt += e0.elapsed_time(e1)
+            res[name] = tt / reps
+        res['volumes_per_s'] = 4 / (res['forward_ms'] / 1000.0)
+        res['ratio'] = res['forward_adjoint_ms'] / res['forward_ms']
+        out['b4x%d' % n] = res
+        p.close()
+        del xb, ob, gy, gx
+    return out
+
+
 def run_gpu(args):
     import torch
     import shearcuda_gb300 as sc
@@ -411,6 +461,10 @@ def run_gpu(args):
         res['images'] = 16
         line['differentiable_d16'] = res
         del pd
+
+        # ---- 3-D volumes: batches of 4 x 128^3 and 4 x 192^3 (72 directional
+        # bands, numDir 2, 2, 4), hard threshold, forward vs forward + adjoint
+        line['volume_v3'] = volume_bench(sc, torch, dev, stream, flush, rank)
 
     if rank == 0:
         cb = cpu_baseline()

@@ -127,6 +127,7 @@ template <> struct FftPlan<144> { using type = RadixList<3, 3, 4, 4>; };
 template <> struct FftPlan<96> { using type = RadixList<3, 4, 8>; };
 template <> struct FftPlan<128> { using type = RadixList<8, 4, 4>; };
 template <> struct FftPlan<192> { using type = RadixList<3, 8, 8>; };
+template <> struct FftPlan<216> { using type = RadixList<3, 3, 3, 8>; };
 template <> struct FftPlan<256> { using type = RadixList<4, 8, 8>; };
 template <> struct FftPlan<384> { using type = RadixList<3, 2, 8, 8>; };
 template <> struct FftPlan<512> { using type = RadixList<8, 8, 8>; };

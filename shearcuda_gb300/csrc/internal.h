@@ -125,11 +125,6 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
 cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
 
 // ------------------------------------------------------------------- 3-D path
-struct V3Axis {  // one axis of a batched 3-D FFT
-  int axis, d2;
-  long long nseq, si, ss;
-  size_t item_stride;
-};
 struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)
   int K[3];
   int nr[3];
@@ -137,10 +132,40 @@ struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)
   const float* v1;
   const float* v2;
 };
-bool fft3_len_supported(int n);
-cudaError_t prepare_fft3(int n);
-cudaError_t launch_fft3_axis(float2* vol, int nitems, size_t item_stride, int d0, int d1, int d2, int axis, int dir,
-                             const float2* tw, cudaStream_t st);
+// One pass of a batched 3-D FFT with a fused prologue / epilogue
+// (k_vol3d_pass.cu).  Ranges along the two non-transformed axes select the
+// CTA's sequences: axis 2 (z rows): a = x, b = y; axis 1: a = x, b = z;
+// axis 0: a = y, b = z; b_n is a multiple of 8.
+enum { V3_LD_CPLX = 0, V3_LD_REAL = 1, V3_LD_PAIR = 2, V3_LD_MASKED = 3 };
+enum { V3_ST_CPLX = 0, V3_ST_REAL = 1, V3_ST_THRESH = 2, V3_ST_SPEC = 3, V3_ST_PAIR = 4 };
+struct V3Pass {
+  int axis = 2;
+  int D1 = 0, D2 = 0;             // work buffer dims 1, 2
+  int a_lo = 0, a_n = 0, b_lo = 0, b_n = 0;
+  int in_lo = 0, in_n = 0;        // loaded range along the axis (zero elsewhere)
+  int out_lo = 0, out_n = 0;      // stored range along the axis
+  size_t item_stride = 0;         // float2 per item of the work buffers
+  const float2* spec = nullptr;   // LD_PAIR / ST_SPEC: filter-pair spectrum (shared by the items)
+  const float* rsrc = nullptr;    // LD_REAL / LD_MASKED: real volume of a box
+  float* rdst = nullptr;          // ST_REAL / ST_THRESH / ST_PAIR: real volume of a box
+  float* rdst2 = nullptr;         // ST_PAIR: second band
+  size_t r_stride = 0;            // floats per item of rsrc / rdst
+  int r1 = 0, r2 = 0;             // box dims 1, 2
+  int o0 = 0, o1 = 0, o2 = 0;     // box origin in work-buffer coordinates
+  const uint8_t* mka = nullptr;   // LD_MASKED keep bits (linear bit order over the box)
+  const uint8_t* mkb = nullptr;
+  uint8_t* mwa = nullptr;         // ST_THRESH keep bits written
+  uint8_t* mwb = nullptr;
+  size_t m_stride = 0;            // mask bytes per item
+  const float* th = nullptr;      // ST_THRESH thresholds [item][nb_item]
+  int ia = 0, ib = -1, nb_item = 0;
+  float scale = 1.f;
+  int first = 0;                  // ST_SPEC: assign instead of accumulate
+};
+bool v3_pass_len_supported(int n);
+cudaError_t prepare_v3_pass(int n);
+cudaError_t launch_v3_pass(int N, int dir, int ld, int st, float2* out, const float2* in, const V3Pass& P,
+                           const float2* tw, int nitems, cudaStream_t stream);
 cudaError_t launch_pad_real(const float* in, size_t in_stride, float2* out, size_t out_stride, int n, int m0, int m1,
                             int m2, int L0, int L1, int L2, cudaStream_t st);
 cudaError_t launch_pad_edge(const float* in, size_t in_stride, float2* out, size_t out_stride, int n, int n0, int n1,
@@ -155,21 +180,8 @@ cudaError_t launch_pyr_dec(float2* Xh, size_t stride, float2* Lp, size_t lp_stri
                            int s0, int s1, int s2, const PyrWin& w, float invDN, cudaStream_t st);
 cudaError_t launch_pyr_rec(float2* Hh, size_t stride, const float2* Lp, size_t lp_stride, int n, int d0, int d1,
                            int d2, int s0, int s1, int s2, const PyrWin& w, float DN, cudaStream_t st);
-cudaError_t launch_band_pair(const float2* Y, size_t y_stride, const float2* Fa, const float2* Fb, float2* W,
-                             size_t w_stride, int n, size_t total, cudaStream_t st);
-cudaError_t launch_crop_pair(const float2* W, size_t w_stride, float* out_a, float* out_b, size_t o_stride, int n,
-                            int m0, int m1, int m2, int L1, int L2, int off, float scale, cudaStream_t st);
-cudaError_t launch_crop_thresh_acc(const float2* W, size_t w_stride, float* acc, size_t a_stride, int n, int m0,
-                                   int m1, int m2, int L1, int L2, int off, const float* th, int ia, int ib,
-                                   int nb_item, float scale, uint32_t* ma, uint32_t* mb, size_t mask_stride,
-                                   cudaStream_t st);
-cudaError_t launch_place_masked(const float* u, size_t u_stride, const uint32_t* ma, const uint32_t* mb,
-                                size_t mask_stride, float2* W, size_t w_stride, int n, int m0, int m1, int m2, int L0,
-                                int L1, int L2, int off, cudaStream_t st);
-cudaError_t launch_spec_acc(const float2* Z, size_t z_stride, const float2* Fa, const float2* Fb, float2* S,
-                            size_t s_stride, int n, size_t total, bool first, cudaStream_t st);
-cudaError_t launch_fold_edge(const float* g, size_t g_stride, float* out, size_t o_stride, int n, int n0, int n1,
-                             int n2, int d0, int d1, int d2, cudaStream_t st);
+cudaError_t launch_fold_edge(const float* g, size_t g_stride, float* out, size_t o_stride, float* scratch,
+                             size_t s_stride, int n, int n0, int n1, int n2, int d0, int d1, int d2, cudaStream_t st);
 std::vector<double> meyer_filters_3d(int cube, int nlevels, const int* num_dirs);
 void filter_spectrum_3d(const double* f, int cube, int L0, int L1, int L2, std::vector<std::complex<double>>* out);
 void pyr_window_1d(int nr, double w, double tbw, int* K, std::vector<double>* v);

@@ -32,16 +32,20 @@ namespace {
 constexpr int kCube = 24;          // Meyer filter support (GetMeyerBasedFilter.m:18)
 constexpr int kSameOff = 12;       // convnfft 'same' offset: ceil((24 - 1) / 2)
 constexpr int kMaxGrid = 192;      // largest padded grid per dimension
-const int kFftLens[] = {16, 24, 32, 48, 64, 72, 96, 128, 144, 192, 256};
+const int kFftLens[] = {16, 24, 32, 48, 64, 72, 96, 128, 144, 192, 216, 256};
 
 bool is_fft_len(int n) {
   for (int v : kFftLens)
     if (v == n) return true;
   return false;
 }
-int conv_len(int m) {  // smallest supported length >= m + 23 (linear convolution)
+// Smallest supported circular-convolution length for the 'same' part of a
+// linear convolution of m samples with the 24-tap filter: outputs 12 .. m+11
+// alias no wrapped tap once N >= m + 12 (taps reach 23 back and 11 ahead of
+// the kept range), so the full m + 23 is not needed.
+int conv_len(int m) {
   for (int v : kFftLens)
-    if (v >= m + kCube - 1) return v;
+    if (v >= m + kSameOff) return v;
   return -1;
 }
 
@@ -161,9 +165,9 @@ struct nsst3_plan {
   float* th = nullptr;
 
   // differentiation: keep bits of every band of the last thresholded forward
-  uint32_t* mask = nullptr;
-  size_t mask_words = 0;            // per item
-  std::vector<size_t> mask_off;     // per band, in words
+  uint8_t* mask = nullptr;
+  size_t mask_bytes = 0;            // per item
+  std::vector<size_t> mask_off;     // per band, in bytes (bit k = voxel k of the band, linear order)
   int masks_valid_n = 0;            // items covered by the stored masks (0 = none)
 
   std::vector<double> scalars;
@@ -176,12 +180,78 @@ struct nsst3_plan {
 
 namespace {
 
-// Batched 3-D FFT of n complex volumes d0 x d1 x d2 (item stride `stride`):
-// axis 2, then 1, then 0; unnormalised.
-nsst_status fft3(nsst3_plan* p, float2* v, size_t stride, int n, const int* d, int dir, cudaStream_t st) {
-  for (int axis = 2; axis >= 0; axis--)
-    V3_CUDA(launch_fft3_axis(v, n, stride, d[0], d[1], d[2], axis, dir, p->twid(d[axis]), st));
+// Pass descriptors.  A pass transforms `axis`; (a, b) select the sequences
+// (axis 2: x, y; axis 1: x, z; axis 0: y, z), `in` the loaded index range and
+// `out` the stored one.
+struct Range {
+  int lo, n;
+};
+V3Pass make_pass(int axis, const int* D, size_t stride, Range a, Range b, Range in, Range out) {
+  V3Pass P;
+  P.axis = axis;
+  P.D1 = D[1];
+  P.D2 = D[2];
+  P.a_lo = a.lo, P.a_n = a.n, P.b_lo = b.lo, P.b_n = b.n;
+  P.in_lo = in.lo, P.in_n = in.n, P.out_lo = out.lo, P.out_n = out.n;
+  P.item_stride = stride;
+  return P;
+}
+void set_box(V3Pass& P, const int* m, int o) {
+  P.r1 = m[1];
+  P.r2 = m[2];
+  P.o0 = P.o1 = P.o2 = o;
+}
+
+nsst_status run_pass(nsst3_plan* p, const V3Pass& P, int dir, int ld, int st_mode, float2* out, const float2* in,
+                     int D_axis, int n, cudaStream_t st) {
+  V3_CUDA(launch_v3_pass(D_axis, dir, ld, st_mode, out, in, P, p->twid(D_axis), n, st));
   return NSST_OK;
+}
+
+// Batched full 3-D FFT of n complex volumes d0 x d1 x d2 (item stride
+// `stride`), in place: axis 2, then 1, then 0; unnormalised.
+nsst_status fft3(nsst3_plan* p, float2* v, size_t stride, int n, const int* d, int dir, cudaStream_t st) {
+  V3_TRY(run_pass(p, make_pass(2, d, stride, {0, d[0]}, {0, d[1]}, {0, d[2]}, {0, d[2]}), dir, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[2], n, st));
+  V3_TRY(run_pass(p, make_pass(1, d, stride, {0, d[0]}, {0, d[2]}, {0, d[1]}, {0, d[1]}), dir, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[1], n, st));
+  V3_TRY(run_pass(p, make_pass(0, d, stride, {0, d[1]}, {0, d[2]}, {0, d[0]}, {0, d[0]}), dir, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[0], n, st));
+  return NSST_OK;
+}
+
+// Forward FFT of real volumes of dims m (item stride rstride floats) zero
+// padded at the origin to the complex buffer v of dims d: the passes read
+// only the non-zero part.
+nsst_status fft3_real(nsst3_plan* p, const float* x, size_t rstride, const int* m, float2* v, size_t stride,
+                      const int* d, int n, cudaStream_t st) {
+  V3Pass P = make_pass(2, d, stride, {0, m[0]}, {0, m[1]}, {0, m[2]}, {0, d[2]});
+  P.rsrc = x;
+  P.r_stride = rstride;
+  set_box(P, m, 0);
+  V3_TRY(run_pass(p, P, -1, V3_LD_REAL, V3_ST_CPLX, v, v, d[2], n, st));
+  V3_TRY(run_pass(p, make_pass(1, d, stride, {0, m[0]}, {0, d[2]}, {0, m[1]}, {0, d[1]}), -1, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[1], n, st));
+  V3_TRY(run_pass(p, make_pass(0, d, stride, {0, d[1]}, {0, d[2]}, {0, m[0]}, {0, d[0]}), -1, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[0], n, st));
+  return NSST_OK;
+}
+
+// Inverse FFT of the complex buffer v (dims d) whose real part, times scale,
+// is wanted only in the box [o, o + m) of each axis: later passes skip the
+// sequences outside the box, the last one writes the real box to x.
+nsst_status ifft3_real_box(nsst3_plan* p, float2* v, size_t stride, const int* d, const int* m, int o, float* x,
+                           size_t rstride, float scale, int n, cudaStream_t st) {
+  V3_TRY(run_pass(p, make_pass(2, d, stride, {0, d[0]}, {0, d[1]}, {0, d[2]}, {o, m[2]}), +1, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[2], n, st));
+  V3_TRY(run_pass(p, make_pass(1, d, stride, {0, d[0]}, {o, m[2]}, {0, d[1]}, {o, m[1]}), +1, V3_LD_CPLX, V3_ST_CPLX,
+                  v, v, d[1], n, st));
+  V3Pass P = make_pass(0, d, stride, {o, m[1]}, {o, m[2]}, {0, d[0]}, {o, m[0]});
+  P.rdst = x;
+  P.r_stride = rstride;
+  P.scale = scale;
+  set_box(P, m, o);
+  return run_pass(p, P, +1, V3_LD_CPLX, V3_ST_REAL, v, v, d[0], n, st);
 }
 
 PyrWin level_window(const nsst3_plan* p, int l) {
@@ -198,7 +268,8 @@ PyrWin level_window(const nsst3_plan* p, int l) {
 }
 
 // PyrNDDec_mm.m:20-109 (OutD 'S') for n volumes x (dims in[3], padded to the
-// grid by edge replication) into the sub-band layout bp (item stride bp_floats).
+// grid by edge replication, or by zeros for the adjoint) into the sub-band
+// layout bp (item stride bp_floats).
 nsst_status run_pyr_dec(nsst3_plan* p, const float* x, const int* in, float* bp, int n, cudaStream_t st,
                         bool zero_pad = false) {
   const size_t xs = (size_t)in[0] * in[1] * in[2];
@@ -219,9 +290,8 @@ nsst_status run_pyr_dec(nsst3_plan* p, const float* x, const int* in, float* bp,
     }
     // subs{l} = real(ifftn(ccsym(Hp, 3, 'e')))   (lowpass: the last Lp)
     V3_CUDA(launch_conj_extend(p->xh + a.xh_off, p->xh_elems, p->vol, p->vol_elems, n, a.m[0], a.m[1], a.m[2], st));
-    V3_TRY(fft3(p, p->vol, p->vol_elems, n, a.m, +1, st));
-    V3_CUDA(launch_crop_real(p->vol, p->vol_elems, bp + a.bp_off, p->bp_floats, n, a.m[0], a.m[1], a.m[2], a.m[1],
-                             a.m[2], 0, 0, 0, (float)(1.0 / (double)a.vol()), st));
+    V3_TRY(ifft3_real_box(p, p->vol, p->vol_elems, a.m, a.m, 0, bp + a.bp_off, p->bp_floats,
+                          (float)(1.0 / (double)a.vol()), n, st));
   }
   return NSST_OK;
 }
@@ -231,9 +301,7 @@ nsst_status run_pyr_rec(nsst3_plan* p, const float* bp, float* x, const int* out
   for (int l = p->L; l >= 0; l--) {
     const nsst3_plan::Level& a = p->lev[l];
     // ccsym(fftn(subs{l}), 3, 'c')
-    V3_CUDA(launch_pad_real(bp + a.bp_off, p->bp_floats, p->vol, p->vol_elems, n, a.m[0], a.m[1], a.m[2], a.m[0],
-                            a.m[1], a.m[2], st));
-    V3_TRY(fft3(p, p->vol, p->vol_elems, n, a.m, -1, st));
+    V3_TRY(fft3_real(p, bp + a.bp_off, p->bp_floats, a.m, p->vol, p->vol_elems, a.m, n, st));
     V3_CUDA(launch_half(p->vol, p->vol_elems, p->xh + a.xh_off, p->xh_elems, n, a.m[0], a.m[1], a.m[2], st));
     if (l < p->L) {
       const nsst3_plan::Level& b = p->lev[l + 1];
@@ -250,36 +318,52 @@ nsst_status run_pyr_rec(nsst3_plan* p, const float* bp, float* x, const int* out
   return NSST_OK;
 }
 
-// Directional stage of one level.  acc != NULL: hard threshold (th, or none
-// when th is NULL) and band sum into acc (sub-band layout, level l region,
-// item stride bp_floats).  acc == NULL: band coefficients into coeffs
-// (nb volumes of the level per item, item stride nb * vol).
+// Directional stage of one level.  Y = FFT3(zero-pad(bp_l)) once; per band
+// pair, W = IFFT3(Y .* C) with C = F_a + i F_b, cut to the 'same' box at
+// offset 12.  acc != NULL: hard threshold (th, or none when th is NULL) and
+// band sum into acc (sub-band layout, level l region, item stride
+// bp_floats), with keep bits when record_masks.  acc == NULL: band
+// coefficients into coeffs (nb volumes of the level per item).
 nsst_status run_sh_level(nsst3_plan* p, const float* bp, int l, float* acc, const float* th, float* coeffs, int n,
                          cudaStream_t st, bool record_masks = false) {
   const nsst3_plan::Level& a = p->lev[l];
-  const size_t cv = a.conv();
-  V3_CUDA(launch_pad_real(bp + a.bp_off, p->bp_floats, p->Y, p->conv_elems, n, a.m[0], a.m[1], a.m[2], a.lc[0],
-                          a.lc[1], a.lc[2], st));
-  V3_TRY(fft3(p, p->Y, p->conv_elems, n, a.lc, -1, st));
-  const float scale = (float)(1.0 / (double)cv);
+  const int* N = a.lc;
+  const int* m = a.m;
+  const int o = kSameOff;
+  const size_t cs = p->conv_elems;
+  V3_TRY(fft3_real(p, bp + a.bp_off, p->bp_floats, m, p->Y, cs, N, n, st));
+  const float scale = (float)(1.0 / (double)a.conv());
   for (int k = 0; k < a.nb; k += 2) {
     const int ba = a.first_band + k;
     const int bb = k + 1 < a.nb ? ba + 1 : -1;
-    const float2* Fa = p->spec + a.spec_off + (size_t)k * cv;
-    const float2* Fb = bb >= 0 ? Fa + cv : nullptr;
-    V3_CUDA(launch_band_pair(p->Y, p->conv_elems, Fa, Fb, p->Wk, p->conv_elems, n, cv, st));
-    V3_TRY(fft3(p, p->Wk, p->conv_elems, n, a.lc, +1, st));
+    const float2* C = p->spec + a.spec_off + (size_t)(k / 2) * a.conv();
+    // z rows: the product, stored only where the box needs it
+    V3Pass P1 = make_pass(2, N, cs, {0, N[0]}, {0, N[1]}, {0, N[2]}, {o, m[2]});
+    P1.spec = C;
+    V3_TRY(run_pass(p, P1, +1, V3_LD_PAIR, V3_ST_CPLX, p->Wk, p->Y, N[2], n, st));
+    V3_TRY(run_pass(p, make_pass(1, N, cs, {0, N[0]}, {o, m[2]}, {0, N[1]}, {o, m[1]}), +1, V3_LD_CPLX, V3_ST_CPLX,
+                    p->Wk, p->Wk, N[1], n, st));
+    V3Pass P3 = make_pass(0, N, cs, {o, m[1]}, {o, m[2]}, {0, N[0]}, {o, m[0]});
+    set_box(P3, m, o);
+    P3.r_stride = p->bp_floats;
+    P3.scale = scale;
     if (acc) {
-      uint32_t* ma = record_masks ? p->mask + p->mask_off[ba] : nullptr;
-      uint32_t* mb = (record_masks && bb >= 0) ? p->mask + p->mask_off[bb] : nullptr;
-      V3_CUDA(launch_crop_thresh_acc(p->Wk, p->conv_elems, acc + a.bp_off, p->bp_floats, n, a.m[0], a.m[1], a.m[2],
-                                     a.lc[1], a.lc[2], kSameOff, th, ba, bb, p->nbands, scale, ma, mb, p->mask_words,
-                                     st));
+      P3.rdst = acc + a.bp_off;
+      P3.th = th;
+      P3.ia = ba;
+      P3.ib = bb;
+      P3.nb_item = p->nbands;
+      if (record_masks) {
+        P3.mwa = p->mask + p->mask_off[ba];
+        P3.mwb = bb >= 0 ? p->mask + p->mask_off[bb] : nullptr;
+        P3.m_stride = p->mask_bytes;
+      }
+      V3_TRY(run_pass(p, P3, +1, V3_LD_CPLX, V3_ST_THRESH, p->Wk, p->Wk, N[0], n, st));
     } else {
-      float* oa = coeffs + (size_t)k * a.vol();
-      float* ob = bb >= 0 ? oa + a.vol() : nullptr;
-      V3_CUDA(launch_crop_pair(p->Wk, p->conv_elems, oa, ob, (size_t)a.nb * a.vol(), n, a.m[0], a.m[1], a.m[2],
-                               a.lc[1], a.lc[2], kSameOff, scale, st));
+      P3.rdst = coeffs + (size_t)k * a.vol();
+      P3.rdst2 = bb >= 0 ? P3.rdst + a.vol() : nullptr;
+      P3.r_stride = (size_t)a.nb * a.vol();
+      V3_TRY(run_pass(p, P3, +1, V3_LD_CPLX, V3_ST_PAIR, p->Wk, p->Wk, N[0], n, st));
     }
   }
   return NSST_OK;
@@ -393,7 +477,7 @@ nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, i
         }
     p->nbands += a.nb;
     a.spec_off = spec_off;
-    spec_off += (size_t)a.nb * a.conv();
+    spec_off += (size_t)((a.nb + 1) / 2) * a.conv();  // one spectrum F_a + i F_b per band pair
     p->conv_elems = std::max(p->conv_elems, a.conv());
   }
   p->bp_floats = bp_off;
@@ -431,8 +515,8 @@ nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, i
       if (l < p->L) add_tw(p->lev[l].lc[k]);
     }
   for (auto& kv : p->tw_off) {
-    cudaError_t e = prepare_fft3(kv.first);
-    if (e != cudaSuccess) return cuda_fail3(e, "prepare_fft3");
+    cudaError_t e = prepare_v3_pass(kv.first);
+    if (e != cudaSuccess) return cuda_fail3(e, "prepare_v3_pass");
   }
 
   // one device arena
@@ -478,11 +562,16 @@ nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, i
       (e = cudaMemcpy(p->tw, tw_host.data(), tw_host.size() * sizeof(float2), cudaMemcpyHostToDevice)))
     return cleanup(cuda_fail3(e, "plan tables"));
 
-  // Meyer filters (FP64) and their convolution spectra, FP64 on host worker
-  // threads, each band converted to FP32 and uploaded as it is finished.
+  // Meyer filters (FP64) and the convolution spectra of each band pair,
+  // C = F_a + i F_b, FP64 on host worker threads, converted to FP32 and
+  // uploaded as each is finished.
   const std::vector<double> filt = meyer_filters_3d(kCube, p->L, cfg->num_dirs);
   const size_t f3 = (size_t)kCube * kCube * kCube;
-  const int nthreads = std::min(host_threads3(), p->nbands);
+  std::vector<int> pair_a;  // first band of every pair
+  for (int l = 0; l < p->L; l++)
+    for (int k = 0; k < p->lev[l].nb; k += 2) pair_a.push_back(p->lev[l].first_band + k);
+  const int npairs = (int)pair_a.size();
+  const int nthreads = std::min(host_threads3(), npairs);
   std::vector<cudaError_t> terr(nthreads, cudaSuccess);
   std::vector<std::thread> workers;
   for (int t = 0; t < nthreads; t++) {
@@ -491,14 +580,21 @@ nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, i
         terr[t] = cudaErrorInvalidDevice;
         return;
       }
-      std::vector<cd> S;
+      std::vector<cd> Sa, Sb;
       std::vector<float2> s32;
-      for (int b = t; b < raw->nbands; b += nthreads) {
+      for (int q = t; q < npairs; q += nthreads) {
+        const int b = pair_a[q];
         const nsst3_plan::Level& a = raw->lev[raw->band_level[b]];
-        filter_spectrum_3d(filt.data() + (size_t)b * f3, kCube, a.lc[0], a.lc[1], a.lc[2], &S);
-        s32.resize(S.size());
-        for (size_t i = 0; i < S.size(); i++) s32[i] = make_float2((float)S[i].real(), (float)S[i].imag());
-        const size_t dst = a.spec_off + (size_t)(b - a.first_band) * a.conv();
+        const bool has_b = b + 1 < a.first_band + a.nb;
+        filter_spectrum_3d(filt.data() + (size_t)b * f3, kCube, a.lc[0], a.lc[1], a.lc[2], &Sa);
+        if (has_b) filter_spectrum_3d(filt.data() + (size_t)(b + 1) * f3, kCube, a.lc[0], a.lc[1], a.lc[2], &Sb);
+        s32.resize(Sa.size());
+        for (size_t i = 0; i < Sa.size(); i++) {
+          cd c = Sa[i];
+          if (has_b) c += cd(0, 1) * Sb[i];
+          s32[i] = make_float2((float)c.real(), (float)c.imag());
+        }
+        const size_t dst = a.spec_off + (size_t)((b - a.first_band) / 2) * a.conv();
         cudaError_t ce = cudaMemcpy(raw->spec + dst, s32.data(), s32.size() * sizeof(float2), cudaMemcpyHostToDevice);
         if (ce != cudaSuccess) {
           terr[t] = ce;
@@ -692,16 +788,16 @@ nsst_status nsst3_plan_enable_grad(nsst3_plan* p) {
   if (cudaSetDevice(p->device) != cudaSuccess) return fail3(NSST_ERR_CUDA, "cudaSetDevice failed");
   std::lock_guard<std::mutex> lk(p->mu);
   p->mask_off.assign(p->nbands, 0);
-  size_t words = 0;
+  size_t bytes = 0;
   for (int b = 0; b < p->nbands; b++) {
-    p->mask_off[b] = words;
-    words += align_up3(p->lev[p->band_level[b]].vol() / 32, 8);
+    p->mask_off[b] = bytes;
+    bytes += align_up3(p->lev[p->band_level[b]].vol() / 8, 256);
   }
-  p->mask_words = words;
+  p->mask_bytes = bytes;
   void* m = nullptr;
-  cudaError_t e = dev_alloc(&m, (size_t)p->B * words * sizeof(uint32_t));
+  cudaError_t e = dev_alloc(&m, (size_t)p->B * bytes);
   if (e != cudaSuccess) return cuda_fail3(e, "mask buffer");
-  p->mask = (uint32_t*)m;
+  p->mask = (uint8_t*)m;
   p->masks_valid_n = 0;
   return NSST_OK;
 }
@@ -715,24 +811,36 @@ nsst_status nsst3_denoise_backward(nsst3_plan* p, const float* gy, float* gx, in
   const cudaStream_t st = (cudaStream_t)stream;
   // u = pyr_dec(zero-pad(gy)): the adjoint of crop + pyr_rec
   V3_TRY(run_pyr_dec(p, gy, p->n, p->rbp, n, st, true));
-  // per level: bp_bar_l = sum_b corr(mask_b * u_l, f_b)
+  // per level: bp_bar_l = sum_b corr(mask_b * u_l, f_b).  Per band pair,
+  // Z = FFT3(place(mask_a u + i mask_b u)) from the box outwards (the zero
+  // outside the box is never read), then S (+)= conj(C) .* Z in the last
+  // pass; one inverse transform of S per level, cut to the box at 0.
   for (int l = 0; l < p->L; l++) {
     const nsst3_plan::Level& a = p->lev[l];
-    const size_t cv = a.conv();
+    const int* N = a.lc;
+    const int* m = a.m;
+    const int o = kSameOff;
+    const size_t cs = p->conv_elems;
     for (int k = 0; k < a.nb; k += 2) {
       const int ba = a.first_band + k;
       const int bb = k + 1 < a.nb ? ba + 1 : -1;
-      const float2* Fa = p->spec + a.spec_off + (size_t)k * cv;
-      const float2* Fb = bb >= 0 ? Fa + cv : nullptr;
-      V3_CUDA(launch_place_masked(p->rbp + a.bp_off, p->bp_floats, p->mask + p->mask_off[ba],
-                                  bb >= 0 ? p->mask + p->mask_off[bb] : nullptr, p->mask_words, p->Wk, p->conv_elems,
-                                  n, a.m[0], a.m[1], a.m[2], a.lc[0], a.lc[1], a.lc[2], kSameOff, st));
-      V3_TRY(fft3(p, p->Wk, p->conv_elems, n, a.lc, -1, st));
-      V3_CUDA(launch_spec_acc(p->Wk, p->conv_elems, Fa, Fb, p->Y, p->conv_elems, n, cv, k == 0, st));
+      V3Pass P1 = make_pass(0, N, cs, {o, m[1]}, {o, m[2]}, {o, m[0]}, {0, N[0]});
+      set_box(P1, m, o);
+      P1.rsrc = p->rbp + a.bp_off;
+      P1.r_stride = p->bp_floats;
+      P1.mka = p->mask + p->mask_off[ba];
+      P1.mkb = bb >= 0 ? p->mask + p->mask_off[bb] : nullptr;
+      P1.m_stride = p->mask_bytes;
+      V3_TRY(run_pass(p, P1, -1, V3_LD_MASKED, V3_ST_CPLX, p->Wk, p->Wk, N[0], n, st));
+      V3_TRY(run_pass(p, make_pass(1, N, cs, {0, N[0]}, {o, m[2]}, {o, m[1]}, {0, N[1]}), -1, V3_LD_CPLX, V3_ST_CPLX,
+                      p->Wk, p->Wk, N[1], n, st));
+      V3Pass P3 = make_pass(2, N, cs, {0, N[0]}, {0, N[1]}, {o, m[2]}, {0, N[2]});
+      P3.spec = p->spec + a.spec_off + (size_t)(k / 2) * a.conv();
+      P3.first = k == 0;
+      V3_TRY(run_pass(p, P3, -1, V3_LD_CPLX, V3_ST_SPEC, p->Y, p->Wk, N[2], n, st));
     }
-    V3_TRY(fft3(p, p->Y, p->conv_elems, n, a.lc, +1, st));
-    V3_CUDA(launch_crop_real(p->Y, p->conv_elems, p->bp + a.bp_off, p->bp_floats, n, a.m[0], a.m[1], a.m[2], a.lc[1],
-                             a.lc[2], 0, 0, 0, (float)(1.0 / (double)cv), st));
+    V3_TRY(ifft3_real_box(p, p->Y, cs, N, m, 0, p->bp + a.bp_off, p->bp_floats, (float)(1.0 / (double)a.conv()), n,
+                          st));
   }
   // the lowpass passes through unchanged
   const nsst3_plan::Level& lp = p->lev[p->L];
@@ -740,8 +848,8 @@ nsst_status nsst3_denoise_backward(nsst3_plan* p, const float* gy, float* gx, in
                             p->bp_floats * sizeof(float), lp.vol() * sizeof(float), n, cudaMemcpyDeviceToDevice, st));
   // pyr_rec (the adjoint of pyr_dec) to the full grid, then fold the edge padding
   V3_TRY(run_pyr_rec(p, p->bp, p->rbp, p->g, n, st));
-  V3_CUDA(launch_fold_edge(p->rbp, p->vol_elems, gx, p->in_elems, n, p->n[0], p->n[1], p->n[2], p->g[0], p->g[1],
-                           p->g[2], st));
+  V3_CUDA(launch_fold_edge(p->rbp, p->vol_elems, gx, p->in_elems, (float*)p->vol, 2 * p->vol_elems, n, p->n[0],
+                           p->n[1], p->n[2], p->g[0], p->g[1], p->g[2], st));
   return NSST_OK;
 }
 
