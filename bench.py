@@ -42,6 +42,11 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
+    ap.add_argument('--batch', type=int, default=BATCH, help='images per batched pass (smaller for profiling)')
+    ap.add_argument('--workload', default='2d', choices=['2d', 'v3'],
+                    help="v3: only the 3-D volume extra (for profiling its kernels)")
+    ap.add_argument('--v3-sizes', default='128,192', help='volume edge lengths of the v3 workload')
+    ap.add_argument('--v3-batch', type=int, default=4, help='volumes per batched v3 pass')
     return ap.parse_args()
 
 
@@ -197,18 +202,18 @@ def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
     return b
 
 
-def volume_bench(sc, torch, dev, stream, flush, rank, reps=3):
+def volume_bench(sc, torch, dev, stream, flush, rank, reps=3, sizes=(128, 192), batch=4):
     """3-D denoise of seeded ellipsoid sequences (sigma 30, T = [3.3 3 3]):
     volumes/s of the batched forward and of forward + adjoint (gradient with
     respect to the volumes at the forward's threshold masks)."""
     from shearcuda_gb300.synth import noisy_volume
     out = {'num_dirs': list(sc.V3_NUM_DIRS), 'T': list(sc.DEMO_T[:3]), 'sigma': 30.0}
-    for n in (128, 192):
-        p = sc.VolumePlan(n, n, n, num_dirs=sc.V3_NUM_DIRS, batch=4)
+    for n in sizes:
+        p = sc.VolumePlan(n, n, n, num_dirs=sc.V3_NUM_DIRS, batch=batch)
         sc.nsst_scalars3(p, seed=9)
         p.enable_grad()
         xb = torch.stack([torch.tensor(noisy_volume((n, n, n), 30.0, 500 * rank + i)[1].astype(np.float32),
-                                       device=dev) for i in range(4)])
+                                       device=dev) for i in range(batch)])
         ob = torch.empty_like(xb)
         gy = torch.randn_like(xb)
         gx = torch.empty_like(xb)
@@ -239,9 +244,9 @@ def volume_bench(sc, torch, dev, stream, flush, rank, reps=3):
                 torch.cuda.synchronize()
                 tt += e0.elapsed_time(e1)
             res[name] = tt / reps
-        res['volumes_per_s'] = 4 / (res['forward_ms'] / 1000.0)
+        res['volumes_per_s'] = batch / (res['forward_ms'] / 1000.0)
         res['ratio'] = res['forward_adjoint_ms'] / res['forward_ms']
-        out['b4x%d' % n] = res
+        out['b%dx%d' % (batch, n)] = res
         p.close()
         del xb, ob, gy, gx
     return out
@@ -344,7 +349,8 @@ def run_gpu(args):
     line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded ellipses + gradient + N(0, 20^2))',
-            'config': {'workload': 'batch of 64 x 512x512 images, one batched NSST dec+hard-thresh+rec pass per step',
+            'config': {'workload': 'batch of %d x 512x512 images, one batched NSST dec+hard-thresh+rec pass per step'
+                                   % BATCH,
                        'H': H, 'W': W, 'batch_per_gpu': BATCH, 'dcomp': DCOMP, 'dsize': DSIZE, 'lpfilt': 'maxflat',
                        'K': K, 'sigma': SIGMA, 'parallelism': 'replicas' if world > 1 else 'single',
                        'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True},
@@ -476,10 +482,25 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_v3(args):
+    import torch
+    import shearcuda_gb300 as sc
+    dev = torch.device('cuda', 0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    sizes = tuple(int(v) for v in args.v3_sizes.split(','))
+    res = volume_bench(sc, torch, dev, torch.cuda.current_stream(), flush, 0, reps=max(1, args.steps), sizes=sizes,
+                       batch=args.v3_batch)
+    print(json.dumps({'workload': 'v3', 'volume_v3': res}), flush=True)
+
+
 def main():
     args = parse()
+    global BATCH
+    BATCH = args.batch
     if args.impl == 'reference':
         run_reference(args)
+    elif args.workload == 'v3':
+        run_v3(args)
     else:
         run_gpu(args)
 
