@@ -109,6 +109,46 @@ struct Dft<8, DIR> {
   }
 };
 
+// 16 = 4 x 4: 4-point DFTs over n2 of x[n1 + 4 n2], twiddles W16^(n1 k2),
+// 4-point DFTs over n1 -> X[k2 + 4 k1].
+template <int DIR>
+struct Dft<16, DIR> {
+  __device__ __forceinline__ static void run(float2* v) {
+    const float r = 0.70710678118654752440f;   // cos(pi/4)
+    const float c1 = 0.92387953251128675613f;  // cos(pi/8)
+    const float s1 = 0.38268343236508977173f;  // sin(pi/8)
+    float2 y[4][4];
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++) {
+      float2 t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+      Dft<4, DIR>::run(t);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; k2++) y[n1][k2] = t[k2];
+    }
+    // W16^m = exp(DIR * 2 pi i m / 16) for m = n1 * k2 in {1, 2, 3, 4, 6, 9}
+    const float sg = DIR < 0 ? -1.f : 1.f;
+    auto rot = [&](float2 a, float c, float sn) {  // a * (c + i sg sn)
+      return make_float2(a.x * c - sg * sn * a.y, a.y * c + sg * sn * a.x);
+    };
+    y[1][1] = rot(y[1][1], c1, s1);
+    y[1][2] = rot(y[1][2], r, r);
+    y[1][3] = rot(y[1][3], s1, c1);
+    y[2][1] = rot(y[2][1], r, r);
+    y[2][2] = mul_i<DIR>(y[2][2]);
+    y[2][3] = rot(y[2][3], -r, r);
+    y[3][1] = rot(y[3][1], s1, c1);
+    y[3][2] = rot(y[3][2], -r, r);
+    y[3][3] = rot(y[3][3], -c1, -s1);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) {
+      float2 t[4] = {y[0][k2], y[1][k2], y[2][k2], y[3][k2]};
+      Dft<4, DIR>::run(t);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; k1++) v[k2 + 4 * k1] = t[k1];
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Radix plans per length (product of radices == N).
 // ---------------------------------------------------------------------------
@@ -117,23 +157,23 @@ struct RadixList {};
 
 template <int N>
 struct FftPlan;
-template <> struct FftPlan<16> { using type = RadixList<4, 4>; };
+template <> struct FftPlan<16> { using type = RadixList<16>; };
 template <> struct FftPlan<24> { using type = RadixList<3, 8>; };
 template <> struct FftPlan<32> { using type = RadixList<4, 8>; };
-template <> struct FftPlan<48> { using type = RadixList<3, 4, 4>; };
+template <> struct FftPlan<48> { using type = RadixList<3, 16>; };
 template <> struct FftPlan<64> { using type = RadixList<8, 8>; };
 template <> struct FftPlan<72> { using type = RadixList<3, 3, 8>; };
-template <> struct FftPlan<144> { using type = RadixList<3, 3, 4, 4>; };
+template <> struct FftPlan<144> { using type = RadixList<3, 3, 16>; };
 template <> struct FftPlan<96> { using type = RadixList<3, 4, 8>; };
-template <> struct FftPlan<128> { using type = RadixList<8, 4, 4>; };
+template <> struct FftPlan<128> { using type = RadixList<16, 8>; };
 template <> struct FftPlan<192> { using type = RadixList<3, 8, 8>; };
 template <> struct FftPlan<216> { using type = RadixList<3, 3, 3, 8>; };
-template <> struct FftPlan<256> { using type = RadixList<4, 8, 8>; };
-template <> struct FftPlan<384> { using type = RadixList<3, 2, 8, 8>; };
+template <> struct FftPlan<256> { using type = RadixList<16, 16>; };
+template <> struct FftPlan<384> { using type = RadixList<3, 16, 8>; };
 template <> struct FftPlan<512> { using type = RadixList<8, 8, 8>; };
-template <> struct FftPlan<768> { using type = RadixList<3, 4, 8, 8>; };
-template <> struct FftPlan<1024> { using type = RadixList<8, 8, 8, 2>; };
-template <> struct FftPlan<2048> { using type = RadixList<4, 8, 8, 8>; };
+template <> struct FftPlan<768> { using type = RadixList<3, 16, 16>; };
+template <> struct FftPlan<1024> { using type = RadixList<16, 16, 4>; };
+template <> struct FftPlan<2048> { using type = RadixList<16, 16, 8>; };
 
 // One Stockham pass of radix R over NSEQ sequences of length N, in place.
 // NS = product of the radices already applied.  All threads participate.
@@ -360,6 +400,94 @@ __device__ __forceinline__ float2* fft_pp_passes(float2* a, float2* b, const flo
 template <int N, int NSEQ, int T, int DIR>
 __device__ __forceinline__ float2* block_fft_pp(float2* a, float2* b, const float2* __restrict__ tw) {
   return fft_pp_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, typename FftPlan<N>::type{});
+}
+
+// ---------------------------------------------------------------------------
+// Ping-pong FFT with hooks: the first pass reads its inputs through `ld`
+// (natural index, sequence) and the last pass writes its outputs through
+// `st` (natural index, sequence, value) instead of the shared buffers, so a
+// prologue (a spectrum product, the packed-real pre-processing, a load from
+// global memory) or an epilogue (a threshold, a store to global memory) costs
+// no extra shared-memory round trip or barrier.  Intermediate passes use a
+// and b alternately (pass 1 writes b).  The first pass ends with a barrier
+// like every pass, so `ld` may read the buffer the second pass writes.
+// ---------------------------------------------------------------------------
+template <typename RL>
+struct RadixCount;
+template <int... Rs>
+struct RadixCount<RadixList<Rs...>> {
+  static constexpr int value = sizeof...(Rs);
+};
+template <int N>
+__host__ __device__ constexpr int fft_npasses() {
+  return RadixCount<typename FftPlan<N>::type>::value;
+}
+
+template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT, class Rd, class Wr>
+__device__ __forceinline__ void stockham_hook(const Rd& rd, const Wr& wr, const float2* __restrict__ tw) {
+  constexpr int NB = N / R;
+  constexpr int TOTAL = NB * NSEQ;
+  constexpr int STEP = N / (NS * R);
+#pragma unroll 2
+  for (int w = threadIdx.x; w < TOTAL; w += T) {
+    const int s = w % NSEQ;
+    const int j = w / NSEQ;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = rd(swz_row<NSEQ, SWZ_IN>(j + r * NB), s);
+    const int k = j % NS;
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        float2 t = __ldg(&tw[r * k * STEP]);
+        v[r] = DIR < 0 ? cmul(v[r], t) : cmulc(v[r], t);
+      }
+    }
+    Dft<R, DIR>::run(v);
+    const int base = (j / NS) * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) wr(swz_row<NSEQ, SWZ_OUT>(base + r * NS), s, v[r]);
+  }
+  __syncthreads();
+}
+
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St>
+__device__ __forceinline__ void fft_hook_passes(float2*, float2*, const float2* __restrict__, const Ld&, const St&,
+                                                RadixList<>) {}
+
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, int R, int... Rest>
+__device__ __forceinline__ void fft_hook_passes(float2* a, float2* b, const float2* __restrict__ tw, const Ld& ld,
+                                                const St& st, RadixList<R, Rest...>) {
+  constexpr bool first = NS == 1;
+  constexpr bool last = sizeof...(Rest) == 0;
+  constexpr int SWZ_OUT = (first && !last && R % 2 == 0) ? R : 0;
+  auto rd = [&](int row, int s) -> float2 {
+    if constexpr (first)
+      return ld(row, s);
+    else
+      return a[row * NSEQ + s];
+  };
+  auto wr = [&](int row, int s, float2 v) {
+    if constexpr (last)
+      st(row, s, v);
+    else
+      b[row * NSEQ + s] = v;
+  };
+  stockham_hook<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+  fft_hook_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(b, a, tw, ld, st, RadixList<Rest...>{});
+}
+
+// The buffer the last pass's default target would be (a for an even pass
+// count, b for an odd one); an `st` writing shared memory writes there.
+template <int N>
+__device__ __forceinline__ float2* fft_hook_target(float2* a, float2* b) {
+  return (fft_npasses<N>() & 1) ? b : a;
+}
+
+template <int N, int NSEQ, int T, int DIR, class Ld, class St>
+__device__ __forceinline__ void block_fft_hook(float2* a, float2* b, const float2* __restrict__ tw, const Ld& ld,
+                                               const St& st) {
+  fft_hook_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, ld, st, typename FftPlan<N>::type{});
 }
 
 // Out-of-place packed-real post-processing (after a forward FFT of the

@@ -50,7 +50,8 @@ struct ColCfg {  // N = H points per column
 // CTA keep that share at 8 complex values per thread.
 template <int N>
 struct SynCfg : ColCfg<N> {
-  static constexpr int T = N >= 2048 ? 1024 : 512;
+  static constexpr int T = N >= 2048 ? 1024 : ((N * ColCfg<N>::CS) % 512 == 0 ? 512 : 256);
+  static constexpr int MINB = 1024 / T;
 };
 
 __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
@@ -79,6 +80,75 @@ __device__ __forceinline__ void store_rows(float2* __restrict__ dst, const float
   }
 }
 
+// FFT hooks (see block_fft_hook).
+template <int NSEQ>
+struct SmemLd {
+  const float2* p;
+  __device__ __forceinline__ float2 operator()(int i, int s) const { return p[i * NSEQ + s]; }
+};
+template <int NSEQ>
+struct SmemSt {
+  float2* p;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[i * NSEQ + s] = v; }
+};
+// packed-real pre-processing of index k (see c2r_pre): Z[k] = E + iO with
+// E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k; k = 0 unpacks
+// the two real bins.
+template <int WH, int NSEQ>
+struct C2RPreLd {
+  const float2* X;
+  const float2* twW;
+  __device__ __forceinline__ float2 operator()(int k, int s) const {
+    const float2 xk = X[k * NSEQ + s];
+    if (k == 0) return make_float2(xk.x + xk.y, xk.x - xk.y);
+    const float2 xmc = cconj(X[(WH - k) * NSEQ + s]);
+    const float2 E = cadd(xk, xmc);
+    const float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));
+    return make_float2(E.x - O.y, E.y + O.x);
+  }
+};
+template <int NSEQ>
+struct ThreshSt {
+  float2* p;
+  float th;
+  int mode;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const {
+    v.x = apply_thresh(v.x, th, mode);
+    v.y = apply_thresh(v.y, th, mode);
+    p[i * NSEQ + s] = v;
+  }
+};
+// rows of the CTA straight to global memory: element (i, s) -> dst[s * WH + i]
+template <int WH>
+struct RowGlobalSt {
+  float2* dst;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { dst[(size_t)s * WH + i] = v; }
+};
+
+// packed-real post-processing of every index k (see r2c_post) fused with the
+// store of the CTA's rows: X[k] = E + w^k O, E = (Z[k] + conj(Z[WH-k]))/2,
+// O = (Z[k] - conj(Z[WH-k]))/(2i); k = 0 packs the two real bins.
+template <int WH, int RS, int T>
+__device__ __forceinline__ void r2c_post_store(float2* __restrict__ dst, const float2* Z,
+                                               const float2* __restrict__ twW) {
+#pragma unroll 4
+  for (int e = threadIdx.x; e < WH * RS; e += T) {
+    const int s = e % RS, k = e / RS;
+    const float2 zk = Z[k * RS + s];
+    float2 out;
+    if (k == 0) {
+      out = make_float2(zk.x + zk.y, zk.x - zk.y);
+    } else {
+      const float2 zmc = cconj(Z[(WH - k) * RS + s]);
+      const float2 E = cscale(cadd(zk, zmc), 0.5f);
+      const float2 d = cscale(csub(zk, zmc), 0.5f);
+      const float2 To = cmul(__ldg(&twW[k]), make_float2(d.y, -d.x));
+      out = cadd(E, To);
+    }
+    dst[(size_t)s * WH + k] = out;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Row kernels.  grid = (H / RS, njobs).
 // ---------------------------------------------------------------------------
@@ -97,10 +167,9 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_fwd(const RowJob* __rest
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  float2* X = block_fft_pp<WH, C::RS, C::T, -1>(A, B, twWh);
-  float2* Y = (X == A) ? B : A;
-  r2c_post_pp<WH, C::RS, C::LD, C::T>(X, Y, twW);
-  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, Y);
+  float2* Z = fft_hook_target<WH>(A, B);
+  block_fft_hook<WH, C::RS, C::T, -1>(A, B, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{Z});
+  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
 }
 
 // packed rows -> real rows (inverse C2R along W, unnormalised: x W)
@@ -117,9 +186,8 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_inv(const RowJob* __rest
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
-  float2* X = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
-  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, X);
+  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW},
+                                      RowGlobalSt<WH>{dst_base + job.dst + off});
 }
 
 // packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
@@ -138,23 +206,15 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __r
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
-  float2* X = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
-  for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
-    const int i = e / C::RS, s = e % C::RS;
-    float2 v = X[i * C::LD + s];
-    v.x = apply_thresh(v.x, th, mode);
-    v.y = apply_thresh(v.y, th, mode);
-    X[i * C::LD + s] = v;
-  }
-  __syncthreads();
+  // C2R (pre-processing in the first pass) with the threshold in the last pass
+  float2* X = fft_hook_target<WH>(A, B);
+  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW}, ThreshSt<C::RS>{X, th, mode});
+  // R2C of the thresholded rows; post-processing fused with the store
   float2* Y = (X == A) ? B : A;
-  float2* Z = block_fft_pp<WH, C::RS, C::T, -1>(X, Y, twWh);
-  float2* O = (Z == A) ? B : A;
-  r2c_post_pp<WH, C::RS, C::LD, C::T>(Z, O, twW);
-  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, O);
+  float2* Z = fft_hook_target<WH>(X, Y);
+  block_fft_hook<WH, C::RS, C::T, -1>(X, Y, twWh, SmemLd<C::RS>{X}, SmemSt<C::RS>{Z});
+  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
 }
-
 
 // Backward band row pass (adjoint of the threshold step, rows of one band):
 // coefficients c = C2R(Qc) are recomputed, g = C2R(Qg) is the gradient w.r.t.
@@ -217,7 +277,40 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
 // Column kernels.  grid = (WH / CS, njobs).
 // ---------------------------------------------------------------------------
 
-// plain column FFT (forward or inverse) src -> dst
+// Column hooks: element (i, s) of the CTA's column group is image element
+// (row i, column col0 + s) of an H x WH packed array.
+struct ColGlobalLd {
+  const float2* src;
+  int WH;
+  __device__ __forceinline__ float2 operator()(int i, int s) const { return src[(size_t)i * WH + s]; }
+};
+struct ColGlobalSt {
+  float2* dst;
+  int WH;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { dst[(size_t)i * WH + s] = v; }
+};
+// Wk .* Z for the analysis, with the packed DC/Nyquist column's
+// Z'[u] = P[u] Z[u] + M[u] conj(Z[-u]) (src, spec: column group origin)
+template <int H>
+struct AnalysisLd {
+  const float2* src;
+  const float2* spec;
+  const float2* m0;
+  int WH;
+  bool dc;  // the group holds column 0
+  __device__ __forceinline__ float2 operator()(int i, int s) const {
+    const size_t g = (size_t)i * WH + s;
+    float2 r = cmul(__ldg(&spec[g]), src[g]);
+    if (dc && s == 0) {
+      const float2 zm = src[(size_t)((H - i) % H) * WH];
+      r = cadd(r, cmul(__ldg(&m0[i]), cconj(zm)));
+    }
+    return r;
+  }
+};
+
+// plain column FFT (forward or inverse) src -> dst, straight from and to
+// global memory through the first and last passes
 template <int H, int DIR>
 __global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH,
                                                         const float2* src_base, float2* dst_base,
@@ -228,18 +321,8 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict_
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
-#pragma unroll 4
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int i = e / C::CS, s = e % C::CS;
-    A[i * C::LD + s] = src_base[job.src + (size_t)i * WH + col0 + s];
-  }
-  __syncthreads();
-  float2* X = block_fft_pp<H, C::CS, C::T, DIR>(A, B, twH);
-#pragma unroll 4
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int i = e / C::CS, s = e % C::CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
-  }
+  block_fft_hook<H, C::CS, C::T, DIR>(A, B, twH, ColGlobalLd{src_base + job.src + col0, WH},
+                                      ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
 // analysis band: dst = colIFFT( Wk .* src ), src = fully transformed level spectrum
@@ -254,32 +337,17 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_band_analysis(const ColJob* __
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
-#pragma unroll 4
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int i = e / C::CS, s = e % C::CS;
-    const size_t g = (size_t)i * WH + col0 + s;
-    const float2 z = src_base[job.src + g];
-    float2 r = cmul(__ldg(&spec_base[job.spec + g]), z);
-    if (col0 + s == 0) {  // packed DC/Nyquist column
-      const float2 zm = src_base[job.src + (size_t)((H - i) % H) * WH];
-      r = cadd(r, cmul(__ldg(&spec_base[job.m0 + i]), cconj(zm)));
-    }
-    A[i * C::LD + s] = r;
-  }
-  __syncthreads();
-  float2* X = block_fft_pp<H, C::CS, C::T, +1>(A, B, twH);
-#pragma unroll 4
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int i = e / C::CS, s = e % C::CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
-  }
+  block_fft_hook<H, C::CS, C::T, +1>(
+      A, B, twH,
+      AnalysisLd<H>{src_base + job.src + col0, spec_base + job.spec + col0, spec_base + job.m0, WH, col0 == 0},
+      ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
 // synthesis: dst = colIFFT( sum_k conj(Wk) .* colFFT(src_k) ) over job.nbands
 // bands stored at src + k * band_stride, spectra at spec + k * band_stride,
 // side arrays at m0 + k * H.  The running sum stays in registers.
 template <int H>
-__global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active,
+__global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active,
                                                                   int WH, const float2* src_base, float2* dst_base,
                                                                   const float2* __restrict__ spec_base,
                                                                   size_t band_stride,
@@ -295,9 +363,12 @@ __global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synt
   float2 acc[EPT];
 #pragma unroll
   for (int it = 0; it < EPT; it++) acc[it] = make_float2(0.f, 0.f);
+  float2* const X = fft_hook_target<H>(A, B);
   for (int k = 0; k < job.nbands; k++) {
     const float2* src = src_base + job.src + k * band_stride;
     const float2* spec = spec_base + job.spec + k * band_stride;
+    // staged through shared memory: the accumulator already holds 2 EPT
+    // registers per thread across the transform
 #pragma unroll
     for (int it = 0; it < EPT; it++) {
       const int e = threadIdx.x + it * C::T;
@@ -305,7 +376,7 @@ __global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synt
       A[i * C::LD + s] = src[(size_t)i * WH + col0 + s];
     }
     __syncthreads();
-    const float2* X = block_fft_pp<H, C::CS, C::T, -1>(A, B, twH);
+    block_fft_hook<H, C::CS, C::T, -1>(A, B, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{X});
 #pragma unroll
     for (int it = 0; it < EPT; it++) {
       const int e = threadIdx.x + it * C::T;
@@ -327,12 +398,7 @@ __global__ void __launch_bounds__(SynCfg<H>::T, 1024 / SynCfg<H>::T) k_band_synt
     A[i * C::LD + s] = acc[it];
   }
   __syncthreads();
-  const float2* X = block_fft_pp<H, C::CS, C::T, +1>(A, B, twH);
-#pragma unroll 4
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int i = e / C::CS, s = e % C::CS;
-    dst_base[job.dst + (size_t)i * WH + col0 + s] = X[i * C::LD + s];
-  }
+  block_fft_hook<H, C::CS, C::T, +1>(A, B, twH, SmemLd<C::CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
 // ---------------------------------------------------------------------------
