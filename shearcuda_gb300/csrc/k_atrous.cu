@@ -17,9 +17,10 @@
 //
 // Tiling: a CTA owns 64 columns x 64 rows of one polyphase row class
 // (rows r = phase + M*t); with that split every tap row of the dilated filter
-// is a neighbouring tile row.  Each thread keeps 16 vertically adjacent
-// outputs in registers and streams one tap column at a time: 16+F-1 shared
-// loads feed 16*F FMAs.
+// is a neighbouring tile row.  Each thread keeps 8 vertically adjacent
+// outputs of two columns 32 apart in registers, as float2 pairs, and streams
+// one tap column at a time: 2(8+F-1) conflict-free shared loads feed 8F
+// packed FP32 FMAs (FFMA2, two outputs per instruction).
 #include <mutex>
 
 #include "internal.h"
@@ -27,10 +28,11 @@
 namespace nsst {
 
 constexpr int kAtTX = 64;   // tile width (columns)
-constexpr int kAtP = 16;    // outputs per thread (poly rows)
-constexpr int kAtTY = 4;    // thread rows
+constexpr int kAtHX = kAtTX / 2;  // threads across: columns tx and tx + 32
+constexpr int kAtP = 8;     // outputs per thread and column (poly rows)
+constexpr int kAtTY = 8;    // thread rows
 constexpr int kAtRows = kAtP * kAtTY;  // poly rows per tile
-constexpr int kAtThreads = kAtTX * kAtTY;
+constexpr int kAtThreads = kAtHX * kAtTY;
 
 __device__ __forceinline__ int mirror_index(int i, int n) {
   if (i < 0) i = -1 - i;
@@ -46,7 +48,7 @@ template <int F, bool ZERO>
 __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
                                                   int prow0, int col0, const float* __restrict__ taps,
                                                   const int* __restrict__ tapcols, int ntapcols, float* tile,
-                                                  float (&acc)[kAtP]) {
+                                                  float2 (&acc)[kAtP]) {
   constexpr int C0 = ZERO ? F - 1 : (F - 1) / 2;
   constexpr int TR = kAtRows + F - 1;
   const int TC = kAtTX + M * (F - 1);
@@ -64,18 +66,22 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
     }
   }
   __syncthreads();
-  const int tx = tid % kAtTX, ty = tid / kAtTX;
+  const int tx = tid % kAtHX, ty = tid / kAtHX;
   const float* base = tile + (ty * kAtP) * TC + tx;
   for (int ib = 0; ib < ntapcols; ib++) {
     const int b = tapcols[ib];
-    float col[kAtP + F - 1];
+    float2 col[kAtP + F - 1];
 #pragma unroll
-    for (int t = 0; t < kAtP + F - 1; t++) col[t] = base[t * TC + M * b];
+    for (int t = 0; t < kAtP + F - 1; t++) {
+      const float* q = base + t * TC + M * b;
+      col[t] = make_float2(q[0], q[kAtHX]);
+    }
 #pragma unroll
     for (int a = 0; a < F; a++) {
       const float w = taps[a * F + b];
+      const float2 w2 = make_float2(w, w);
 #pragma unroll
-      for (int p = 0; p < kAtP; p++) acc[p] = fmaf(w, col[p + a], acc[p]);
+      for (int p = 0; p < kAtP; p++) acc[p] = __ffma2_rn(w2, col[p + a], acc[p]);
     }
   }
   __syncthreads();
@@ -97,9 +103,9 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
   const int prow0 = (blockIdx.y / M) * kAtRows;
   const int nprow = (Ho - phase + M - 1) / M;  // output poly rows of this phase
   if (col0 >= Wo || prow0 >= nprow) return;
-  float acc[kAtP];
+  float2 acc[kAtP];
 #pragma unroll
-  for (int p = 0; p < kAtP; p++) acc[p] = 0.f;
+  for (int p = 0; p < kAtP; p++) acc[p] = make_float2(0.f, 0.f);
 
   for (int e = threadIdx.x; e < FA * FA; e += kAtThreads) s_taps[e] = ta.w[e];
   for (int e = threadIdx.x; e < ta.ncols; e += kAtThreads) s_cols[e] = ta.cols[e];
@@ -112,13 +118,15 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
     atrous_accumulate<(FB > 0 ? FB : 1), ZERO>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
                                                 at_smem, acc);
   }
-  const int tx = threadIdx.x % kAtTX, ty = threadIdx.x / kAtTX;
+  const int tx = threadIdx.x % kAtHX, ty = threadIdx.x / kAtHX;
   const int c = col0 + tx;
-  if (c < Wo) {
 #pragma unroll
-    for (int p = 0; p < kAtP; p++) {
-      int pr = prow0 + ty * kAtP + p;
-      if (pr < nprow) job.out[(size_t)(phase + M * pr) * Wo + c] = acc[p];
+  for (int p = 0; p < kAtP; p++) {
+    const int pr = prow0 + ty * kAtP + p;
+    if (pr < nprow) {
+      float* o = job.out + (size_t)(phase + M * pr) * Wo;
+      if (c < Wo) o[c] = acc[p].x;
+      if (c + kAtHX < Wo) o[c + kAtHX] = acc[p].y;
     }
   }
 }
