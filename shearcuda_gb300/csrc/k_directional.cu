@@ -34,7 +34,8 @@ namespace nsst {
 template <int N>
 struct RowCfg {  // N = W/2 complex points per row
   static constexpr int RS = N >= 1024 ? 4 : 8;
-  static constexpr int T = 256;
+  // 256 = 16 x 16: a radix-16 pass has 16 butterflies per row, one per thread
+  static constexpr int T = N == 256 ? 128 : 256;
   static constexpr int LD = RS;
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
@@ -367,16 +368,7 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
   for (int k = 0; k < job.nbands; k++) {
     const float2* src = src_base + job.src + k * band_stride;
     const float2* spec = spec_base + job.spec + k * band_stride;
-    // staged through shared memory: the accumulator already holds 2 EPT
-    // registers per thread across the transform
-#pragma unroll
-    for (int it = 0; it < EPT; it++) {
-      const int e = threadIdx.x + it * C::T;
-      const int i = e / C::CS, s = e % C::CS;
-      A[i * C::LD + s] = src[(size_t)i * WH + col0 + s];
-    }
-    __syncthreads();
-    block_fft_hook<H, C::CS, C::T, -1>(A, B, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{X});
+    block_fft_hook<H, C::CS, C::T, -1>(A, B, twH, ColGlobalLd{src + col0, WH}, SmemSt<C::CS>{X});
 #pragma unroll
     for (int it = 0; it < EPT; it++) {
       const int e = threadIdx.x + it * C::T;
