@@ -73,8 +73,8 @@ struct nsst_plan {
 
   RowJob* j_rows_lev_fwd = nullptr;   // pyr[1..] -> lev           (B*nlev)
   ColJob* j_cols_lev = nullptr;       // lev in place              (B*nlev)
-  ColJob* j_analysis = nullptr;       // lev -> band, band-major   (B*ndir_total)
-  RowJob* j_rows_bands = nullptr;     // band in place, band-major (B*ndir_total)
+  ColJob* j_analysis = nullptr;       // lev -> band, band-major in groups of 8 items (B*ndir_total)
+  RowJob* j_rows_bands = nullptr;     // band in place, same order (B*ndir_total)
   ColJob* j_synthesis = nullptr;      // band -> sum, level-major  (B*nlev)
   RowJob* j_rows_lev_inv = nullptr;   // sum -> rec[1..]           (B*nlev)
   RowJob* j_coeff_fwd = nullptr;      // caller coeffs -> band (item 0)
@@ -392,14 +392,19 @@ nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, 
         j6.push_back(RowJob{sum + (size_t)l * HWh, rec + (size_t)(l + 1) * HWh, 0, i});
       }
     }
-    // band-major over items: CTAs running together read the same spectrum tile
-    for (int b = 0; b < p->ndir_total; b++) {
-      const int l = p->band_level[1 + b] - 1;
-      for (int i = 0; i < B; i++) {
-        const size_t lev = f2(p->lev + i * p->s_lev), band = f2(p->band + i * p->s_band);
-        j3.push_back(ColJob{lev + (size_t)l * HWh, band + (size_t)b * HWh, (size_t)b * HWh,
-                            p->m0_off + (size_t)b * H, 1, i});
-        j4.push_back(RowJob{band + (size_t)b * HWh, band + (size_t)b * HWh, i * p->nbands + 1 + b, i});
+    // groups of 8 items, band-major inside a group: the CTAs running together
+    // read the same filter spectrum, and a group's level spectra (8 x 4 B/px)
+    // stay in L2 across the bands of their level
+    constexpr int kGroup = 8;
+    for (int g0 = 0; g0 < B; g0 += kGroup) {
+      for (int b = 0; b < p->ndir_total; b++) {
+        const int l = p->band_level[1 + b] - 1;
+        for (int i = g0; i < std::min(B, g0 + kGroup); i++) {
+          const size_t lev = f2(p->lev + i * p->s_lev), band = f2(p->band + i * p->s_band);
+          j3.push_back(ColJob{lev + (size_t)l * HWh, band + (size_t)b * HWh, (size_t)b * HWh,
+                              p->m0_off + (size_t)b * H, 1, i});
+          j4.push_back(RowJob{band + (size_t)b * HWh, band + (size_t)b * HWh, i * p->nbands + 1 + b, i});
+        }
       }
     }
     for (int l = 0; l < p->nlev; l++) {
@@ -681,8 +686,7 @@ nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* 
   NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
                         st));
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
-  // item-0 analysis jobs sit at stride B in the band-major list: use a per-band
-  // launch window of B jobs with n_active = 1
+  // the job list covers every item; n_active = 1 skips the others
   NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, p->B * p->ndir_total, 1, p->H, p->W, A2, A2, p->spec, 0,
                         p->twH, st));
   timer_mark(p, "band_analysis_cols", st);
