@@ -401,6 +401,11 @@ template <int N, int NSEQ, int T, int DIR>
 __device__ __forceinline__ float2* block_fft_pp(float2* a, float2* b, const float2* __restrict__ tw) {
   return fft_pp_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, typename FftPlan<N>::type{});
 }
+// Same with an explicit radix plan (a RadixList whose product is N).
+template <int N, int NSEQ, int T, int DIR, class Plan>
+__device__ __forceinline__ float2* block_fft_pp_plan(float2* a, float2* b, const float2* __restrict__ tw) {
+  return fft_pp_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, Plan{});
+}
 
 // ---------------------------------------------------------------------------
 // Ping-pong FFT with hooks: the first pass reads its inputs through `ld`

@@ -6,7 +6,10 @@
 // (axis 2), or 8 adjacent z at one x (axis 1) or one y (axis 0).  Only the
 // index range [in_lo, in_lo + in_n) is loaded (the rest is zero: the
 // zero-extension of a padded volume costs no memory traffic) and only
-// [out_lo, out_lo + out_n) is stored.
+// [out_lo, out_lo + out_n) is stored.  Loads and stores run as separate
+// loops over all 256 threads around the shared-memory FFT: these passes are
+// bound by global-memory latency, and spreading each sequence group's loads
+// over every thread keeps the most of them in flight.
 //
 // Prologues:  complex buffer | real volume in a box (zero outside) |
 //             spectrum product Y .* C | real volume masked by two keep-bit sets
@@ -35,6 +38,19 @@ __device__ __forceinline__ void pass_coords(int axis, int a, int b, int i, int& 
   }
 }
 }  // namespace
+
+// Radix plans of the volume passes: radix <= 8, so that with 8 sequences a
+// pass keeps most of the CTA's 256 threads busy (a radix-16 pass of a
+// 144-point sequence would have 72 butterflies).
+template <int N>
+struct FftPlan3 {
+  using type = typename FftPlan<N>::type;
+};
+template <> struct FftPlan3<16> { using type = RadixList<4, 4>; };
+template <> struct FftPlan3<48> { using type = RadixList<3, 4, 4>; };
+template <> struct FftPlan3<128> { using type = RadixList<8, 4, 4>; };
+template <> struct FftPlan3<144> { using type = RadixList<3, 3, 4, 4>; };
+template <> struct FftPlan3<256> { using type = RadixList<4, 8, 8>; };
 
 template <int N, int DIR, int LD, int ST>
 __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, const float2* __restrict__ in,
@@ -65,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
       if (LD == V3_LD_CPLX) {
         v = in[wbase + g];
       } else if (LD == V3_LD_PAIR) {
-        v = cmul(in[wbase + g], P.spec[g]);
+        v = cmul(in[wbase + g], __ldg(&P.spec[g]));
       } else {
         int x, y, z;
         pass_coords(P.axis, a, b0 + s, i, x, y, z);
@@ -84,7 +100,7 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
     A[i * kSeq + s] = v;
   }
   __syncthreads();
-  float2* X = block_fft_pp<N, kSeq, kThreads, DIR>(A, Bf, tw);
+  float2* X = block_fft_pp_plan<N, kSeq, kThreads, DIR, typename FftPlan3<N>::type>(A, Bf, tw);
 
   float ta = -1.f, tb = -1.f;
   if (ST == V3_ST_THRESH && P.th) {
@@ -100,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
       if (st) out[wbase + g] = v;
     } else if (ST == V3_ST_SPEC) {
       if (st) {
-        const float2 c = P.spec[g];
+        const float2 c = __ldg(&P.spec[g]);
         const float2 prod = make_float2(c.x * v.x + c.y * v.y, c.x * v.y - c.y * v.x);  // conj(c) * v
         float2 o = prod;
         if (!P.first) {
