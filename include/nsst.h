@@ -215,6 +215,19 @@ nsst_status nsst_denoise_tau_backward(nsst_plan* plan, const float* const* x, co
                                       float* const* grad_x, int n, const float* tau, float* grad_tau,
                                       int accumulate_tau, int mode, void* stream);
 
+/* Same as nsst_denoise_tau_backward for the n images of the most recent
+ * nsst_denoise_tau_batch on this plan, without recomputing their band
+ * coefficients: once nsst_plan_enable_grad has been called, that forward
+ * keeps its pre-threshold band spectra and pyramid lowpass in the plan (the
+ * thresholded bands go to a separate buffer).  Any other execute call on the
+ * plan drops them; nsst_plan_saved_items tells how many images are held (0 =
+ * none), and this call fails with NSST_ERR_INVALID_ARG unless it is n.  The
+ * caller is responsible for x being unchanged since that forward. */
+nsst_status nsst_denoise_tau_backward_saved(nsst_plan* plan, const float* const* grad_out, float* const* grad_x,
+                                            int n, const float* tau, float* grad_tau, int accumulate_tau, int mode,
+                                            void* stream);
+int nsst_plan_saved_items(const nsst_plan* plan);
+
 /* Store per-band noise scalars in the plan (nbands doubles). */
 nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
 

@@ -4,8 +4,10 @@ loss = f(NSST^-1(T(NSST(x), tau))) with per-band thresholds tau (one per
 band, shared by the images of a batch).  Forward and backward both run in
 libnsst.so (nsst_denoise_tau_batch / nsst_denoise_tau_backward); PyTorch only
 routes gradients.  Batches larger than the plan's capacity are processed in
-chunks; the band coefficients are recomputed in the backward pass, never
-stored, so memory does not grow with the batch.
+chunks.  When the whole batch fits the plan and nothing else ran on the plan
+since the forward, the backward reuses the band coefficients the forward left
+in the plan (nsst_denoise_tau_backward_saved); otherwise it recomputes them
+chunk by chunk, so memory does not grow with the batch.
 """
 import ctypes
 
@@ -46,8 +48,10 @@ class NsstDenoiseFn(torch.autograd.Function):
             n = xs.shape[0]
             check(lib().nsst_denoise_tau_batch(plan.handle, _ptrs(xs, n), _ptrs(os_, n), n,
                                                ctypes.c_void_p(tau.data_ptr()), mode, st))
+        plan._diff_token = getattr(plan, '_diff_token', 0) + 1
         ctx.save_for_backward(x, tau)
-        ctx.plan, ctx.mode = plan, mode
+        ctx.plan, ctx.mode, ctx.token = plan, mode, plan._diff_token
+        ctx.single = x.shape[0] <= plan.batch
         return out
 
     @staticmethod
@@ -58,6 +62,13 @@ class NsstDenoiseFn(torch.autograd.Function):
         gx = torch.empty_like(x)
         gtau = torch.zeros_like(tau)
         st = _stream()
+        n = x.shape[0]
+        if (ctx.single and ctx.token == getattr(plan, '_diff_token', -1)
+                and lib().nsst_plan_saved_items(plan.handle) == n):
+            check(lib().nsst_denoise_tau_backward_saved(plan.handle, _ptrs(grad_out, n), _ptrs(gx, n), n,
+                                                        ctypes.c_void_p(tau.data_ptr()),
+                                                        ctypes.c_void_p(gtau.data_ptr()), 0, mode, st))
+            return gx, gtau, None, None
         for k, c0 in enumerate(range(0, x.shape[0], plan.batch)):
             xs, gs, gxs = x[c0:c0 + plan.batch], grad_out[c0:c0 + plan.batch], gx[c0:c0 + plan.batch]
             n = xs.shape[0]

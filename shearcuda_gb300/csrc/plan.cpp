@@ -107,6 +107,12 @@ struct nsst_plan {
   RowJob* gj_rows_lev_fwd = nullptr;   // gyp[1..] -> lev2
   ColJob* gj_cols_lev = nullptr;       // lev2 in place
   ColJob* gj_analysis = nullptr;       // lev2 -> band2
+  // differentiable forward: thresholded bands go to bandT so that band keeps
+  // the coefficients the backward needs (valid for saved_n items)
+  float2* bandT = nullptr;
+  RowJob* gj_rows_T = nullptr;         // band -> bandT, threshold
+  ColJob* gj_synth_T = nullptr;        // bandT -> sum
+  int saved_n = 0;
   RowJob* gj_rows_backward = nullptr;  // band (plan arena) + band2 -> band2
   ColJob* gj_synthesis = nullptr;      // band2 -> sum2
   RowJob* gj_rows_lev_inv = nullptr;   // sum2 -> gy[1..]
@@ -610,8 +616,11 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 }
 
 // The fused batched pipeline (no host work, no allocation): capturable.
+// keep: the differentiable forward writes the thresholded bands to bandT,
+// leaving the pre-threshold band spectra (and the pyramid's lowpass) for
+// nsst_denoise_tau_backward_saved.
 nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* const* out, int mode, bool lowpass_th,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool keep = false) {
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
@@ -625,11 +634,19 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   timer_mark(p, "fft_cols_fwd", st);
   NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
   timer_mark(p, "band_analysis_cols", st);
-  NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, p->th,
-                        mode, st));
-  timer_mark(p, "band_rows_threshold", st);
-  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
-                        p->twH, st));
+  if (keep) {
+    NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW,
+                          p->th, mode, st));
+    timer_mark(p, "band_rows_threshold", st);
+    NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
+                          (size_t)H * p->WH, p->twH, st));
+  } else {
+    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, p->th,
+                          mode, st));
+    timer_mark(p, "band_rows_threshold", st);
+    NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
+                          p->twH, st));
+  }
   timer_mark(p, "band_synthesis_cols", st);
   NSST_CUDA(launch_rows(RowOp::Inv, p->j_rows_lev_inv, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
   timer_mark(p, "fft_rows_inv", st);
@@ -658,6 +675,7 @@ extern "C" {
 nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   float* yb = y;
@@ -667,6 +685,7 @@ nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream)
 nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   return run_atrousrec(p, 1, &y, nullptr, &x, st);
@@ -676,6 +695,7 @@ nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* 
   if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   char* A = p->arena;
@@ -711,6 +731,7 @@ nsst_status nsst_inverse_shear(nsst_plan* p, const float* coeffs, float* x, void
   if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   char* A = p->arena;
@@ -736,6 +757,7 @@ nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const
   for (int i = 0; i < n; i++)
     if (!x[i] || !out[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   float lmax = 0.f;
   NSST_TRY(upload_thresholds(p, n, sigma, K, scalars, st, &lmax));
@@ -999,6 +1021,8 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   size_t o_j1 = take(sizeof(RowJob) * nL), o_j2 = take(sizeof(ColJob) * nL), o_j3 = take(sizeof(ColJob) * nD);
   size_t o_j4 = take(sizeof(RowJob) * nD), o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
   size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
+  size_t o_bandT = take(sizeof(float2) * NB * p->ndir_total * HWh);
+  size_t o_jT = take(sizeof(RowJob) * nD), o_jS = take(sizeof(ColJob) * nL);
   cudaError_t ce = dev_alloc((void**)&p->garena, off);
   if (ce != cudaSuccess) {
     p->garena = nullptr;
@@ -1022,6 +1046,9 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   p->gj_rows_lev_inv = (RowJob*)(G + o_j6);
   p->gj_coeff_fwd = (RowJob*)(G + o_j7);
   p->gj_band_to_coeff = (RowJob*)(G + o_j8);
+  p->bandT = (float2*)(G + o_bandT);
+  p->gj_rows_T = (RowJob*)(G + o_jT);
+  p->gj_synth_T = (ColJob*)(G + o_jS);
   auto g2 = [&](const void* ptr) { return (size_t)((const char*)ptr - G) / sizeof(float2); };
   auto a2 = [&](const void* ptr) { return (size_t)((const char*)ptr - p->arena) / sizeof(float2); };
   std::vector<RowJob> j1, j4, j6, j7, j8;
@@ -1056,6 +1083,26 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
     j7.push_back(RowJob{(size_t)(1 + b) * HWh, band20 + (size_t)b * HWh, 1 + b, 0});
     j8.push_back(RowJob{band20 + (size_t)b * HWh, (size_t)(1 + b) * HWh, 1 + b, 0});
   }
+  // forward jobs of the differentiable path: the forward's own job order,
+  // threshold output to bandT, synthesis reading bandT
+  std::vector<RowJob> jT(nD);
+  std::vector<ColJob> jS(nL);
+  {
+    std::vector<RowJob> fr(nD);
+    std::vector<ColJob> fs(nL);
+    ce = cudaMemcpy(fr.data(), p->j_rows_bands, nD * sizeof(RowJob), cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(fs.data(), p->j_synthesis, nL * sizeof(ColJob), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return cuda_fail(ce, "read forward job lists");
+    const size_t bandA = a2(p->band), bandT = g2(p->bandT);
+    for (size_t k = 0; k < nD; k++) {
+      jT[k] = fr[k];
+      jT[k].dst = fr[k].dst - bandA + bandT;  // same item and band offset inside bandT
+    }
+    for (size_t k = 0; k < nL; k++) {
+      jS[k] = fs[k];
+      jS[k].src = fs[k].src - bandA + bandT;
+    }
+  }
   auto up = [&](void* dst, const void* src, size_t bytes) { return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice); };
   ce = up(p->gj_rows_lev_fwd, j1.data(), j1.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_cols_lev, j2.data(), j2.size() * sizeof(ColJob));
@@ -1065,6 +1112,8 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   if (ce == cudaSuccess) ce = up(p->gj_rows_lev_inv, j6.data(), j6.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_coeff_fwd, j7.data(), j7.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_rows_T, jT.data(), jT.size() * sizeof(RowJob));
+  if (ce == cudaSuccess) ce = up(p->gj_synth_T, jS.data(), jS.size() * sizeof(ColJob));
   if (ce != cudaSuccess) return cuda_fail(ce, "upload gradient job lists");
   for (int F : {p->pf.F[0], p->pf.F[1], p->pf.F[2], p->pf.F[3]}) {
     ce = prepare_atrous_kernels(F, 0, Mmax);
@@ -1079,6 +1128,7 @@ nsst_status nsst_shear_trans_adjoint(nsst_plan* p, const float* coeffs, float* x
   if (!p || !coeffs || !x) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   NSST_TRY(need_grad(p));
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   char* G = p->garena;
@@ -1102,6 +1152,7 @@ nsst_status nsst_inverse_shear_adjoint(nsst_plan* p, const float* x, float* coef
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   NSST_TRY(need_grad(p));
   std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   char* G = p->garena;
@@ -1131,20 +1182,24 @@ nsst_status nsst_denoise_tau_batch(nsst_plan* p, const float* const* x, float* c
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   NSST_CUDA(launch_broadcast_tau(tau, p->th, p->nbands, n, st));
-  return enqueue_denoise(p, n, x, out, mode, true, st);
+  const bool keep = p->garena != nullptr;
+  p->saved_n = 0;
+  NSST_TRY(enqueue_denoise(p, n, x, out, mode, true, st, keep));
+  if (keep) p->saved_n = n;
+  return NSST_OK;
 }
 
-nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const float* const* grad_out,
-                                      float* const* grad_x, int n, const float* tau, float* grad_tau,
-                                      int accumulate_tau, int mode, void* stream) {
-  if (!p || !x || !grad_out || !grad_x || !tau || !grad_tau) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
-  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
-  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
-  NSST_TRY(need_grad(p));
-  for (int i = 0; i < n; i++)
-    if (!x[i] || !grad_out[i] || !grad_x[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
-  std::lock_guard<std::mutex> lk(p->mu);
-  cudaStream_t st = (cudaStream_t)stream;
+int nsst_plan_saved_items(const nsst_plan* p) { return p ? p->saved_n : 0; }
+
+}  // extern "C"
+
+namespace {
+
+// The backward of nsst_denoise_tau_batch; x == NULL: the band spectra and the
+// pyramid's lowpass of the last differentiable forward are still in the
+// arena (saved_n == n), so step 1 is skipped.  Called with the plan locked.
+nsst_status tau_backward(nsst_plan* p, const float* const* x, const float* const* grad_out, float* const* grad_x,
+                         int n, const float* tau, float* grad_tau, int accumulate_tau, int mode, cudaStream_t st) {
   timer_begin(p, st);
   char* A = p->arena;
   float2* A2 = (float2*)A;
@@ -1159,11 +1214,15 @@ nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const
     gyp[i] = p->gyp + i * (p->nlev + 1) * HW;
     gy[i] = p->gy + i * (p->nlev + 1) * HW;
   }
-  NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
-  timer_mark(p, "recompute_coefficients", st);
+  if (x) {
+    NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
+    NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0,
+                          st));
+    NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+    NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH,
+                          st));
+    timer_mark(p, "recompute_coefficients", st);
+  }
   // 2. d loss / d thresholded coefficients = D P_s^T grad_out
   NSST_TRY(run_atrousrec_adjoint(p, n, grad_out, gyp.data(), st));
   NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_rows_lev_fwd, B * p->nlev, n, H, W, G, G, p->twWh, p->twW, nullptr, 0, st));
@@ -1192,6 +1251,43 @@ nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const
   NSST_CUDA(launch_reduce_tau(p->partials, n * p->ntiles, pstride, p->nbands, grad_tau, accumulate_tau != 0, st));
   timer_mark(p, "reduce_tau", st);
   return NSST_OK;
+}
+
+nsst_status tau_backward_check(nsst_plan* p, const float* const* grad_out, float* const* grad_x, int n,
+                               const float* tau, float* grad_tau, int mode) {
+  if (!p || !grad_out || !grad_x || !tau || !grad_tau) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
+  NSST_TRY(need_grad(p));
+  for (int i = 0; i < n; i++)
+    if (!grad_out[i] || !grad_x[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  return NSST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const float* const* grad_out,
+                                      float* const* grad_x, int n, const float* tau, float* grad_tau,
+                                      int accumulate_tau, int mode, void* stream) {
+  NSST_TRY(tau_backward_check(p, grad_out, grad_x, n, tau, grad_tau, mode));
+  if (!x) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  for (int i = 0; i < n; i++)
+    if (!x[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;  // step 1 rewrites the arena's band spectra
+  return tau_backward(p, x, grad_out, grad_x, n, tau, grad_tau, accumulate_tau, mode, (cudaStream_t)stream);
+}
+
+nsst_status nsst_denoise_tau_backward_saved(nsst_plan* p, const float* const* grad_out, float* const* grad_x, int n,
+                                            const float* tau, float* grad_tau, int accumulate_tau, int mode,
+                                            void* stream) {
+  NSST_TRY(tau_backward_check(p, grad_out, grad_x, n, tau, grad_tau, mode));
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->saved_n != n)
+    return fail(NSST_ERR_INVALID_ARG, "no saved coefficients of n items: the plan ran another call since the forward");
+  return tau_backward(p, nullptr, grad_out, grad_x, n, tau, grad_tau, accumulate_tau, mode, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -1273,6 +1369,7 @@ nsst_status nsst_multi_denoise(nsst_multi* m, const nsst_item* items, int n, con
     if (!groups[g].empty() && !m->plans[g]->has_scalars)
       return fail(NSST_ERR_INVALID_ARG, "plan without stored scalars");
   }
+  for (nsst_plan* q : m->plans) q->saved_n = 0;  // the replay rewrites the plans' arenas
   // thresholds into every plan's pinned staging; the previous replay must be done with them
   NSST_CUDA(cudaEventSynchronize(m->finished));
   std::vector<char> lowth(np, 0);

@@ -179,3 +179,44 @@ def test_learnable_thresholds_reduce_the_loss(built_lib, cuda):
         opt.step()
         losses.append(float(loss))
     assert losses[-1] < losses[0]
+
+
+def test_saved_coefficients_backward_matches_recompute(built_lib, cuda):
+    # the backward that reuses the forward's band spectra gives the same
+    # gradients, bit for bit, as the one that recomputes them; any other
+    # call on the plan drops the saved spectra
+    import ctypes
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300._lib import NsstError, THRESH_SOFT, check, lib
+    from shearcuda_gb300.autograd import _ptrs
+    plan, sf, scal = _setup()
+    rng = np.random.default_rng(11)
+    x = torch.tensor(rng.standard_normal((2, 256, 256)) * 30 + 100, dtype=torch.float32, device=cuda)
+    tau = torch.tensor(flat_scalars(_tau_lists(scal)), dtype=torch.float32, device=cuda)
+    xg = x.clone().requires_grad_(True)
+    tg = tau.clone().requires_grad_(True)
+    out = sc.nsst_denoise_diff(xg, tg, plan, THRESH_SOFT)
+    assert lib().nsst_plan_saved_items(plan.handle) == 2
+    gy = torch.randn_like(out)
+    out.backward(gy)
+    torch.cuda.synchronize()
+    gx_r, gt_r = torch.empty_like(x), torch.zeros_like(tau)
+    check(lib().nsst_denoise_tau_backward(plan.handle, _ptrs(x, 2), _ptrs(gy, 2), _ptrs(gx_r, 2), 2,
+                                          ctypes.c_void_p(tau.data_ptr()), ctypes.c_void_p(gt_r.data_ptr()), 0,
+                                          THRESH_SOFT, None))
+    torch.cuda.synchronize()
+    assert torch.equal(xg.grad, gx_r)
+    assert torch.equal(tg.grad, gt_r)
+    # the recomputing backward rewrote the arena: nothing is saved any more
+    assert lib().nsst_plan_saved_items(plan.handle) == 0
+    with pytest.raises(NsstError):
+        check(lib().nsst_denoise_tau_backward_saved(plan.handle, _ptrs(gy, 2), _ptrs(gx_r, 2), 2,
+                                                    ctypes.c_void_p(tau.data_ptr()), ctypes.c_void_p(gt_r.data_ptr()),
+                                                    0, THRESH_SOFT, None))
+    # a forward, then another call on the plan: the autograd backward falls back to recomputing
+    xg2 = x.clone().requires_grad_(True)
+    out2 = sc.nsst_denoise_diff(xg2, tau, plan, THRESH_SOFT)
+    sc.shear_trans_cuda(x[0], 'maxflat', plan)
+    assert lib().nsst_plan_saved_items(plan.handle) == 0
+    out2.backward(gy)
+    assert torch.equal(xg2.grad, gx_r)
