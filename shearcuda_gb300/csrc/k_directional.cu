@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
                                                                   float* __restrict__ partials, size_t pstride) {
   using C = RowCfg<WH>;
   extern __shared__ float2 smem[];
-  float2 *A = smem, *B = smem + (size_t)WH * C::LD, *Cb = smem + 2 * (size_t)WH * C::LD,
-         *D = smem + 3 * (size_t)WH * C::LD;
+  float2 *A = smem, *B = smem + (size_t)WH * C::LD, *Cb = smem + 2 * (size_t)WH * C::LD;
   __shared__ float red[32];
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
@@ -240,24 +239,24 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   load_rows<WH, C::RS, C::LD, C::T>(Cb, dst_base + job.dst + off);
   __syncthreads();
-  c2r_pre_pp<WH, C::RS, C::LD, C::T>(A, B, twW);
-  c2r_pre_pp<WH, C::RS, C::LD, C::T>(Cb, D, twW);
-  float2* Xc = block_fft_pp<WH, C::RS, C::T, +1>(B, A, twWh);
-  float2* Xg = block_fft_pp<WH, C::RS, C::T, +1>(D, Cb, twWh);
+  // coefficients c = C2R(Qc) (pre-processing in the first pass)
+  float2* const Xc = fft_hook_target<WH>(A, B);
+  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW}, SmemSt<C::RS>{Xc});
+  // gradient g = C2R(Qg), masked by 1[|c| > t] in the last pass, which also
+  // accumulates this thread's share of -sum g sign(c) 1[|c| > t] (soft)
+  float2* const S = (Xc == A) ? B : A;
+  float2* const Xg = fft_hook_target<WH>(Cb, S);
   float part = 0.0f;
-  for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
-    const int i = e / C::RS, s = e % C::RS;
-    const float2 c = Xc[i * C::LD + s];
-    float2 g = Xg[i * C::LD + s];
+  auto mask_st = [&](int i, int sq, float2 g) {
+    const float2 c = Xc[i * C::RS + sq];
     const bool kx = fabsf(c.x) > th, ky = fabsf(c.y) > th;
     if (mode == THRESH_SOFT) {
-      if (kx) part -= (c.x > 0.0f ? g.x : -g.x);  // -g sign(c)
+      if (kx) part -= (c.x > 0.0f ? g.x : -g.x);
       if (ky) part -= (c.y > 0.0f ? g.y : -g.y);
     }
-    g.x = kx ? g.x : 0.0f;
-    g.y = ky ? g.y : 0.0f;
-    Xg[i * C::LD + s] = g;
-  }
+    Xg[i * C::RS + sq] = make_float2(kx ? g.x : 0.0f, ky ? g.y : 0.0f);
+  };
+  block_fft_hook<WH, C::RS, C::T, +1>(Cb, S, twWh, C2RPreLd<WH, C::RS>{Cb, twW}, mask_st);
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
   __syncthreads();
@@ -267,11 +266,11 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
     if (threadIdx.x == 0)
       partials[(size_t)job.th_index * pstride + (size_t)job.item * gridDim.x + blockIdx.x] = v;
   }
-  float2* Y = (Xg == Cb) ? D : Cb;
-  float2* Z = block_fft_pp<WH, C::RS, C::T, -1>(Xg, Y, twWh);
-  float2* O = (Z == Cb) ? D : Cb;
-  r2c_post_pp<WH, C::RS, C::LD, C::T>(Z, O, twW);
-  store_rows<WH, C::RS, C::LD, C::T>(dst_base + job.dst + off, O);
+  // R2C of the masked gradient; post-processing fused with the store
+  float2* const Y = (Xg == Cb) ? S : Cb;
+  float2* const Z = fft_hook_target<WH>(Xg, Y);
+  block_fft_hook<WH, C::RS, C::T, -1>(Xg, Y, twWh, SmemLd<C::RS>{Xg}, SmemSt<C::RS>{Z});
+  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
 }
 
 // ---------------------------------------------------------------------------
@@ -440,7 +439,7 @@ cudaError_t prepare_row_kernels(int wh) {
     cudaError_t e = opt_in(k_rows_fwd<n>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
-    if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 2 * sm);             \
+    if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * sm / 2);         \
     return e;                                                                 \
   }
     NSST_ROW_SIZES(CASE)
@@ -507,7 +506,7 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
   switch (WH) {
 #define CASE(n)                                                                                      \
   case n: {                                                                                          \
-    constexpr size_t sm = 2 * RowCfg<n>::smem();                                                     \
+    constexpr size_t sm = 3 * RowCfg<n>::smem() / 2;                                                 \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                                             \
     k_rows_backward<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, tau, mode, \
                                                       partials, pstride);                           \
