@@ -53,16 +53,23 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
   constexpr int TR = kAtRows + F - 1;
   const int TC = kAtTX + M * (F - 1);
   const int tid = threadIdx.x;
-  for (int e = tid; e < TR * TC; e += kAtThreads) {
-    int tr = e / TC, tc = e - tr * TC;
-    int r = phase + M * (prow0 + tr - C0);
-    int c = col0 - M * C0 + tc;
+  // halo tile: one warp per tile row at a time (the row's source index and
+  // mirror are computed once), lanes across the row
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int tr = warp; tr < TR; tr += kAtThreads / 32) {
+    const int r = phase + M * (prow0 + tr - C0);
+    float* trow = tile + tr * TC;
+    const int cbase = col0 - M * C0;
     if (ZERO) {
-      tile[e] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(&x[(size_t)r * W + c]) : 0.0f;
+      const bool rin = r >= 0 && r < H;
+      const float* src = x + (size_t)(rin ? r : 0) * W;
+      for (int tc = lane; tc < TC; tc += 32) {
+        const int c = cbase + tc;
+        trow[tc] = (rin && c >= 0 && c < W) ? __ldg(&src[c]) : 0.0f;
+      }
     } else {
-      r = mirror_index(r, H);
-      c = mirror_index(c, W);
-      tile[e] = __ldg(&x[(size_t)r * W + c]);
+      const float* src = x + (size_t)mirror_index(r, H) * W;
+      for (int tc = lane; tc < TC; tc += 32) trow[tc] = __ldg(&src[mirror_index(cbase + tc, W)]);
     }
   }
   __syncthreads();
