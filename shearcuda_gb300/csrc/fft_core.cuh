@@ -495,6 +495,81 @@ __device__ __forceinline__ void block_fft_hook(float2* a, float2* b, const float
   fft_hook_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, ld, st, typename FftPlan<N>::type{});
 }
 
+// In-place variant of block_fft_hook on one buffer: every pass loads all of
+// the thread's butterflies into registers, synchronises, then writes them
+// back (two barriers per pass, half the shared memory of the ping-pong form,
+// so more CTAs fit on an SM).  `st` of the last pass may write `buf`.
+template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT, class Rd, class Wr>
+__device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const float2* __restrict__ tw) {
+  constexpr int NB = N / R;
+  constexpr int TOTAL = NB * NSEQ;
+  constexpr int IPT = (TOTAL + T - 1) / T;
+  constexpr int STEP = N / (NS * R);
+  float2 v[IPT][R];
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      const int s = w % NSEQ, j = w / NSEQ;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[it][r] = rd(swz_row<NSEQ, SWZ_IN>(j + r * NB), s);
+      const int k = j % NS;
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+          const float2 t = __ldg(&tw[r * k * STEP]);
+          v[it][r] = DIR < 0 ? cmul(v[it][r], t) : cmulc(v[it][r], t);
+        }
+      }
+      Dft<R, DIR>::run(v[it]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      const int s = w % NSEQ, j = w / NSEQ, k = j % NS;
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) wr(swz_row<NSEQ, SWZ_OUT>(base + r * NS), s, v[it][r]);
+    }
+  }
+  __syncthreads();
+}
+
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St>
+__device__ __forceinline__ void fft_hook_ip_passes(float2*, const float2* __restrict__, const Ld&, const St&,
+                                                   RadixList<>) {}
+
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, int R, int... Rest>
+__device__ __forceinline__ void fft_hook_ip_passes(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                   const St& st, RadixList<R, Rest...>) {
+  constexpr bool first = NS == 1;
+  constexpr bool last = sizeof...(Rest) == 0;
+  constexpr int SWZ_OUT = (first && !last && R % 2 == 0) ? R : 0;
+  auto rd = [&](int row, int s) -> float2 {
+    if constexpr (first)
+      return ld(row, s);
+    else
+      return buf[row * NSEQ + s];
+  };
+  auto wr = [&](int row, int s, float2 v) {
+    if constexpr (last)
+      st(row, s, v);
+    else
+      buf[row * NSEQ + s] = v;
+  };
+  stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+  fft_hook_ip_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, st, RadixList<Rest...>{});
+}
+
+template <int N, int NSEQ, int T, int DIR, class Ld, class St>
+__device__ __forceinline__ void block_fft_hook_ip(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                  const St& st) {
+  fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, typename FftPlan<N>::type{});
+}
+
 // Out-of-place packed-real post-processing (after a forward FFT of the
 // W/2-point complex view); see r2c_post for the formulas.
 template <int WH, int NSEQ, int LD, int T>

@@ -44,6 +44,7 @@ struct ColCfg {  // N = H points per column
   static constexpr int CS = N >= 1024 ? 4 : 8;
   static constexpr int T = N >= 2048 ? 512 : 256;
   static constexpr int LD = CS;
+  static constexpr int MINB = 1024 / T;  // in-place column passes: 4 CTAs of 256 threads per SM
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 
@@ -312,7 +313,7 @@ struct AnalysisLd {
 // plain column FFT (forward or inverse) src -> dst, straight from and to
 // global memory through the first and last passes
 template <int H, int DIR>
-__global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH,
+__global__ void __launch_bounds__(ColCfg<H>::T, ColCfg<H>::MINB) k_cols(const ColJob* __restrict__ jobs, int n_active, int WH,
                                                         const float2* src_base, float2* dst_base,
                                                         const float2* __restrict__ twH) {
   using C = ColCfg<H>;
@@ -321,13 +322,14 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_cols(const ColJob* __restrict_
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
-  block_fft_hook<H, C::CS, C::T, DIR>(A, B, twH, ColGlobalLd{src_base + job.src + col0, WH},
-                                      ColGlobalSt{dst_base + job.dst + col0, WH});
+  (void)B;
+  block_fft_hook_ip<H, C::CS, C::T, DIR>(A, twH, ColGlobalLd{src_base + job.src + col0, WH},
+                                         ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
 // analysis band: dst = colIFFT( Wk .* src ), src = fully transformed level spectrum
 template <int H>
-__global__ void __launch_bounds__(ColCfg<H>::T) k_band_analysis(const ColJob* __restrict__ jobs, int n_active,
+__global__ void __launch_bounds__(ColCfg<H>::T, ColCfg<H>::MINB) k_band_analysis(const ColJob* __restrict__ jobs, int n_active,
                                                                  int WH, const float2* src_base, float2* dst_base,
                                                                  const float2* __restrict__ spec_base,
                                                                  const float2* __restrict__ twH) {
@@ -337,8 +339,9 @@ __global__ void __launch_bounds__(ColCfg<H>::T) k_band_analysis(const ColJob* __
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
-  block_fft_hook<H, C::CS, C::T, +1>(
-      A, B, twH,
+  (void)B;
+  block_fft_hook_ip<H, C::CS, C::T, +1>(
+      A, twH,
       AnalysisLd<H>{src_base + job.src + col0, spec_base + job.spec + col0, spec_base + job.m0, WH, col0 == 0},
       ColGlobalSt{dst_base + job.dst + col0, WH});
 }
@@ -530,12 +533,13 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
   case n: {                                                                                           \
     constexpr size_t sm = ColCfg<n>::smem();                                                          \
     dim3 grid(WH / ColCfg<n>::CS, njobs);                                                             \
-    if (op == ColOp::Fwd)                                                                             \
-      k_cols<n, -1><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                   \
+    if (op == ColOp::Fwd)  /* in-place transforms: one buffer */                                     \
+      k_cols<n, -1><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, twH);               \
     else if (op == ColOp::Inv)                                                                        \
-      k_cols<n, 1><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                    \
+      k_cols<n, 1><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, twH);                \
     else if (op == ColOp::Analysis)                                                                   \
-      k_band_analysis<n><<<grid, ColCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base, twH);   \
+      k_band_analysis<n><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,     \
+                                                         twH);                                        \
     else                                                                                              \
       k_band_synthesis<n><<<grid, SynCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,        \
                                                       band_stride, twH);                              \
