@@ -52,6 +52,8 @@ struct ColCfg {  // N = H points per column
 // CTA keep that share at 8 complex values per thread.
 template <int N>
 struct SynCfg : ColCfg<N> {
+  // two column buffers (transform, running sum) and the DC column
+  static constexpr size_t smem() { return (2 * (size_t)N * ColCfg<N>::LD + N) * sizeof(float2); }
   static constexpr int T = N >= 2048 ? 1024 : ((N * ColCfg<N>::CS) % 512 == 0 ? 512 : 256);
   static constexpr int MINB = 1024 / T;
 };
@@ -348,7 +350,12 @@ __global__ void __launch_bounds__(ColCfg<H>::T, ColCfg<H>::MINB) k_band_analysis
 
 // synthesis: dst = colIFFT( sum_k conj(Wk) .* colFFT(src_k) ) over job.nbands
 // bands stored at src + k * band_stride, spectra at spec + k * band_stride,
-// side arrays at m0 + k * H.  The running sum stays in registers.
+// side arrays at m0 + k * H.  Each band's column FFT runs in place in A; its
+// last pass accumulates conj(Wk) .* X straight into the running sum in S
+// (each output element has one owner thread per pass, and passes are
+// separated by barriers).  The packed DC/Nyquist column also needs X[-u]:
+// the CTA holding column 0 keeps that column in D and adds
+// conj(M[u] X[-u]) after the transform.
 template <int H>
 __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesis(const ColJob* __restrict__ jobs, int n_active,
                                                                   int WH, const float2* src_base, float2* dst_base,
@@ -356,43 +363,32 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
                                                                   size_t band_stride,
                                                                   const float2* __restrict__ twH) {
   using C = SynCfg<H>;
-  constexpr int EPT = H * C::CS / C::T;
-  static_assert(H * C::CS % C::T == 0, "tile must divide evenly");
   extern __shared__ float2 smem[];
-  float2 *A = smem, *B = smem + (size_t)H * C::LD;
+  float2 *A = smem, *S = smem + (size_t)H * C::LD, *D = smem + 2 * (size_t)H * C::LD;
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
-  float2 acc[EPT];
-#pragma unroll
-  for (int it = 0; it < EPT; it++) acc[it] = make_float2(0.f, 0.f);
-  float2* const X = fft_hook_target<H>(A, B);
+  const bool dc = col0 == 0;
   for (int k = 0; k < job.nbands; k++) {
     const float2* src = src_base + job.src + k * band_stride;
-    const float2* spec = spec_base + job.spec + k * band_stride;
-    block_fft_hook<H, C::CS, C::T, -1>(A, B, twH, ColGlobalLd{src + col0, WH}, SmemSt<C::CS>{X});
-#pragma unroll
-    for (int it = 0; it < EPT; it++) {
-      const int e = threadIdx.x + it * C::T;
-      const int i = e / C::CS, s = e % C::CS;
-      const float2 z = X[i * C::LD + s];
-      acc[it] = cadd(acc[it], cmulc(z, __ldg(&spec[(size_t)i * WH + col0 + s])));
-      if (col0 + s == 0) {
-        const float2 zm = X[((H - i) % H) * C::LD];
+    const float2* spec = spec_base + job.spec + k * band_stride + col0;
+    const bool first = k == 0;
+    auto acc_st = [&](int i, int sq, float2 z) {
+      const float2 p = cmulc(z, __ldg(&spec[(size_t)i * WH + sq]));
+      float2* t = &S[i * C::LD + sq];
+      *t = first ? p : cadd(*t, p);
+      if (dc && sq == 0) D[i] = z;
+    };
+    block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, ColGlobalLd{src + col0, WH}, acc_st);
+    if (dc) {
+      for (int i = threadIdx.x; i < H; i += C::T) {
         const float2 m = __ldg(&spec_base[job.m0 + (size_t)k * H + i]);
-        acc[it] = cadd(acc[it], cconj(cmul(m, zm)));  // conj(M) conj(z[-u])
+        S[i * C::LD] = cadd(S[i * C::LD], cconj(cmul(m, D[(H - i) % H])));  // conj(M) conj(z[-u])
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
-#pragma unroll
-  for (int it = 0; it < EPT; it++) {
-    const int e = threadIdx.x + it * C::T;
-    const int i = e / C::CS, s = e % C::CS;
-    A[i * C::LD + s] = acc[it];
-  }
-  __syncthreads();
-  block_fft_hook<H, C::CS, C::T, +1>(A, B, twH, SmemLd<C::CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
+  block_fft_hook_ip<H, C::CS, C::T, +1>(S, twH, SmemLd<C::CS>{S}, ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
 // ---------------------------------------------------------------------------
@@ -460,7 +456,7 @@ cudaError_t prepare_col_kernels(int h) {
     cudaError_t e = opt_in(k_cols<n, -1>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_cols<n, 1>, sm);                       \
     if (e == cudaSuccess) e = opt_in(k_band_analysis<n>, sm);                 \
-    if (e == cudaSuccess) e = opt_in(k_band_synthesis<n>, sm);                \
+    if (e == cudaSuccess) e = opt_in(k_band_synthesis<n>, SynCfg<n>::smem());  \
     return e;                                                                 \
   }
     NSST_COL_SIZES(CASE)
@@ -541,7 +537,8 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
       k_band_analysis<n><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,     \
                                                          twH);                                        \
     else                                                                                              \
-      k_band_synthesis<n><<<grid, SynCfg<n>::T, sm, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,        \
+      k_band_synthesis<n><<<grid, SynCfg<n>::T, SynCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base, dst_base,   \
+                                                                       spec_base,                     \
                                                       band_stride, twH);                              \
     return cudaGetLastError();                                                                        \
   }
