@@ -36,6 +36,7 @@ struct RowCfg {  // N = W/2 complex points per row
   static constexpr int RS = N >= 1024 ? 4 : 8;
   // 256 = 16 x 16: a radix-16 pass has 16 butterflies per row, one per thread
   static constexpr int T = N == 256 ? 128 : 256;
+  static constexpr int MINB = 1024 / T;  // <= 64 registers: at least 32 warps per SM
   static constexpr int LD = RS;
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
@@ -159,7 +160,7 @@ __device__ __forceinline__ void r2c_post_store(float2* __restrict__ dst, const f
 
 // real rows -> packed half-spectrum rows (forward R2C along W)
 template <int WH>
-__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_fwd(const RowJob* __restrict__ jobs, int n_active,
+__global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_fwd(const RowJob* __restrict__ jobs, int n_active,
                                                              const float2* src_base, float2* dst_base,
                                                              const float2* __restrict__ twWh,
                                                              const float2* __restrict__ twW) {
@@ -171,14 +172,14 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_fwd(const RowJob* __rest
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  float2* Z = fft_hook_target<WH>(A, B);
-  block_fft_hook<WH, C::RS, C::T, -1>(A, B, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{Z});
-  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
+  (void)B;
+  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{A});
+  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
 
 // packed rows -> real rows (inverse C2R along W, unnormalised: x W)
 template <int WH>
-__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_inv(const RowJob* __restrict__ jobs, int n_active,
+__global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_inv(const RowJob* __restrict__ jobs, int n_active,
                                                              const float2* src_base, float2* dst_base,
                                                              const float2* __restrict__ twWh,
                                                              const float2* __restrict__ twW) {
@@ -190,13 +191,14 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_inv(const RowJob* __rest
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
-  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW},
-                                      RowGlobalSt<WH>{dst_base + job.dst + off});
+  (void)B;
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW},
+                                         RowGlobalSt<WH>{dst_base + job.dst + off});
 }
 
 // packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
 template <int WH>
-__global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active,
+__global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active,
                                                                 const float2* src_base, float2* dst_base,
                                                                 const float2* __restrict__ twWh,
                                                                 const float2* __restrict__ twW,
@@ -211,13 +213,13 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_thresh(const RowJob* __r
   load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
   __syncthreads();
   // C2R (pre-processing in the first pass) with the threshold in the last pass
-  float2* X = fft_hook_target<WH>(A, B);
-  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW}, ThreshSt<C::RS>{X, th, mode});
+  // (both transforms in place on one buffer: every pass reads all of its
+  // inputs, the pre-processing's mirrored ones included, before a barrier)
+  (void)B;
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW}, ThreshSt<C::RS>{A, th, mode});
   // R2C of the thresholded rows; post-processing fused with the store
-  float2* Y = (X == A) ? B : A;
-  float2* Z = fft_hook_target<WH>(X, Y);
-  block_fft_hook<WH, C::RS, C::T, -1>(X, Y, twWh, SmemLd<C::RS>{X}, SmemSt<C::RS>{Z});
-  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
+  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{A});
+  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
 
 // Backward band row pass (adjoint of the threshold step, rows of one band):
@@ -477,7 +479,7 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
   switch (WH) {
 #define CASE(n)                                                                        \
   case n: {                                                                            \
-    constexpr size_t sm = RowCfg<n>::smem();                                           \
+    constexpr size_t sm = RowCfg<n>::smem() / 2; /* in place: one buffer */            \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                               \
     if (op == RowOp::Fwd)                                                              \
       k_rows_fwd<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
