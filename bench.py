@@ -38,7 +38,7 @@ UNIT = 'images/s'
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--steps', type=int, default=50)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
@@ -55,6 +55,23 @@ def dist_env():
     world = int(os.environ.get('WORLD_SIZE', '1'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
     return rank, world, local
+
+
+def max_over_ranks(value, device):
+    """The largest of every rank's value (the slowest replica times the job);
+    the value itself on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, seconds):
+    """Whole-job units/s: every replica processes units_per_rank in the job time."""
+    return units_per_rank * world / seconds
 
 
 # --------------------------------------------------------------- CPU baseline
@@ -129,7 +146,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                          '--format=csv,noheader,nounits', '-lms', '50'],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -310,13 +327,9 @@ def run_gpu(args):
     barrier()
     clocks = sampler.stop()
     total_ms = sum(a.elapsed_time(b) for a, b in times)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
-    value = BATCH * world * args.steps / (total_ms / 1000.0)
+    value = job_throughput(BATCH * args.steps, world, total_ms / 1000.0)
 
     # ---- per-stage timing of the same batched pass (eager, events per stage)
     plan.use_graphs(False)
