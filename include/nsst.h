@@ -47,7 +47,8 @@ typedef struct nsst_config {
   int dcomp[NSST_MAX_LEVELS];   /* level i has 2^dcomp[i] directions, coarse -> fine */
   int dsize[NSST_MAX_LEVELS];   /* local support of level i's shearing filter */
   char lpfilt[16];              /* pyramid filter name, NUL-terminated */
-  int pyramid;                  /* NSST_PYRAMID_*: direct dilated conv or DCT-domain */
+  int pyramid;                  /* NSST_PYRAMID_AUTO or _DIRECT: the dilated direct
+                                   convolution; _SPECTRAL is reserved and rejected */
 } nsst_config;
 
 typedef struct nsst_plan nsst_plan;
@@ -68,6 +69,32 @@ nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** o
 /* Like nsst_plan_create, with work buffers for up to B images of this size
  * processed together by nsst_denoise_batch (the filter spectra are shared). */
 nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, nsst_plan** out);
+
+/* The reference's shearing-filter bank file, "SHFM0002" (little-endian): the
+ * magic, uint16 number of scales, uint16 data type (NSST_DATA_SINGLE 0 or
+ * NSST_DATA_DOUBLE 2), per scale uint16 filter size n and uint16 number of
+ * directions d followed by d n x n filters in MATLAB column-major order, then
+ * the four pyramid filters h0, h1, g0, g1 as uint16 size F and F x F values.
+ * nsst_filters_save writes the bank of `cfg` (the Meyer shearing filters of
+ * shearing_filters_Myer.m and the pyramid filters named in cfg->lpfilt);
+ * replaces save_shearing_filters.m:46-84. */
+enum { NSST_DATA_SINGLE = 0, NSST_DATA_DOUBLE = 2 };
+nsst_status nsst_filters_save(const char* path, const nsst_config* cfg, int data_type);
+
+/* Read an SHFM0002 file: nlevels, and per level dsize / ndir (arrays of
+ * NSST_MAX_LEVELS), F[4], the shearing filters (sum_l ndir*dsize^2 doubles,
+ * row-major, level after level) and the pyramid filters (sum_k F[k]^2
+ * doubles, row-major); every output but nlevels may be NULL.  Replaces
+ * ShearConfig::readFromFile (demoImageDenoise/shearconfig.cpp:26-78). */
+nsst_status nsst_filters_load(const char* path, int* nlevels, int* dsize, int* ndir, int* F, double* shear,
+                              double* pyramid, int* data_type);
+
+/* A plan whose shearing filters and pyramid filters come from an SHFM0002
+ * file instead of being constructed (dcomp = log2 of each scale's direction
+ * count, dsize = its filter size; the spectra are normalised as
+ * nsst_dec2.m:47-57 does).  With the library's own bank saved as doubles the
+ * plan is identical to nsst_plan_create_batch's. */
+nsst_status nsst_plan_create_from_file(const char* path, int H, int W, int B, nsst_plan** out);
 
 /* Batch capacity B of a plan. */
 int nsst_plan_batch_capacity(const nsst_plan* plan);

@@ -49,6 +49,9 @@ SIGNATURES = [
     ('nsst_plan_create', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, ctypes.POINTER(_vp)]),
     ('nsst_plan_create_batch', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, _ci, ctypes.POINTER(_vp)]),
     ('nsst_plan_batch_capacity', _ci, [_vp]),
+    ('nsst_filters_save', _ci, [ctypes.c_char_p, ctypes.POINTER(NsstConfig), _ci]),
+    ('nsst_filters_load', _ci, [ctypes.c_char_p, _ip, _ip, _ip, _ip, _dp, _dp, _ip]),
+    ('nsst_plan_create_from_file', _ci, [ctypes.c_char_p, _ci, _ci, _ci, ctypes.POINTER(_vp)]),
     ('nsst_plan_use_graphs', _ci, [_vp, _ci]),
     ('nsst_plan_destroy', _ci, [_vp]),
     ('nsst_plan_num_bands', _ci, [_vp]),

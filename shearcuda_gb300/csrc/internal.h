@@ -198,6 +198,19 @@ struct PyramidFilters {
 // atrousfilters.m tables; returns false for an unknown name.
 bool pyramid_filters(const std::string& name, PyramidFilters* out);
 
+// A complete filter bank as the reference's SHFM0002 file holds it
+// (host_filterfile.cpp): per level the shearing filters, row-major, and the
+// four pyramid filters.
+constexpr int kShfmSingle = 0, kShfmDouble = 2;  // the file's data-type codes
+struct FilterSet {
+  int nlev = 0, dtype = kShfmDouble;
+  int dsize[NSST_MAX_LEVELS] = {}, ndir[NSST_MAX_LEVELS] = {};
+  std::vector<double> shear[NSST_MAX_LEVELS];  // ndir x dsize x dsize each
+  PyramidFilters pf;
+};
+bool read_filter_file(const char* path, FilterSet* fs, std::string* err);
+bool write_filter_file(const char* path, const FilterSet& fs, std::string* err);
+
 // shearing_filters_Myer.m: (2^level) filters of n1 x n1, row-major, FP64.
 std::vector<double> shearing_filters_myer(int n1, int level);
 

@@ -49,6 +49,7 @@ struct nsst_plan {
   int H = 0, W = 0, WH = 0, nlev = 0, nbands = 0, ndir_total = 0, B = 1;
   std::vector<int> ndir, first_band, band_level;  // per level / per band
   PyramidFilters pf;
+  std::vector<std::vector<double>> shear_w;  // FP64 shearing filters per level (ndir x dsize^2, row-major)
   std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1 (forward steps)
   std::vector<float> h32[4];    // FP32 unflipped h0, h1, g0, g1 (adjoint steps)
   int device = 0;
@@ -167,6 +168,8 @@ int host_threads() {
 
 nsst_status validate_config(const nsst_config* cfg, int H, int W) {
   if (!cfg) return fail(NSST_ERR_INVALID_ARG, "config is NULL");
+  if (cfg->pyramid != NSST_PYRAMID_AUTO && cfg->pyramid != NSST_PYRAMID_DIRECT)
+    return fail(NSST_ERR_INVALID_ARG, "only the direct (dilated convolution) pyramid is implemented");
   // the dilated direct convolution stages a (64 + 2^(L-1)(F-1))-wide halo
   // tile in shared memory, which bounds the depth at 6 levels
   if (cfg->nlevels < 1 || cfg->nlevels > 6) return fail(NSST_ERR_INVALID_ARG, "nlevels must be in [1, 6]");
@@ -233,7 +236,13 @@ nsst_status nsst_shearing_filters(int n1, int level, double* out) {
   return NSST_OK;
 }
 
-nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, nsst_plan** out) {
+}  // extern "C"
+
+namespace {
+
+// Plan construction; ext (optional) supplies the filter bank instead of the
+// Meyer construction and the named pyramid filters.
+nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const FilterSet* ext, nsst_plan** out) {
   if (!out) return fail(NSST_ERR_INVALID_ARG, "out is NULL");
   *out = nullptr;
   NSST_TRY(validate_config(cfg, H, W));
@@ -264,7 +273,12 @@ nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, 
   };
 
   const char* fname = p->cfg.lpfilt[0] ? p->cfg.lpfilt : "maxflat";
-  if (!pyramid_filters(fname, &p->pf)) return destroy(fail(NSST_ERR_INVALID_ARG, "unknown pyramid filter"));
+  if (ext)
+    p->pf = ext->pf;
+  else if (!pyramid_filters(fname, &p->pf))
+    return destroy(fail(NSST_ERR_INVALID_ARG, "unknown pyramid filter"));
+  for (int l = 0; l < p->nlev; l++)
+    p->shear_w.push_back(ext ? ext->shear[l] : shearing_filters_myer(cfg->dsize[l], cfg->dcomp[l]));
   if (!atrous_pair_supported(p->pf.F[0], 0) || !atrous_pair_supported(p->pf.F[1], 0) ||
       !atrous_pair_supported(p->pf.F[2], p->pf.F[3]))
     return destroy(fail(NSST_ERR_INVALID_ARG, "pyramid filter sizes not compiled"));
@@ -353,9 +367,8 @@ nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, 
     const int WC = p->WH + 1;
     const double scale = 1.0 / ((double)H * W);
     for (int l = 0; l < p->nlev; l++) {
-      std::vector<double> w = shearing_filters_myer(cfg->dsize[l], cfg->dcomp[l]);
       std::vector<cd> S;
-      if (!level_spectra(w, p->ndir[l], cfg->dsize[l], H, W, &S, host_threads()))
+      if (!level_spectra(p->shear_w[l], p->ndir[l], cfg->dsize[l], H, W, &S, host_threads()))
         return destroy(fail(NSST_ERR_NUMERIC, "shearing filter normalisation divides by zero"));
       for (int k = 0; k < p->ndir[l]; k++) {
         const int b = p->first_band[l] + k;
@@ -450,6 +463,82 @@ nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, 
   return NSST_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_plan_create_batch(const nsst_config* cfg, int H, int W, int B, nsst_plan** out) {
+  return create_plan(cfg, H, W, B, nullptr, out);
+}
+
+nsst_status nsst_plan_create_from_file(const char* path, int H, int W, int B, nsst_plan** out) {
+  if (!out) return fail(NSST_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!path) return fail(NSST_ERR_INVALID_ARG, "path is NULL");
+  FilterSet fs;
+  std::string err;
+  if (!read_filter_file(path, &fs, &err)) return fail(NSST_ERR_INVALID_ARG, err);
+  nsst_config cfg{};
+  cfg.nlevels = fs.nlev;
+  for (int l = 0; l < fs.nlev; l++) {
+    int dc = 0;
+    while ((1 << dc) < fs.ndir[l]) dc++;
+    if ((1 << dc) != fs.ndir[l]) return fail(NSST_ERR_INVALID_ARG, "number of directions must be a power of two");
+    cfg.dcomp[l] = dc;
+    cfg.dsize[l] = fs.dsize[l];
+  }
+  std::strcpy(cfg.lpfilt, "file");
+  cfg.pyramid = NSST_PYRAMID_DIRECT;
+  return create_plan(&cfg, H, W, B, &fs, out);
+}
+
+nsst_status nsst_filters_save(const char* path, const nsst_config* cfg, int data_type) {
+  if (!path || !cfg) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (data_type != kShfmSingle && data_type != kShfmDouble)
+    return fail(NSST_ERR_INVALID_ARG, "data_type must be 0 (single) or 2 (double)");
+  if (cfg->nlevels < 1 || cfg->nlevels > NSST_MAX_LEVELS) return fail(NSST_ERR_INVALID_ARG, "bad nlevels");
+  FilterSet fs;
+  fs.nlev = cfg->nlevels;
+  fs.dtype = data_type;
+  for (int l = 0; l < fs.nlev; l++) {
+    if (cfg->dcomp[l] < 0 || cfg->dcomp[l] > 6 || cfg->dsize[l] < 2 || cfg->dsize[l] > 256)
+      return fail(NSST_ERR_INVALID_ARG, "bad dcomp / dsize");
+    fs.dsize[l] = cfg->dsize[l];
+    fs.ndir[l] = 1 << cfg->dcomp[l];
+    fs.shear[l] = shearing_filters_myer(cfg->dsize[l], cfg->dcomp[l]);
+  }
+  char name[17] = {0};
+  std::memcpy(name, cfg->lpfilt, 16);
+  if (!pyramid_filters(name[0] ? name : "maxflat", &fs.pf)) return fail(NSST_ERR_INVALID_ARG, "unknown pyramid filter");
+  std::string err;
+  if (!write_filter_file(path, fs, &err)) return fail(NSST_ERR_INVALID_ARG, err);
+  return NSST_OK;
+}
+
+nsst_status nsst_filters_load(const char* path, int* nlevels, int* dsize, int* ndir, int* F, double* shear,
+                              double* pyr, int* data_type) {
+  if (!path || !nlevels) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  FilterSet fs;
+  std::string err;
+  if (!read_filter_file(path, &fs, &err)) return fail(NSST_ERR_INVALID_ARG, err);
+  *nlevels = fs.nlev;
+  if (data_type) *data_type = fs.dtype;
+  size_t at = 0;
+  for (int l = 0; l < fs.nlev; l++) {
+    if (dsize) dsize[l] = fs.dsize[l];
+    if (ndir) ndir[l] = fs.ndir[l];
+    if (shear) std::memcpy(shear + at, fs.shear[l].data(), fs.shear[l].size() * sizeof(double));
+    at += fs.shear[l].size();
+  }
+  at = 0;
+  for (int k = 0; k < 4; k++) {
+    if (F) F[k] = fs.pf.F[k];
+    if (pyr) std::memcpy(pyr + at, fs.pf.h[k].data(), fs.pf.h[k].size() * sizeof(double));
+    at += fs.pf.h[k].size();
+  }
+  return NSST_OK;
+}
+
 nsst_status nsst_plan_create(const nsst_config* cfg, int H, int W, nsst_plan** out) {
   return nsst_plan_create_batch(cfg, H, W, 1, out);
 }
@@ -493,7 +582,11 @@ nsst_status nsst_level_spectra(int dsize, int dcomp, int H, int W, double* out) 
 
 nsst_status nsst_plan_level_spectra(const nsst_plan* p, int level, double* out) {
   if (!p || !out || level < 0 || level >= p->nlev) return fail(NSST_ERR_INVALID_ARG, "bad arguments");
-  return nsst_level_spectra(p->cfg.dsize[level], p->cfg.dcomp[level], p->H, p->W, out);
+  std::vector<cd> S;
+  if (!level_spectra(p->shear_w[level], p->ndir[level], p->cfg.dsize[level], p->H, p->W, &S, host_threads()))
+    return fail(NSST_ERR_NUMERIC, "shearing filter normalisation divides by zero");
+  std::memcpy(out, S.data(), S.size() * sizeof(cd));
+  return NSST_OK;
 }
 
 nsst_status nsst_plan_set_scalars(nsst_plan* p, const double* s) {

@@ -34,7 +34,7 @@ __all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters
            'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'atrousdec_noalloc',
            'nsst_scalars',
            'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
-           'level_spectra', 'launch_count', 'NsstError']
+           'level_spectra', 'launch_count', 'NsstError', 'save_shearing_filters', 'load_shearing_filters']
 
 
 def _dptr(a):
@@ -81,6 +81,27 @@ class ShearPlan:
         check(lib().nsst_plan_band_levels(h, lv))
         self.band_levels = list(lv)
         self.batch = lib().nsst_plan_batch_capacity(h)
+
+    @classmethod
+    def from_file(cls, path, H, W=None, batch=1):
+        """A plan over the filter bank of an SHFM0002 file (the reference's
+        exported dictionary) instead of the constructed one."""
+        W = H if W is None else W
+        h = ctypes.c_void_p()
+        check(lib().nsst_plan_create_from_file(str(path).encode(), int(H), int(W), int(batch), ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        info = load_shearing_filters(path)
+        self.dcomp = [int(round(np.log2(s.shape[0]))) for s in info['shear']]
+        self.dsize = [s.shape[1] for s in info['shear']]
+        self.H, self.W, self.lpfilt = int(H), int(W), 'file'
+        self.nlevels = len(self.dcomp)
+        self.nbands = lib().nsst_plan_num_bands(h)
+        lv = (ctypes.c_int * self.nbands)()
+        check(lib().nsst_plan_band_levels(h, lv))
+        self.band_levels = list(lv)
+        self.batch = lib().nsst_plan_batch_capacity(h)
+        return self
 
     def use_graphs(self, on=True):
         check(lib().nsst_plan_use_graphs(self.handle, 1 if on else 0))
@@ -190,11 +211,16 @@ def atrousdec_noalloc(x, nlevels, y, lpfilt='maxflat', stream=None):
     return y
 
 
+def _check_lpfilt(lpfilt, shear):
+    # a dictionary read from a filter-bank file carries its own pyramid filters
+    if shear.lpfilt != 'file' and lpfilt != shear.lpfilt:
+        raise NsstError(1, 'lpfilt %r does not match the prepared dictionary (%r)' % (lpfilt, shear.lpfilt))
+
+
 def shear_trans_cuda(x, lpfilt, shear, coeff=None, stream=None):
     """Forward NSST.  ``coeff`` (optional) is written in place, like the
     reference's coeff_inplace argument (shear_trans_cuda.cpp:191-205)."""
-    if lpfilt != shear.lpfilt:
-        raise NsstError(1, 'lpfilt %r does not match the prepared dictionary (%r)' % (lpfilt, shear.lpfilt))
+    _check_lpfilt(lpfilt, shear)
     if coeff is None:
         coeff = torch.empty((shear.nbands, shear.H, shear.W), device=x.device, dtype=torch.float32)
     check(lib().nsst_shear_trans(shear.handle, _dev(x, 'x', (shear.H, shear.W)),
@@ -218,8 +244,7 @@ def softth_cuda(coeff, sigma, K, scalars, shear, stream=None):
 
 
 def inverse_shear_cuda(coeff, lpfilt, shear, stream=None):
-    if lpfilt != shear.lpfilt:
-        raise NsstError(1, 'lpfilt %r does not match the prepared dictionary (%r)' % (lpfilt, shear.lpfilt))
+    _check_lpfilt(lpfilt, shear)
     x = torch.empty((shear.H, shear.W), device=coeff.device, dtype=torch.float32)
     check(lib().nsst_inverse_shear(shear.handle, _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W)),
                                    _dev(x, 'x'), _stream(stream)))
@@ -319,6 +344,48 @@ def nsst_scalars(shear, seed=0):
 
 
 # ------------------------------------------------------------ host-only helpers
+def save_shearing_filters(m, num, data_type='single', path=None, lpfilt='maxflat'):
+    """Write the filter bank of dsize m / dcomp num as the reference's
+    SHFM0002 file (save_shearing_filters.m:46-84); the default file name is
+    the reference's, shearFilters_<num..>_<data_type>.bin.  Returns the path."""
+    if len(m) != len(num):
+        raise NsstError(1, 'm and num must have the same length')
+    if data_type not in ('single', 'double'):
+        raise NsstError(1, "data_type must be 'single' or 'double'")
+    if path is None:
+        path = 'shearFilters' + ''.join('_%d' % v for v in num) + '_' + data_type + '.bin'
+    cfg = NsstConfig()
+    cfg.nlevels = len(num)
+    for i, (c, sz) in enumerate(zip(num, m)):
+        cfg.dcomp[i] = int(c)
+        cfg.dsize[i] = int(sz)
+    cfg.lpfilt = lpfilt.encode()
+    check(lib().nsst_filters_save(str(path).encode(), ctypes.byref(cfg), 0 if data_type == 'single' else 2))
+    return path
+
+
+def load_shearing_filters(path):
+    """Read an SHFM0002 file: {'data_type', 'shear': [(ndir, n, n) per scale],
+    'atrous': [h0, h1, g0, g1]} as FP64 arrays (row-major)."""
+    nl = ctypes.c_int()
+    ds, nd = (ctypes.c_int * 8)(), (ctypes.c_int * 8)()
+    F, dt = (ctypes.c_int * 4)(), ctypes.c_int()
+    check(lib().nsst_filters_load(str(path).encode(), ctypes.byref(nl), ds, nd, F, None, None, ctypes.byref(dt)))
+    shear = np.empty(sum(nd[l] * ds[l] ** 2 for l in range(nl.value)), np.float64)
+    pyr = np.empty(sum(f * f for f in F), np.float64)
+    check(lib().nsst_filters_load(str(path).encode(), ctypes.byref(nl), ds, nd, F, _dptr(shear), _dptr(pyr), None))
+    out, at = [], 0
+    for l in range(nl.value):
+        k = nd[l] * ds[l] ** 2
+        out.append(shear[at:at + k].reshape(nd[l], ds[l], ds[l]))
+        at += k
+    atr, at = [], 0
+    for f in F:
+        atr.append(pyr[at:at + f * f].reshape(f, f))
+        at += f * f
+    return {'data_type': 'single' if dt.value == 0 else 'double', 'shear': out, 'atrous': atr}
+
+
 def pyramid_filters(name='maxflat'):
     F = (ctypes.c_int * 4)()
     check(lib().nsst_pyramid_filters(name.encode(), F, None))
