@@ -258,6 +258,20 @@ int nsst_plan_saved_items(const nsst_plan* plan);
 /* Store per-band noise scalars in the plan (nbands doubles). */
 nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
 
+/* nsst_thresh, then the largest thresholded magnitude relative to its band's
+ * scalar, max_b max|c_b| / scalars[b] (bands with scalar 0 skipped), into
+ * *maxabs; waits for the stream.  Replaces thresh_cuda's opt == 1 output
+ * (thresh_cuda.cpp:199-205, thresh.m:38-41). */
+nsst_status nsst_thresh_max(nsst_plan* plan, float* coeffs, double sigma, const double* K, const double* scalars,
+                            int mode, double* maxabs, void* stream);
+
+/* Exact l2 norm of every band's shearlet (nbands doubles, coefficient plane
+ * order): the coefficients of an impulse of height sqrt(H W) at (H/2, W/2),
+ * E_b = ||C_b|| / sqrt(H W) — the deterministic alternative to the Monte-Carlo
+ * scalars, usable as nsst_thresh's scalars.  Synchronous.  Replaces com_norm.m
+ * (com_norm.m:25-55) and norm_cuda (norm_cuda.cpp:57-215). */
+nsst_status nsst_band_norms(nsst_plan* plan, double* E);
+
 /* Per-band noise scalars by the Monte-Carlo rule of nsst_scalars.m:28-45:
  * a seeded N(0,1) image (generated in FP64 on the host) is transformed on the
  * GPU and each band's MAD/0.6745 is taken on the host in FP64.  Writes nbands

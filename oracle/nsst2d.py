@@ -427,3 +427,19 @@ def denoise_tau_grad(x, tau, clean, shear_f, fname='maxflat', mode='soft', nthre
         gy.append(np.real(sfft.ifft2(np.sum(np.conj(shear_f[i]) * C, axis=0), workers=w)))
     gx = atrousdec_adjoint(gy, fname)
     return loss, gx, gtau
+
+
+def com_norm(H, W, dcomp, dsize, fname='maxflat', shear_f=None, nthreads=1):
+    """com_norm.m:25-55: l2 norm of every band's shearlet from the transform
+    of X = fftshift(real(ifft2(ones))) * sqrt(H W), an impulse at (H/2, W/2);
+    flat in coefficient plane order (lowpass first)."""
+    X = np.fft.fftshift(np.real(np.fft.ifft2(np.ones((H, W))))) * math.sqrt(H * W)
+    dst, _ = nsst_dec2(X, dcomp, dsize, fname, shear_f=shear_f, nthreads=nthreads)
+    planes = [dst[0]] + [p for lev in dst[1:] for p in lev]
+    return np.array([math.sqrt(float(np.sum(p * p)) / (H * W)) for p in planes])
+
+
+def thresh_maxi(coeffs, scalars):
+    """thresh.m:38-41 (opt == 1): max over bands of max|c_b / E_b| of the
+    thresholded coefficients (flat planes, flat scalars)."""
+    return max(float(np.max(np.abs(c))) / s for c, s in zip(coeffs, scalars) if s > 0)

@@ -81,6 +81,8 @@ SIGNATURES = [
     ('nsst_denoise_tau_backward_saved', _ci, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _ci, _vp, _vp, _ci, _ci,
                                               _vp]),
     ('nsst_plan_saved_items', _ci, [_vp]),
+    ('nsst_thresh_max', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _dp, _vp]),
+    ('nsst_band_norms', _ci, [_vp, _dp]),
     ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
     ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst_timers_enable', _ci, [_vp, _ci]),

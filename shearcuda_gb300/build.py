@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libnsst.so')
 NVCC = os.environ.get('NVCC', '/usr/local/cuda/bin/nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-SOURCES = ['k_directional.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
+SOURCES = ['k_directional.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_reduce.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
            'host_filters3d.cpp', 'plan.cpp', 'plan3d.cpp']
 HEADERS = ['fft_core.cuh', 'internal.h', 'pyramid_tables.h']
 

@@ -123,6 +123,12 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
                                  void* dst_base, const float2* twWh, const float2* twW, const float* tau, int mode,
                                  float* partials, size_t pstride, cudaStream_t st);
 cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
+// per-plane reductions (k_reduce.cu): FP64 partial sums of squares,
+// partial[plane * blocks + block]; bit patterns of the largest |x| (maxbits zeroed first)
+cudaError_t launch_plane_sumsq(const float* data, size_t n, int nplanes, double* partial, int blocks,
+                               cudaStream_t st);
+cudaError_t launch_plane_maxabs(const float* data, size_t n, int nplanes, unsigned* maxbits, int blocks,
+                                cudaStream_t st);
 
 // ------------------------------------------------------------------- 3-D path
 struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)

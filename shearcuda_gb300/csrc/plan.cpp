@@ -50,6 +50,7 @@ struct nsst_plan {
   std::vector<int> ndir, first_band, band_level;  // per level / per band
   PyramidFilters pf;
   std::vector<std::vector<double>> shear_w;  // FP64 shearing filters per level (ndir x dsize^2, row-major)
+  double* red_scratch = nullptr;  // per-plane reduction partials (nbands x kRedBlocks doubles)
   std::vector<float> hflip[4];  // FP32 flipped h0, h1, g0, g1 (forward steps)
   std::vector<float> h32[4];    // FP32 unflipped h0, h1, g0, g1 (adjoint steps)
   int device = 0;
@@ -153,6 +154,8 @@ nsst_status cuda_fail(cudaError_t e, const char* what) {
   } while (0)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+constexpr int kRedBlocks = 64;  // blocks per plane of the per-plane reductions
 
 std::vector<float> flip_to_float(const std::vector<double>& h, int F) {
   std::vector<float> out((size_t)F * F);
@@ -320,6 +323,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_band = take(sizeof(float2) * p->s_band * NB);
   size_t o_sum = take(sizeof(float2) * p->s_sum * NB);
   size_t o_rec = take(sizeof(float) * p->s_rec * NB);
+  size_t o_red = take(sizeof(double) * p->nbands * kRedBlocks);
   size_t o_th = take(sizeof(float) * p->nbands * NB);
   const size_t nL = NB * p->nlev, nD = NB * p->ndir_total;
   size_t o_j1 = take(sizeof(RowJob) * nL), o_j2 = take(sizeof(ColJob) * nL);
@@ -352,6 +356,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->sum = (float2*)(A + o_sum);
   p->rec = (float*)(A + o_rec);
   p->th = (float*)(A + o_th);
+  p->red_scratch = (double*)(A + o_red);
   p->j_rows_lev_fwd = (RowJob*)(A + o_j1);
   p->j_cols_lev = (ColJob*)(A + o_j2);
   p->j_analysis = (ColJob*)(A + o_j3);
@@ -817,6 +822,69 @@ nsst_status nsst_thresh(nsst_plan* p, float* coeffs, double sigma, const double*
   cudaStream_t st = (cudaStream_t)stream;
   NSST_TRY(upload_thresholds(p, 1, &sigma, K, scalars, st, nullptr));
   NSST_CUDA(launch_thresh_bands(coeffs, (size_t)p->H * p->W, p->nbands, p->th, mode, st));
+  return NSST_OK;
+}
+
+nsst_status nsst_thresh_max(nsst_plan* p, float* coeffs, double sigma, const double* K, const double* scalars,
+                            int mode, double* maxabs, void* stream) {
+  if (!maxabs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(nsst_thresh(p, coeffs, sigma, K, scalars, mode, stream));
+  if (!scalars && !p->has_scalars) return fail(NSST_ERR_INVALID_ARG, "no scalars");
+  const double* sc = scalars ? scalars : p->scalars.data();
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned* bits = reinterpret_cast<unsigned*>(p->red_scratch);
+  NSST_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * p->nbands, st));
+  NSST_CUDA(launch_plane_maxabs(coeffs, (size_t)p->H * p->W, p->nbands, bits, kRedBlocks, st));
+  std::vector<unsigned> hb(p->nbands);
+  NSST_CUDA(cudaMemcpyAsync(hb.data(), bits, sizeof(unsigned) * p->nbands, cudaMemcpyDeviceToHost, st));
+  NSST_CUDA(cudaStreamSynchronize(st));
+  // thresh.m:38-41: max over the bands of max|c_b| / E_b
+  double m = 0.0;
+  for (int b = 0; b < p->nbands; b++) {
+    float v;
+    std::memcpy(&v, &hb[b], sizeof(float));
+    if (sc[b] > 0) m = std::max(m, (double)v / sc[b]);
+  }
+  *maxabs = m;
+  return NSST_OK;
+}
+
+nsst_status nsst_band_norms(nsst_plan* p, double* E) {
+  if (!p || !E) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  const size_t HW = (size_t)p->H * p->W;
+  // com_norm.m:37-40: X = fftshift(real(ifft2(ones))) * sqrt(HW), an impulse
+  // of height sqrt(HW) at (H/2, W/2)
+  std::vector<float> x(HW, 0.0f);
+  x[(size_t)(p->H / 2) * p->W + p->W / 2] = (float)std::sqrt((double)HW);
+  float *dx = nullptr, *dc = nullptr;
+  cudaError_t e = dev_alloc((void**)&dx, HW * sizeof(float));
+  if (e != cudaSuccess) return cuda_fail(e, "norm scratch");
+  e = dev_alloc((void**)&dc, HW * sizeof(float) * p->nbands);
+  if (e != cudaSuccess) {
+    cudaFree(dx);
+    return cuda_fail(e, "norm scratch");
+  }
+  nsst_status s = NSST_OK;
+  std::vector<double> part((size_t)p->nbands * kRedBlocks);
+  e = cudaMemcpy(dx, x.data(), HW * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) s = nsst_shear_trans(p, dx, dc, nullptr);
+  if (e == cudaSuccess && s == NSST_OK) {
+    std::lock_guard<std::mutex> lk(p->mu);
+    e = launch_plane_sumsq(dc, HW, p->nbands, p->red_scratch, kRedBlocks, nullptr);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(part.data(), p->red_scratch, part.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dx);
+  cudaFree(dc);
+  if (e != cudaSuccess) return cuda_fail(e, "band norms");
+  if (s != NSST_OK) return s;
+  // com_norm.m:45-51: E = sqrt(sum |C_b|^2 / (H W))
+  for (int b = 0; b < p->nbands; b++) {
+    double t = 0.0;
+    for (int k = 0; k < kRedBlocks; k++) t += part[(size_t)b * kRedBlocks + k];
+    E[b] = std::sqrt(t / (double)HW);
+  }
   return NSST_OK;
 }
 

@@ -34,7 +34,7 @@ __all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters
            'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'atrousdec_noalloc',
            'nsst_scalars',
            'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
-           'level_spectra', 'launch_count', 'NsstError', 'save_shearing_filters', 'load_shearing_filters']
+           'level_spectra', 'launch_count', 'NsstError', 'save_shearing_filters', 'load_shearing_filters', 'com_norm']
 
 
 def _dptr(a):
@@ -228,15 +228,31 @@ def shear_trans_cuda(x, lpfilt, shear, coeff=None, stream=None):
     return coeff
 
 
-def thresh_cuda(coeff, sigma, K, scalars, shear, mode=THRESH_HARD, stream=None):
-    """In-place threshold of all bands: t_b = K[level(b)] * sigma * scalars[b]."""
+def thresh_cuda(coeff, sigma, K, scalars, shear, mode=THRESH_HARD, stream=None, opt=0):
+    """In-place threshold of all bands: t_b = K[level(b)] * sigma * scalars[b].
+    opt == 1 returns, like the reference's thresh_cuda, the largest thresholded
+    magnitude relative to its band scalar (max_b max|c_b| / scalars[b]);
+    otherwise the coefficients."""
     s = np.ascontiguousarray(flatten_scalars(scalars), dtype=np.float64)
     if s.size != shear.nbands:
         raise NsstError(1, 'need %d scalars' % shear.nbands)
     K = _kvec(shear, K)
-    check(lib().nsst_thresh(shear.handle, _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W)), float(sigma),
-                            _dptr(K), _dptr(s), mode, _stream(stream)))
+    c = _dev(coeff, 'coeff', (shear.nbands, shear.H, shear.W))
+    if opt == 1:
+        m = ctypes.c_double()
+        check(lib().nsst_thresh_max(shear.handle, c, float(sigma), _dptr(K), _dptr(s), mode, ctypes.byref(m),
+                                    _stream(stream)))
+        return m.value
+    check(lib().nsst_thresh(shear.handle, c, float(sigma), _dptr(K), _dptr(s), mode, _stream(stream)))
     return coeff
+
+
+def com_norm(shear):
+    """Exact l2 norms of the shearlets of every band (com_norm.m:25-55), in
+    coefficient plane order; usable as thresh_cuda's scalars."""
+    out = np.empty(shear.nbands, dtype=np.float64)
+    check(lib().nsst_band_norms(shear.handle, _dptr(out)))
+    return out
 
 
 def softth_cuda(coeff, sigma, K, scalars, shear, stream=None):

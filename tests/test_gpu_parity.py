@@ -186,3 +186,25 @@ def test_allocation_failure_is_reported(built_lib, cuda):
     finally:
         lib().nsst_debug_fail_next_alloc(0)
     sc.ShearPlan(DCOMP, DSIZE, 256, 256)  # and the library still works
+
+
+def test_band_norms_and_thresh_max_match_oracle(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300.synth import noisy_image
+    H = W = 256
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W)
+    E = sc.com_norm(shear)
+    sf = nsst2d.shear_spectra(H, W, DCOMP, DSIZE)
+    E_ref = nsst2d.com_norm(H, W, DCOMP, DSIZE, shear_f=sf)
+    assert np.abs(E / E_ref - 1).max() < 1e-5
+    # thresh_cuda(..., opt=1) with the exact norms as scalars
+    _, noisy = noisy_image(H, W, 20.0, 31)
+    x = torch.tensor(noisy.astype(np.float32), device=cuda)
+    c = sc.shear_trans_cuda(x, 'maxflat', shear)
+    maxi = sc.thresh_cuda(c, 20.0, [0, 3, 3, 3, 4], E, shear, opt=1)
+    got = c.cpu().numpy().astype(np.float64)
+    assert maxi == pytest.approx(nsst2d.thresh_maxi(got, E), rel=1e-12)
+    # the thresholded planes are the plain threshold's
+    c2 = sc.shear_trans_cuda(x, 'maxflat', shear)
+    sc.thresh_cuda(c2, 20.0, [0, 3, 3, 3, 4], E, shear)
+    assert torch.equal(c2.cpu(), torch.tensor(got, dtype=torch.float32))

@@ -125,3 +125,16 @@ def test_oracle_loss_gradient_finite_differences():
     fd = (np.sum((nsst2d.denoise_tau(noisy, tp, sf, nthreads=4)[0] - clean) ** 2) -
           np.sum((nsst2d.denoise_tau(noisy, tm, sf, nthreads=4)[0] - clean) ** 2)) / (2 * h)
     assert abs(fd - gt[2][3]) <= 1e-3 * max(1.0, abs(fd))
+
+
+def test_com_norm_is_the_noise_std():
+    # for white N(0,1) noise every band is Gaussian with std = its shearlet's
+    # l2 norm: the exact norms (com_norm.m) and the Monte-Carlo scalars
+    # (nsst_scalars.m) agree up to Monte-Carlo error
+    H = W = 128
+    sf = nsst2d.shear_spectra(H, W, [2, 3], [16, 16])
+    E = nsst2d.com_norm(H, W, [2, 3], [16, 16], shear_f=sf)
+    mc = nsst2d.nsst_scalars(H, W, sf, seed=3)
+    flat = np.concatenate([[mc[0]]] + [np.asarray(s) for s in mc[1:]])
+    assert E.shape == flat.shape
+    assert np.abs(E / flat - 1).max() < 0.1
