@@ -265,6 +265,12 @@ nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
 nsst_status nsst_thresh_max(nsst_plan* plan, float* coeffs, double sigma, const double* K, const double* scalars,
                             int mode, double* maxabs, void* stream);
 
+/* out = atrousrec(weights .* atrousdec(x)): the image re-synthesised with
+ * weights[0] on the lowpass and weights[1..nlevels] on the band-pass images,
+ * coarse to fine (x, out: H x W device).  Replaces re_weight_band /
+ * re_weight_band_cuda (re_weight_band.m:23-29, re_weight_band_cuda.cpp:59-183). */
+nsst_status nsst_re_weight_band(nsst_plan* plan, const float* x, const double* weights, float* out, void* stream);
+
 /* Exact l2 norm of every band's shearlet (nbands doubles, coefficient plane
  * order): the coefficients of an impulse of height sqrt(H W) at (H/2, W/2),
  * E_b = ||C_b|| / sqrt(H W) — the deterministic alternative to the Monte-Carlo

@@ -443,3 +443,11 @@ def thresh_maxi(coeffs, scalars):
     """thresh.m:38-41 (opt == 1): max over bands of max|c_b / E_b| of the
     thresholded coefficients (flat planes, flat scalars)."""
     return max(float(np.max(np.abs(c))) / s for c, s in zip(coeffs, scalars) if s > 0)
+
+
+def re_weight_band(P, coeff, fname='maxflat', conv='port', nthreads=1):
+    """re_weight_band.m:23-29: atrousdec with len(coeff)-1 levels, band j
+    scaled by coeff[j] (lowpass first), atrousrec."""
+    y = atrousdec(P, fname, len(coeff) - 1, conv=conv, nthreads=nthreads)
+    y = [c * b for c, b in zip(coeff, y)]
+    return atrousrec(y, fname, conv=conv, nthreads=nthreads)

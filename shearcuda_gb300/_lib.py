@@ -83,6 +83,7 @@ SIGNATURES = [
     ('nsst_plan_saved_items', _ci, [_vp]),
     ('nsst_thresh_max', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _dp, _vp]),
     ('nsst_band_norms', _ci, [_vp, _dp]),
+    ('nsst_re_weight_band', _ci, [_vp, _vp, _dp, _vp, _vp]),
     ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
     ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst_timers_enable', _ci, [_vp, _ci]),

@@ -129,6 +129,11 @@ cudaError_t launch_plane_sumsq(const float* data, size_t n, int nplanes, double*
                                cudaStream_t st);
 cudaError_t launch_plane_maxabs(const float* data, size_t n, int nplanes, unsigned* maxbits, int blocks,
                                 cudaStream_t st);
+constexpr int kMaxPlaneWeights = NSST_MAX_LEVELS + 1;
+struct PlaneWeights {  // passed by value
+  float w[kMaxPlaneWeights];
+};
+cudaError_t launch_scale_planes(float* data, size_t n, int nplanes, const PlaneWeights& w, cudaStream_t st);
 
 // ------------------------------------------------------------------- 3-D path
 struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)

@@ -41,6 +41,21 @@ __global__ void __launch_bounds__(kRedThreads) k_plane_maxabs(const float* __res
   if ((threadIdx.x & 31) == 0) atomicMax(&maxbits[blockIdx.y], __float_as_uint(m));
 }
 
+// data[plane][i] *= w[plane]
+__global__ void k_scale_planes(float* __restrict__ data, size_t n, PlaneWeights w) {
+  float* x = data + (size_t)blockIdx.y * n;
+  const float s = w.w[blockIdx.y];
+  for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kRedThreads)
+    x[i] *= s;
+}
+
+cudaError_t launch_scale_planes(float* data, size_t n, int nplanes, const PlaneWeights& w, cudaStream_t st) {
+  if (nplanes > kMaxPlaneWeights) return cudaErrorInvalidValue;
+  count_launch();
+  k_scale_planes<<<dim3(64, nplanes), kRedThreads, 0, st>>>(data, n, w);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_plane_sumsq(const float* data, size_t n, int nplanes, double* partial, int blocks,
                                cudaStream_t st) {
   count_launch();

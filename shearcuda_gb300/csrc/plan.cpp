@@ -850,6 +850,25 @@ nsst_status nsst_thresh_max(nsst_plan* p, float* coeffs, double sigma, const dou
   return NSST_OK;
 }
 
+// re_weight_band.m:23-29: atrousdec, weight per pyramid band, atrousrec
+nsst_status nsst_re_weight_band(nsst_plan* p, const float* x, const double* weights, float* out, void* stream) {
+  if (!p || !x || !weights || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  PlaneWeights w{};
+  for (int k = 0; k <= p->nlev; k++) {
+    if (!std::isfinite(weights[k])) return fail(NSST_ERR_INVALID_ARG, "weights must be finite");
+    w.w[k] = (float)weights[k];
+  }
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  timer_begin(p, st);
+  float* y = p->pyr;  // item 0's pyramid planes: lowpass, then band-pass coarse -> fine
+  NSST_TRY(run_atrousdec(p, 1, &x, &y, nullptr, st));
+  NSST_CUDA(launch_scale_planes(y, (size_t)p->H * p->W, p->nlev + 1, w, st));
+  const float* yc = y;
+  return run_atrousrec(p, 1, &yc, nullptr, &out, st);
+}
+
 nsst_status nsst_band_norms(nsst_plan* p, double* E) {
   if (!p || !E) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   const size_t HW = (size_t)p->H * p->W;

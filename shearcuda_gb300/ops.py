@@ -34,7 +34,7 @@ __all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters
            'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'atrousdec_noalloc',
            'nsst_scalars',
            'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
-           'level_spectra', 'launch_count', 'NsstError', 'save_shearing_filters', 'load_shearing_filters', 'com_norm']
+           'level_spectra', 'launch_count', 'NsstError', 'save_shearing_filters', 'load_shearing_filters', 'com_norm', 're_weight_band']
 
 
 def _dptr(a):
@@ -245,6 +245,19 @@ def thresh_cuda(coeff, sigma, K, scalars, shear, mode=THRESH_HARD, stream=None, 
         return m.value
     check(lib().nsst_thresh(shear.handle, c, float(sigma), _dptr(K), _dptr(s), mode, _stream(stream)))
     return coeff
+
+
+def re_weight_band(P, coeff, shear, out=None, stream=None):
+    """Image re-synthesised with a weight per pyramid band (re_weight_band.m):
+    coeff[0] lowpass, coeff[1:] band-pass coarse to fine (len = nlevels + 1)."""
+    w = np.ascontiguousarray(coeff, dtype=np.float64).ravel()
+    if w.size != shear.nlevels + 1:
+        raise NsstError(1, 'need %d weights' % (shear.nlevels + 1))
+    x = _dev(P, 'P', (shear.H, shear.W))
+    if out is None:
+        out = torch.empty_like(P)
+    check(lib().nsst_re_weight_band(shear.handle, x, _dptr(w), _dev(out, 'out', (shear.H, shear.W)), _stream(stream)))
+    return out
 
 
 def com_norm(shear):

@@ -208,3 +208,20 @@ def test_band_norms_and_thresh_max_match_oracle(built_lib, cuda):
     c2 = sc.shear_trans_cuda(x, 'maxflat', shear)
     sc.thresh_cuda(c2, 20.0, [0, 3, 3, 3, 4], E, shear)
     assert torch.equal(c2.cpu(), torch.tensor(got, dtype=torch.float32))
+
+
+def test_re_weight_band_matches_oracle(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300.synth import noisy_image
+    H, W = 256, 384
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W)
+    _, noisy = noisy_image(H, W, 20.0, 41)
+    x = torch.tensor(noisy.astype(np.float32), device=cuda)
+    w = [0.5, 1.0, 1.5, 2.0, 0.25]
+    got = sc.re_weight_band(x, w, shear).cpu().numpy().astype(np.float64)
+    ref = nsst2d.re_weight_band(noisy.astype(np.float32).astype(np.float64), w)
+    assert rel_l2(got, ref) <= 1e-5
+    ones = sc.re_weight_band(x, [1.0] * 5, shear).cpu().numpy()
+    assert rel_l2(ones, noisy) <= 1e-5  # perfect reconstruction
+    with pytest.raises(sc.NsstError):
+        sc.re_weight_band(x, [1.0] * 4, shear)
