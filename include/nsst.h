@@ -265,11 +265,15 @@ nsst_status nsst_plan_set_scalars(nsst_plan* plan, const double* scalars);
 nsst_status nsst_thresh_max(nsst_plan* plan, float* coeffs, double sigma, const double* K, const double* scalars,
                             int mode, double* maxabs, void* stream);
 
-/* out = atrousrec(weights .* atrousdec(x)): the image re-synthesised with
- * weights[0] on the lowpass and weights[1..nlevels] on the band-pass images,
- * coarse to fine (x, out: H x W device).  Replaces re_weight_band /
- * re_weight_band_cuda (re_weight_band.m:23-29, re_weight_band_cuda.cpp:59-183). */
-nsst_status nsst_re_weight_band(nsst_plan* plan, const float* x, const double* weights, float* out, void* stream);
+/* out = atrousrec(weights .* atrousdec(x, nweights - 1 levels)): the image
+ * re-synthesised with weights[0] on the lowpass and weights[1..nweights-1] on
+ * the band-pass images, coarse to fine, with the plan's pyramid filters
+ * (x, out: H x W device; 2 <= nweights <= nlevels + 1).  Replaces
+ * re_weight_band / re_weight_band_cuda (re_weight_band.m:23-29,
+ * re_weight_band_cuda.cpp:59-183), which likewise take the level count from
+ * the length of the weight vector. */
+nsst_status nsst_re_weight_band(nsst_plan* plan, const float* x, const double* weights, int nweights, float* out,
+                                void* stream);
 
 /* Exact l2 norm of every band's shearlet (nbands doubles, coefficient plane
  * order): the coefficients of an impulse of height sqrt(H W) at (H/2, W/2),
@@ -294,6 +298,63 @@ nsst_status nsst_compute_scalars(nsst_plan* plan, uint64_t seed, double* out);
  * which synchronised the device around every step. */
 nsst_status nsst_timers_enable(nsst_plan* plan, int enable);
 int nsst_timers_read(nsst_plan* plan, char* names, size_t names_len, float* ms, int max_stages);
+
+/* ------------------------------------------------------------------------
+ * Undecimated wavelets and image separation.
+ * ------------------------------------------------------------------------ */
+enum { NSST_MAX_QMF = 64 };
+
+/* The orthonormal QMF of MakeONFilter.m (MakeONFilter.m:1-289): type "Haar",
+ * "Beylkin", "Coiflet" (par 1-5), "Daubechies" (par 4, 6, ..., 20),
+ * "Symmlet" (par 4-10), "Vaidyanathan" or "Battle" (par 1, 3, 5); par is
+ * ignored for the families without one.  Writes f / norm(f) to out (up to
+ * NSST_MAX_QMF doubles) and its length to *len.  Host only. */
+nsst_status nsst_onfilter(const char* type, int par, double* out, int* len);
+
+/* Redundant (undecimated) DWT of n images, L levels, periodic: mrdwt /
+ * mrdwt_cuda (src/mrdwt_r.h:104-209, src_cuda/mrdwt_cuda.cpp:55-255).
+ * x: n x H x W device; h: lh host doubles (lh <= 32), the scaling filter.
+ * yl: n x H x W (the level-L lowpass); yh: n x 3L x H x W, per level the
+ * planes LH, HL, HH (first letter: filtering along a row), level 1 first --
+ * the reference's m x 3nL yh, block by block.  H and W must be multiples of
+ * 2^L, W <= 8192.  x may equal yl.  Asynchronous on stream. */
+nsst_status nsst_mrdwt(const float* x, int n, int H, int W, const double* h, int lh, int L, float* yl, float* yh,
+                       void* stream);
+
+/* Inverse of nsst_mrdwt: mirdwt / mirdwt_cuda (src/mirdwt_r.h:115-219,
+ * src_cuda/mirdwt_cuda.cpp).  yl, yh are left unchanged; x may equal yl.
+ * Takes two planes of stream-ordered scratch per image. */
+nsst_status nsst_mirdwt(const float* yl, const float* yh, int n, int H, int W, const double* h, int lh, int L,
+                        float* x, void* stream);
+
+/* TV correction of n images (x, y: n x H x W device; y != x): one Haar level
+ * of nsst_mrdwt, soft threshold gamma on the three highpass planes, nsst_mirdwt
+ * -- one fused stencil.  Replaces TVCorrection / TVCorrection_cuda
+ * (separate.m:264-285: mrdwt_cuda, softth_cuda, mirdwt_cuda). */
+nsst_status nsst_tv_correction(const float* x, int n, int H, int W, double gamma, float* y, void* stream);
+
+/* What nsst_separate derived from each image before its loop (separate.m:72-126). */
+typedef struct nsst_separate_info {
+  double sigma;          /* MAD / 0.6745 of the HH band of a one-level Daubechies-4 DWT */
+  double stop;           /* stop * sigma */
+  double buff_shear;     /* thresh opt == 1 max of the shearlet coefficients (buff(1)) */
+  double buff_wavelet;   /* max |yh| of the Symmlet-4 mrdwt (buff(2)) */
+  double deltamax;       /* min(buff) */
+  double lambda;         /* (deltamax / stop)^(1 / (1 - itermax)) */
+} nsst_separate_info;
+
+/* Points / curves separation of n images (n <= the plan's batch capacity):
+ * separate.m:1-289 with the plan's shearlets, the 'maxflat' pyramid of the
+ * plan, level2 Symmlet-4 wavelet levels, itermax iterations, the stopping
+ * factor stop, the TV soft threshold gamma and the ncoeff band weights coeff
+ * (re_weight_band; 2 <= ncoeff <= nlevels + 1).  img: n x H x W device;
+ * writes the curve part to C and the point part to P (n x H x W device) and,
+ * if info is not NULL, n nsst_separate_info records.  The per-image setup
+ * (band norms, MAD, the two maxima) waits for the stream; the iterations are
+ * then queued on it without host waits. */
+nsst_status nsst_separate(nsst_plan* plan, const float* img, int n, int level2, int itermax, double stop,
+                          double gamma, const double* coeff, int ncoeff, float* C, float* P,
+                          nsst_separate_info* info, void* stream);
 
 /* Number of kernels this library has launched since load (all plans, all threads). */
 uint64_t nsst_launch_count(void);

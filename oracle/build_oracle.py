@@ -4,8 +4,12 @@
 * ``oracle/_ref/libatrousc_ref.so``: the reference's own
   ``shearlet_toolbox_1/atrousc.cpp``, compiled unchanged where it lies in the
   reference checkout, against the project-written MEX shim in
-  ``oracle/mex_shim`` plus ``atrous_ref_glue.cpp``.  Built only when the
-  reference checkout is present (it is not on machines that only run tests).
+  ``oracle/mex_shim`` plus ``atrous_ref_glue.cpp``.
+* ``oracle/_ref/librwt_ref.so``: the reference's Rice Wavelet Toolbox
+  templates ``shearcuda/src/{mrdwt,mirdwt,mdwt}_r.h``, included where they lie,
+  behind ``rwt_ref_glue.cpp``.
+Both reference builds happen only when the reference checkout is present (it
+is not on machines that only run tests).
 
 Usage: python oracle/build_oracle.py [--reference DIR]
 """
@@ -17,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, 'libatrous_port.so')
 REF_DIR = os.path.join(HERE, '_ref')
 REF_SO = os.path.join(REF_DIR, 'libatrousc_ref.so')
+RWT_SO = os.path.join(REF_DIR, 'librwt_ref.so')
 DEFAULT_REFERENCE = '/root/reference'
 
 
@@ -29,8 +34,8 @@ def _newer(target, sources):
 
 def build_port(force=False):
     src = os.path.join(HERE, 'atrous_port.c')
-    if force or _newer(PORT_SO, [src]):
-        subprocess.check_call(['gcc', '-O3', '-fPIC', '-shared', '-pthread', '-o', PORT_SO, src])
+    if force or _newer(PORT_SO, [src, os.path.abspath(__file__)]):
+        subprocess.check_call(['gcc', '-O3', '-ffp-contract=off', '-fPIC', '-shared', '-pthread', '-o', PORT_SO, src])
     return PORT_SO
 
 
@@ -43,8 +48,21 @@ def build_ref(reference=DEFAULT_REFERENCE, force=False):
     os.makedirs(REF_DIR, exist_ok=True)
     deps = [src, glue, os.path.join(shim, 'mex.h'), os.path.join(shim, 'matrix.h')]
     if force or _newer(REF_SO, deps):
-        subprocess.check_call(['g++', '-O2', '-fPIC', '-shared', '-I', shim, '-o', REF_SO, glue, src])
+        subprocess.check_call(['g++', '-O2', '-ffp-contract=off', '-fPIC', '-shared', '-I', shim, '-o', REF_SO, glue, src])
     return REF_SO
+
+
+def build_rwt_ref(reference=DEFAULT_REFERENCE, force=False):
+    srcdir = os.path.join(reference, 'shearcuda', 'src')
+    heads = [os.path.join(srcdir, f) for f in ('mrdwt_r.h', 'mirdwt_r.h', 'mdwt_r.h')]
+    if not all(os.path.exists(h) for h in heads):
+        return None
+    glue = os.path.join(HERE, 'rwt_ref_glue.cpp')
+    shim = os.path.join(HERE, 'mex_shim')
+    os.makedirs(REF_DIR, exist_ok=True)
+    if force or _newer(RWT_SO, heads + [glue, os.path.join(shim, 'matrix.h')]):
+        subprocess.check_call(['g++', '-O2', '-ffp-contract=off', '-fPIC', '-shared', '-I', shim, '-I', srcdir, '-o', RWT_SO, glue])
+    return RWT_SO
 
 
 def main():
@@ -54,6 +72,7 @@ def main():
     a = ap.parse_args()
     print(build_port(a.force))
     print(build_ref(a.reference, a.force))
+    print(build_rwt_ref(a.reference, a.force))
 
 
 if __name__ == '__main__':

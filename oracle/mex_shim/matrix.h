@@ -1,10 +1,11 @@
 /* Minimal, project-written stand-in for MATLAB's matrix.h.
  *
- * Test infrastructure only: it lets the reference's MEX source
- * shearlet_toolbox_1/atrousc.cpp compile unchanged as a plain shared
- * library so that its convolution loop can serve as the oracle's
- * ground truth.  Only the handful of calls that file makes are provided
- * (atrousc.cpp:83-125).  Arrays are column-major like MATLAB's. */
+ * Test infrastructure only: it lets the reference's MEX sources
+ * shearlet_toolbox_1/atrousc.cpp and the Rice Wavelet Toolbox templates
+ * shearcuda/src/{mrdwt,mirdwt,mdwt}_r.h compile unchanged as plain shared
+ * libraries so that their loops can serve as the oracle's ground truth.
+ * Only the handful of calls those files make are provided (atrousc.cpp:83-125,
+ * mxCalloc in the templates).  Arrays are column-major like MATLAB's. */
 #ifndef NSST_ORACLE_MATRIX_H
 #define NSST_ORACLE_MATRIX_H
 #include <stddef.h>
@@ -27,4 +28,5 @@ bool mxIsClass(const mxArray* a, const char* name);
 double* mxGetPr(const mxArray* a);
 void* mxGetData(const mxArray* a);
 mxArray* mxCreateNumericArray(mwSize ndim, const mwSize* dims, mxClassID cls, mxComplexity cplx);
+void* mxCalloc(size_t n, size_t size);
 #endif

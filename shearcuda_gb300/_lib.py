@@ -32,6 +32,11 @@ class Nsst3Config(ctypes.Structure):
     _fields_ = [('nlevels', ctypes.c_int), ('num_dirs', ctypes.c_int * MAX_LEVELS), ('pyr_mode', ctypes.c_double)]
 
 
+class NsstSeparateInfo(ctypes.Structure):
+    _fields_ = [('sigma', ctypes.c_double), ('stop', ctypes.c_double), ('buff_shear', ctypes.c_double),
+                ('buff_wavelet', ctypes.c_double), ('deltamax', ctypes.c_double), ('lam', ctypes.c_double)]
+
+
 class NsstError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__('%s: %s' % (STATUS_NAMES.get(status, status), msg))
@@ -83,11 +88,17 @@ SIGNATURES = [
     ('nsst_plan_saved_items', _ci, [_vp]),
     ('nsst_thresh_max', _ci, [_vp, _vp, _cd, _dp, _dp, _ci, _dp, _vp]),
     ('nsst_band_norms', _ci, [_vp, _dp]),
-    ('nsst_re_weight_band', _ci, [_vp, _vp, _dp, _vp, _vp]),
+    ('nsst_re_weight_band', _ci, [_vp, _vp, _dp, _ci, _vp, _vp]),
     ('nsst_plan_set_scalars', _ci, [_vp, _dp]),
     ('nsst_compute_scalars', _ci, [_vp, ctypes.c_uint64, _dp]),
     ('nsst_timers_enable', _ci, [_vp, _ci]),
     ('nsst_timers_read', _ci, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_float), _ci]),
+    ('nsst_onfilter', _ci, [ctypes.c_char_p, _ci, _dp, _ip]),
+    ('nsst_mrdwt', _ci, [_vp, _ci, _ci, _ci, _dp, _ci, _ci, _vp, _vp, _vp]),
+    ('nsst_mirdwt', _ci, [_vp, _vp, _ci, _ci, _ci, _dp, _ci, _ci, _vp, _vp]),
+    ('nsst_tv_correction', _ci, [_vp, _ci, _ci, _ci, _cd, _vp, _vp]),
+    ('nsst_separate', _ci, [_vp, _vp, _ci, _ci, _ci, _cd, _cd, _dp, _ci, _vp, _vp, ctypes.POINTER(NsstSeparateInfo),
+                            _vp]),
     ('nsst_launch_count', ctypes.c_uint64, []),
     ('nsst_debug_fail_next_alloc', None, [_ci]),
     ('nsst3_plan_create', _ci, [ctypes.POINTER(Nsst3Config), _ci, _ci, _ci, _ci, ctypes.POINTER(_vp)]),

@@ -15,13 +15,17 @@ BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libnsst.so')
 NVCC = os.environ.get('NVCC', '/usr/local/cuda/bin/nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-SOURCES = ['k_directional.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_reduce.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
-           'host_filters3d.cpp', 'plan.cpp', 'plan3d.cpp']
-HEADERS = ['fft_core.cuh', 'internal.h', 'pyramid_tables.h']
+SOURCES = ['k_directional.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_reduce.cu', 'k_wavelet.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
+           'host_wavelets.cpp',            'host_filters3d.cpp', 'plan.cpp', 'plan3d.cpp']
+HEADERS = ['fft_core.cuh', 'internal.h', 'pyramid_tables.h', 'wavelet_tables.h']
 
 
 def _flags(src):
-    common = ['-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-I', os.path.join(ROOT, 'include')]
+    # -ffp-contract=off: the host's FP64 filter construction (grid rounding in
+    # the Meyer windows) must give the same bits on x86-64 and on aarch64, whose
+    # gcc would otherwise fuse multiply-adds
+    common = ['-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-ffp-contract=off',
+              '-I', os.path.join(ROOT, 'include')]
     if src.endswith('.cu'):
         return common + ARCH + ['-lineinfo', '--expt-relaxed-constexpr']
     return common + ['-x', 'cu'] + ARCH if False else common + ['-x', 'c++']
@@ -37,7 +41,7 @@ def _newer(target, deps):
 def _compile(src, verbose=False):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + '.o')
     deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + \
-        [os.path.join(ROOT, 'include', 'nsst.h')]
+        [os.path.join(ROOT, 'include', 'nsst.h'), os.path.abspath(__file__)]
     if not _newer(obj, deps):
         return obj, ''
     cmd = [NVCC] + _flags(src) + ['-c', os.path.join(CSRC, src), '-o', obj]

@@ -238,6 +238,50 @@ bool level_spectra(const std::vector<double>& filters, int ndir, int n1, int H, 
 std::vector<float2> twiddle_table(int n);            // exp(-2 pi i t / n), t < n
 std::vector<float2> half_twiddle_table(int n);       // exp(-2 pi i k / n), k < n/2
 
+// -------------------------------------------- undecimated wavelets (k_wavelet.cu)
+// MakeONFilter.m: the orthonormal QMF of a family, f / norm(f); false if the
+// family / parameter pair is not tabulated.
+bool on_filter(const std::string& type, int par, std::vector<double>* f);
+
+constexpr int kMaxQmf = 32;  // longest even-length tabulated QMF is Coiflet 5 (30 taps)
+struct WvTaps {              // passed by value; taps multiply x[c + j*sf] (analysis) or x[c - t*sf] (synthesis)
+  float a[kMaxQmf];          // lowpass
+  float b[kMaxQmf];          // highpass
+  int lh;
+};
+// Analysis taps of mrdwt_r.h:118-125 / mdwt_r.h:113-120 in the form used by
+// the kernels: lo = sum_j a[j] x[c + j sf], hi = sum_j b[j] x[c + j sf].
+WvTaps analysis_taps(const std::vector<double>& h);
+// Synthesis taps of mirdwt_r.h:125-130: x = sum_t a[t] lo[c - t sf] + b[t] hi[c - t sf].
+WvTaps synthesis_taps(const std::vector<double>& h);
+
+struct WvPlanes {   // one level of n items (item strides in floats)
+  const float* cur; size_t s_cur;   // level input (x, or the previous level's lowpass)
+  float* yl; size_t s_yl;           // lowpass output
+  float* yh; size_t s_yh;           // this level's three planes [LH, HL, HH]
+};
+// mrdwt, one level: columns into yh planes 1 (lowpass) and 0 (highpass), then
+// rows in place: LL -> yl, HL -> 1, LH -> 0, HH -> 2.  thr (n floats, or
+// NULL) hard-thresholds the three highpass planes: c * (|c| > thr[item]).
+cudaError_t launch_rdwt_level(const WvPlanes& P, int n, int H, int W, int sf, const WvTaps& t, const float* thr,
+                              cudaStream_t st);
+// mirdwt, one level: rows (LL, HL) -> tl, (LH, HH) -> th; columns (tl, th) -> x.
+// tl / th may be the level's HL / LH planes (the coefficients are then consumed).
+cudaError_t launch_irdwt_level(const float* ll, size_t s_ll, const float* yh, size_t s_yh, float* tl, float* th,
+                               size_t s_t, float* x, size_t s_x, int n, int H, int W, int sf, const WvTaps& t,
+                               cudaStream_t st);
+bool rdwt_width_supported(int W);
+// TVCorrection (separate.m:268-276): Haar mrdwt of one level, soft threshold
+// gamma on the three highpass planes, mirdwt -- fused into one 3 x 3 stencil.
+cudaError_t launch_tv_haar(const float* x, float* y, size_t stride, int n, int H, int W, float a, float gamma,
+                           cudaStream_t st);
+// mdwt_r.h:102-176 with L = 1, HH quadrant only, FP64: hh[k][l] =
+// sum_ij b[i] b[j] x[2k + i][2l + j] (periodic), (H/2) x (W/2).
+cudaError_t launch_dwt_hh(const float* x, int H, int W, const double* b, int lh, double* hh, cudaStream_t st);
+// separate.m:146-155 on n items: r = (img - p1) - p2; ra1 = p1 + r; ra2 = p2 + r.
+cudaError_t launch_sep_residual(const float* img, const float* p1, const float* p2, float* ra1, float* ra2,
+                                size_t n, cudaStream_t st);
+
 // error reporting
 void set_error(const std::string& msg);
 

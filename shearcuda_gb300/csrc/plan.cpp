@@ -619,8 +619,8 @@ namespace {
 // atrousdec.m:19-51 on the device for n items: x[i] -> y(i, 0) lowpass,
 // y(i, 1..nlev) bandpass coarse -> fine; y(i, k) = ybase[i] + k * HW.
 nsst_status run_atrousdec(nsst_plan* p, int n, const float* const* x, float* const* ybase, float* lowpass0,
-                          cudaStream_t st) {
-  const int H = p->H, W = p->W, L = p->nlev;
+                          cudaStream_t st, int levels = 0) {
+  const int H = p->H, W = p->W, L = levels > 0 ? levels : p->nlev;
   const size_t HW = (size_t)H * W;
   static const char* kHi[] = {"atrous_dec_h1_M1",  "atrous_dec_h1_M2",  "atrous_dec_h1_M4",  "atrous_dec_h1_M8",
                               "atrous_dec_h1_M16", "atrous_dec_h1_M32", "atrous_dec_h1_M64", "atrous_dec_h1_M128"};
@@ -661,8 +661,8 @@ nsst_status run_atrousdec(nsst_plan* p, int n, const float* const* x, float* con
 // atrousrec.m:18-41 on the device for n items: y(i, k) = ybase[i] + k*HW,
 // except that low[i] (if given) replaces y(i, 0).
 nsst_status run_atrousrec(nsst_plan* p, int n, const float* const* ybase, const float* const* low, float* const* out,
-                          cudaStream_t st) {
-  const int H = p->H, W = p->W, L = p->nlev;
+                          cudaStream_t st, int levels = 0) {
+  const int H = p->H, W = p->W, L = levels > 0 ? levels : p->nlev;
   const size_t HW = (size_t)H * W;
   static const char* kRec[] = {"atrous_rec_M1",  "atrous_rec_M2",  "atrous_rec_M4",  "atrous_rec_M8",
                                "atrous_rec_M16", "atrous_rec_M32", "atrous_rec_M64", "atrous_rec_M128"};
@@ -718,7 +718,8 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 // leaving the pre-threshold band spectra (and the pyramid's lowpass) for
 // nsst_denoise_tau_backward_saved.
 nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* const* out, int mode, bool lowpass_th,
-                            cudaStream_t st, bool keep = false) {
+                            cudaStream_t st, bool keep = false, const float* thr = nullptr) {
+  const float* TH = thr ? thr : p->th;  // [item][band] thresholds on the device
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
@@ -734,12 +735,12 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   timer_mark(p, "band_analysis_cols", st);
   if (keep) {
     NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW,
-                          p->th, mode, st));
+                          TH, mode, st));
     timer_mark(p, "band_rows_threshold", st);
     NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
                           (size_t)H * p->WH, p->twH, st));
   } else {
-    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, p->th,
+    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH,
                           mode, st));
     timer_mark(p, "band_rows_threshold", st);
     NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
@@ -758,7 +759,7 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
     for (int i = 0; i < n; i++) {
       NSST_CUDA(cudaMemcpyAsync(p->rec + i * p->s_rec, p->pyr + i * p->s_pyr, HW * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
-      NSST_CUDA(launch_thresh_bands(p->rec + i * p->s_rec, HW, 1, p->th + (size_t)i * p->nbands, mode, st));
+      NSST_CUDA(launch_thresh_bands(p->rec + i * p->s_rec, HW, 1, TH + (size_t)i * p->nbands, mode, st));
       low[i] = p->rec + i * p->s_rec;
     }
     timer_mark(p, "lowpass_threshold", st);
@@ -850,11 +851,17 @@ nsst_status nsst_thresh_max(nsst_plan* p, float* coeffs, double sigma, const dou
   return NSST_OK;
 }
 
-// re_weight_band.m:23-29: atrousdec, weight per pyramid band, atrousrec
-nsst_status nsst_re_weight_band(nsst_plan* p, const float* x, const double* weights, float* out, void* stream) {
+// re_weight_band.m:23-29 / re_weight_band_cuda.cpp:132-183: atrousdec with
+// nweights - 1 levels, weight per pyramid band, atrousrec
+nsst_status nsst_re_weight_band(nsst_plan* p, const float* x, const double* weights, int nweights, float* out,
+                                void* stream) {
   if (!p || !x || !weights || !out) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  // re_weight_band_cuda.cpp:126-127: at least one band-pass level; the plan's
+  // pyramid buffers hold up to its own level count
+  if (nweights < 2 || nweights > p->nlev + 1)
+    return fail(NSST_ERR_INVALID_ARG, "need 2 to nlevels + 1 weights (nweights - 1 pyramid levels)");
   PlaneWeights w{};
-  for (int k = 0; k <= p->nlev; k++) {
+  for (int k = 0; k < nweights; k++) {
     if (!std::isfinite(weights[k])) return fail(NSST_ERR_INVALID_ARG, "weights must be finite");
     w.w[k] = (float)weights[k];
   }
@@ -863,10 +870,10 @@ nsst_status nsst_re_weight_band(nsst_plan* p, const float* x, const double* weig
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   float* y = p->pyr;  // item 0's pyramid planes: lowpass, then band-pass coarse -> fine
-  NSST_TRY(run_atrousdec(p, 1, &x, &y, nullptr, st));
-  NSST_CUDA(launch_scale_planes(y, (size_t)p->H * p->W, p->nlev + 1, w, st));
+  NSST_TRY(run_atrousdec(p, 1, &x, &y, nullptr, st, nweights - 1));
+  NSST_CUDA(launch_scale_planes(y, (size_t)p->H * p->W, nweights, w, st));
   const float* yc = y;
-  return run_atrousrec(p, 1, &yc, nullptr, &out, st);
+  return run_atrousrec(p, 1, &yc, nullptr, &out, st, nweights - 1);
 }
 
 nsst_status nsst_band_norms(nsst_plan* p, double* E) {
@@ -1620,6 +1627,271 @@ nsst_status nsst_multi_denoise(nsst_multi* m, const nsst_item* items, int n, con
   }
   NSST_CUDA(cudaGraphLaunch(m->exec, st));
   NSST_CUDA(cudaEventRecord(m->finished, st));
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+// ============================================ undecimated wavelets, separation
+namespace {
+
+bool divisible_pow2(int v, int L) { return L >= 1 && L < 30 && v % (1 << L) == 0; }
+
+nsst_status check_rdwt(int n, int H, int W, int lh, int L) {
+  if (n < 1 || n > 65535) return fail(NSST_ERR_INVALID_ARG, "image count outside [1, 65535]");
+  if (lh < 1 || lh > kMaxQmf) return fail(NSST_ERR_INVALID_ARG, "filter length outside [1, 32]");
+  // mrdwt.cpp:94-112: both dimensions must be multiples of 2^L
+  if (H < 1 || W < 1 || !divisible_pow2(H, L) || !divisible_pow2(W, L))
+    return fail(NSST_ERR_INVALID_ARG, "L >= 1 and H, W multiples of 2^L required");
+  if (!rdwt_width_supported(W)) return fail(NSST_ERR_INVALID_ARG, "W above 8192");
+  return NSST_OK;
+}
+
+// mrdwt_r.h:135-208 for n images (x item stride s_x; yl item stride HW; yh
+// item stride 3 L HW); thr (device, n floats) hard-thresholds every highpass
+// plane as it is written (thresh.m:44 with option 1), or NULL.
+nsst_status enqueue_mrdwt(const float* x, size_t s_x, int n, int H, int W, const WvTaps& t, int L, float* yl,
+                          float* yh, const float* thr, cudaStream_t st) {
+  const size_t HW = (size_t)H * W;
+  for (int l = 1; l <= L; l++) {
+    const WvPlanes P{l == 1 ? x : yl, l == 1 ? s_x : HW, yl, HW, yh + (size_t)3 * (l - 1) * HW, (size_t)3 * L * HW};
+    NSST_CUDA(launch_rdwt_level(P, n, H, W, 1 << (l - 1), t, thr, st));
+  }
+  return NSST_OK;
+}
+
+// mirdwt_r.h:148-218 for n images.  scratch == NULL: each level's HL / LH
+// planes take the row pass's outputs (yh is consumed); otherwise scratch holds
+// two planes per image.
+nsst_status enqueue_mirdwt(const float* yl, float* yh, float* scratch, int n, int H, int W, const WvTaps& t, int L,
+                           float* x, cudaStream_t st) {
+  const size_t HW = (size_t)H * W, s_yh = (size_t)3 * L * HW;
+  for (int l = L; l >= 1; l--) {
+    float* lev = yh + (size_t)3 * (l - 1) * HW;
+    float* tl = scratch ? scratch : lev + HW;
+    float* th = scratch ? scratch + HW : lev;
+    const size_t s_t = scratch ? 2 * HW : s_yh;
+    NSST_CUDA(launch_irdwt_level(l == L ? yl : x, HW, lev, s_yh, tl, th, s_t, x, HW, n, H, W, 1 << (l - 1), t, st));
+  }
+  return NSST_OK;
+}
+
+// MAD.m: median(|x - median(x)|) / 0.6745 over the non-NaN values; MATLAB's
+// median averages the two middle values of an even count.
+double median_inplace(std::vector<double>& v) {
+  const size_t m = v.size(), mid = m / 2;
+  std::nth_element(v.begin(), v.begin() + (long)mid, v.end());
+  const double hi = v[mid];
+  if (m % 2) return hi;
+  const double lo = *std::max_element(v.begin(), v.begin() + (long)mid);
+  return (lo + hi) / 2;
+}
+
+double mad(const std::vector<double>& x) {
+  std::vector<double> v;
+  v.reserve(x.size());
+  for (double t : x)
+    if (!std::isnan(t)) v.push_back(t);
+  if (v.empty()) return std::nan("");
+  const double med = median_inplace(v);
+  for (double& t : v) t = std::fabs(t - med);
+  return median_inplace(v) / .6745;
+}
+
+// Stream-ordered device scratch, released (in stream order) on every exit path.
+struct AsyncScratch {
+  void* ptr = nullptr;
+  cudaStream_t st = nullptr;
+  ~AsyncScratch() {
+    if (ptr) cudaFreeAsync(ptr, st);
+  }
+};
+
+nsst_status qmf_vector(const char* type, int par, std::vector<double>* f) {
+  if (!on_filter(type, par, f)) return fail(NSST_ERR_INVALID_ARG, std::string("missing QMF table ") + type);
+  return NSST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_onfilter(const char* type, int par, double* out, int* len) {
+  if (!type || !out || !len) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  std::vector<double> f;
+  if (!on_filter(type, par, &f))
+    return fail(NSST_ERR_INVALID_ARG, std::string("no MakeONFilter table for ") + type + " " + std::to_string(par));
+  if ((int)f.size() > NSST_MAX_QMF) return fail(NSST_ERR_INVALID_ARG, "QMF longer than NSST_MAX_QMF");
+  std::copy(f.begin(), f.end(), out);
+  *len = (int)f.size();
+  return NSST_OK;
+}
+
+nsst_status nsst_mrdwt(const float* x, int n, int H, int W, const double* h, int lh, int L, float* yl, float* yh,
+                       void* stream) {
+  if (!x || !h || !yl || !yh) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_rdwt(n, H, W, lh, L));
+  const WvTaps t = analysis_taps(std::vector<double>(h, h + lh));
+  return enqueue_mrdwt(x, (size_t)H * W, n, H, W, t, L, yl, yh, nullptr, (cudaStream_t)stream);
+}
+
+nsst_status nsst_mirdwt(const float* yl, const float* yh, int n, int H, int W, const double* h, int lh, int L,
+                        float* x, void* stream) {
+  if (!x || !h || !yl || !yh) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_rdwt(n, H, W, lh, L));
+  const WvTaps t = synthesis_taps(std::vector<double>(h, h + lh));
+  cudaStream_t st = (cudaStream_t)stream;
+  AsyncScratch s;
+  s.st = st;
+  NSST_CUDA(cudaMallocAsync(&s.ptr, sizeof(float) * 2 * (size_t)n * H * W, st));
+  // the scratch variant only reads yh
+  return enqueue_mirdwt(yl, const_cast<float*>(yh), (float*)s.ptr, n, H, W, t, L, x, st);
+}
+
+nsst_status nsst_tv_correction(const float* x, int n, int H, int W, double gamma, float* y, void* stream) {
+  if (!x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (x == y) return fail(NSST_ERR_INVALID_ARG, "y must not be x");
+  NSST_TRY(check_rdwt(n, H, W, 2, 1));
+  if (!std::isfinite(gamma) || gamma < 0) return fail(NSST_ERR_INVALID_ARG, "gamma must be finite and >= 0");
+  std::vector<double> haar;
+  NSST_TRY(qmf_vector("Haar", 0, &haar));
+  NSST_CUDA(launch_tv_haar(x, y, (size_t)H * W, n, H, W, (float)haar[0], (float)gamma, (cudaStream_t)stream));
+  return NSST_OK;
+}
+
+// separate.m:41-289 (the GPU branches: re_weight_band_cuda, shear_trans_cuda,
+// thresh_cuda, inverse_shear_cuda, TVCorrection_cuda, mrdwt_cuda /
+// mirdwt_cuda) for n images at once.  Per iteration the shearlet part is the
+// plan's fused dec -> hard threshold -> rec pipeline with thresholds
+// 1.4 delta E_b (lowpass included, thresh.m:29-32 with sc = 1), the wavelet
+// part a Symmlet-4 mrdwt whose highpass planes are thresholded at 1.4 delta
+// as they are written (thresh.m:44), then mirdwt.
+nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int itermax, double stop,
+                          double gamma, const double* coeff, int ncoeff, float* C, float* P,
+                          nsst_separate_info* info, void* stream) {
+  if (!p || !img || !coeff || !C || !P) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "image count outside [1, batch capacity]");
+  if (itermax < 1) return fail(NSST_ERR_INVALID_ARG, "itermax must be >= 1");
+  if (!std::isfinite(stop) || stop <= 0) return fail(NSST_ERR_INVALID_ARG, "stop must be finite and > 0");
+  if (!std::isfinite(gamma) || gamma < 0) return fail(NSST_ERR_INVALID_ARG, "gamma must be finite and >= 0");
+  const int H = p->H, W = p->W, L = level2, nb = p->nbands;
+  const size_t HW = (size_t)H * W;
+  NSST_TRY(check_rdwt(n, H, W, 8, L));
+  if (ncoeff < 2 || ncoeff > p->nlev + 1) return fail(NSST_ERR_INVALID_ARG, "need 2 to nlevels + 1 band weights");
+  cudaStream_t st = (cudaStream_t)stream;
+
+  // separate.m:57-58, 90: Symmlet 4 for the wavelet part, Haar for TV, Daubechies 4 for sigma
+  std::vector<double> qmf, haar, d4;
+  NSST_TRY(qmf_vector("Symmlet", 4, &qmf));
+  NSST_TRY(qmf_vector("Haar", 0, &haar));
+  NSST_TRY(qmf_vector("Daubechies", 4, &d4));
+  const WvTaps ta = analysis_taps(qmf), ts = synthesis_taps(qmf);
+  const int l4 = (int)d4.size();
+  std::vector<double> bd4((size_t)l4);  // mdwt_r.h:118-120: the tap on x[2k + j] is h1[lh-1-j]
+  for (int j = 0; j < l4; j++) {
+    const int i = l4 - 1 - j;
+    bd4[(size_t)j] = (i % 2 == 0) ? -d4[(size_t)i] : d4[(size_t)i];
+  }
+  // separate.m:66: exact band norms
+  std::vector<double> E((size_t)nb);
+  NSST_TRY(nsst_band_norms(p, E.data()));
+
+  // workspace, 256-byte aligned segments
+  auto seg = [](size_t bytes) { return align_up(bytes, 256); };
+  const size_t b_plane = seg(sizeof(float) * n * HW), b_yh = seg(sizeof(float) * n * 3 * L * HW),
+               b_coef = seg(sizeof(float) * nb * HW), b_ths = seg(sizeof(float) * itermax * n * nb),
+               b_thw = seg(sizeof(float) * itermax * n), b_bits = seg(sizeof(unsigned) * 3 * L),
+               b_hh = seg(sizeof(double) * HW / 4);
+  AsyncScratch ws;
+  ws.st = st;
+  NSST_CUDA(cudaMallocAsync(&ws.ptr, 5 * b_plane + b_yh + b_coef + b_ths + b_thw + b_bits + b_hh, st));
+  char* q = (char*)ws.ptr;
+  auto take = [&q](size_t b) {
+    char* r = q;
+    q += b;
+    return r;
+  };
+  float* imgw = (float*)take(b_plane);
+  float* ra1 = (float*)take(b_plane);
+  float* ra2 = (float*)take(b_plane);
+  float* S = (float*)take(b_plane);
+  float* yl = (float*)take(b_plane);
+  float* yh = (float*)take(b_yh);
+  float* coef = (float*)take(b_coef);
+  float* thS = (float*)take(b_ths);
+  float* thW = (float*)take(b_thw);
+  unsigned* bits = (unsigned*)take(b_bits);
+  double* hh = (double*)take(b_hh);
+
+  // separate.m:72-76: band re-weighting
+  for (int i = 0; i < n; i++)
+    NSST_TRY(nsst_re_weight_band(p, img + i * HW, coeff, ncoeff, imgw + i * HW, st));
+
+  std::vector<float> hS((size_t)itermax * n * nb), hW((size_t)itermax * n);
+  std::vector<double> hhh(HW / 4), ones((size_t)p->nlev + 1, 1.0);
+  std::vector<unsigned> hb((size_t)3 * L);
+  for (int i = 0; i < n; i++) {
+    const float* xi = imgw + i * HW;
+    // separate.m:82-102: sigma = MAD of the HH quadrant of a one-level Daubechies-4 mdwt
+    NSST_CUDA(launch_dwt_hh(xi, H, W, bd4.data(), l4, hh, st));
+    NSST_CUDA(cudaMemcpyAsync(hhh.data(), hh, sizeof(double) * hhh.size(), cudaMemcpyDeviceToHost, st));
+    NSST_CUDA(cudaStreamSynchronize(st));
+    const double sigma = mad(hhh), stop_i = stop * sigma;
+    // separate.m:104-114: buff(1), the largest |c_b| / E_b of the shearlet coefficients
+    double b1 = 0.0;
+    NSST_TRY(nsst_shear_trans(p, xi, coef, st));
+    NSST_TRY(nsst_thresh_max(p, coef, 0.0, ones.data(), E.data(), NSST_THRESH_HARD, &b1, st));
+    // separate.m:119-126: buff(2) = max |yh| of the Symmlet-4 mrdwt
+    NSST_TRY(enqueue_mrdwt(xi, HW, 1, H, W, ta, L, yl, yh, nullptr, st));
+    NSST_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * 3 * L, st));
+    NSST_CUDA(launch_plane_maxabs(yh, HW, 3 * L, bits, kRedBlocks, st));
+    NSST_CUDA(cudaMemcpyAsync(hb.data(), bits, sizeof(unsigned) * hb.size(), cudaMemcpyDeviceToHost, st));
+    NSST_CUDA(cudaStreamSynchronize(st));
+    float m2 = 0.0f;
+    for (unsigned u : hb) {
+      float v;
+      std::memcpy(&v, &u, sizeof(float));
+      m2 = std::max(m2, v);
+    }
+    const double b2 = m2;
+    // separate.m:128-131: exponential decrease from deltamax to stop
+    const double deltamax = std::min(b1, b2);
+    const double lambda = std::pow(deltamax / stop_i, 1.0 / (1.0 - itermax));
+    double delta = deltamax;
+    for (int k = 0; k < itermax; k++) {
+      const double t = 1.4 * delta;  // separate.m:169, 215
+      for (int b = 0; b < nb; b++) hS[((size_t)k * n + i) * nb + b] = (float)(1.0 * t * E[(size_t)b]);
+      hW[(size_t)k * n + i] = (float)t;
+      delta = delta * lambda;  // separate.m:253
+    }
+    if (info) info[i] = nsst_separate_info{sigma, stop_i, b1, b2, deltamax, lambda};
+  }
+  NSST_CUDA(cudaMemcpyAsync(thS, hS.data(), sizeof(float) * hS.size(), cudaMemcpyHostToDevice, st));
+  NSST_CUDA(cudaMemcpyAsync(thW, hW.data(), sizeof(float) * hW.size(), cudaMemcpyHostToDevice, st));
+  NSST_CUDA(cudaStreamSynchronize(st));  // the host tables may go out of scope
+
+  // separate.m:144-256: the relaxation loop, queued without host waits
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;
+  timer_begin(p, st);
+  std::vector<const float*> xs((size_t)n);
+  std::vector<float*> os((size_t)n);
+  for (int i = 0; i < n; i++) {
+    xs[(size_t)i] = ra1 + i * HW;
+    os[(size_t)i] = S + i * HW;
+  }
+  NSST_CUDA(cudaMemsetAsync(C, 0, sizeof(float) * n * HW, st));
+  NSST_CUDA(cudaMemsetAsync(P, 0, sizeof(float) * n * HW, st));
+  for (int k = 0; k < itermax; k++) {
+    NSST_CUDA(launch_sep_residual(imgw, C, P, ra1, ra2, n * HW, st));
+    // curves: shearlet hard threshold, then TV correction
+    NSST_TRY(enqueue_denoise(p, n, xs.data(), os.data(), NSST_THRESH_HARD, true, st, false,
+                             thS + (size_t)k * n * nb));
+    NSST_CUDA(launch_tv_haar(S, C, HW, n, H, W, (float)haar[0], (float)gamma, st));
+    // points: wavelet hard threshold
+    NSST_TRY(enqueue_mrdwt(ra2, HW, n, H, W, ta, L, yl, yh, thW + (size_t)k * n, st));
+    NSST_TRY(enqueue_mirdwt(yl, yh, nullptr, n, H, W, ts, L, P, st));
+  }
   return NSST_OK;
 }
 

@@ -249,14 +249,14 @@ def thresh_cuda(coeff, sigma, K, scalars, shear, mode=THRESH_HARD, stream=None, 
 
 def re_weight_band(P, coeff, shear, out=None, stream=None):
     """Image re-synthesised with a weight per pyramid band (re_weight_band.m):
-    coeff[0] lowpass, coeff[1:] band-pass coarse to fine (len = nlevels + 1)."""
+    len(coeff) - 1 pyramid levels (at most the plan's), coeff[0] on the
+    lowpass, coeff[1:] on the band-pass images coarse to fine."""
     w = np.ascontiguousarray(coeff, dtype=np.float64).ravel()
-    if w.size != shear.nlevels + 1:
-        raise NsstError(1, 'need %d weights' % (shear.nlevels + 1))
     x = _dev(P, 'P', (shear.H, shear.W))
     if out is None:
         out = torch.empty_like(P)
-    check(lib().nsst_re_weight_band(shear.handle, x, _dptr(w), _dev(out, 'out', (shear.H, shear.W)), _stream(stream)))
+    check(lib().nsst_re_weight_band(shear.handle, x, _dptr(w), int(w.size), _dev(out, 'out', (shear.H, shear.W)),
+                                    _stream(stream)))
     return out
 
 

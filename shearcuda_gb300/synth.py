@@ -82,3 +82,32 @@ def noisy_volume(shape, sigma, seed):
     clean = clean_volume(tuple(shape), rng)
     noisy = clean + sigma * rng.standard_normal(tuple(shape))
     return clean, noisy
+
+
+def points_and_curves(N, npoints=150, sigma=20.0, seed=0, amp=255.0):
+    """A square test image of side N for the points / curves separation: a
+    smooth bump as background, straight lines of several slopes and a ring
+    (all two pixels wide, value amp), npoints isolated one-pixel points (value
+    amp), plus N(0, sigma^2) noise.  Returns (clean, noisy) float64.  The
+    separation demo's own generator is of this kind (curves, points, noise)
+    at N = 256 with 150 points and sigma 20."""
+    rng = np.random.default_rng(seed)
+    r, c = np.mgrid[0:N, 0:N].astype(np.float64) / N
+    img = amp / (1.0 + np.hypot(r - 0.15, c - 0.1)) ** 3 * 0.8
+    cols = np.arange(N)
+    for _ in range(5):  # lines row = slope * col + offset, or transposed
+        slope = rng.uniform(-2.5, 2.5)
+        off = rng.uniform(0.1, 0.9) * N - slope * N / 2
+        rows = np.round(slope * cols + off).astype(int)
+        for d in (0, 1):
+            ok = (rows + d >= 0) & (rows + d < N)
+            if rng.random() < 0.5:
+                img[rows[ok] + d, cols[ok]] = amp
+            else:
+                img[cols[ok], rows[ok] + d] = amp
+    rad = np.hypot(r - 0.5, c - 0.5) * N
+    ring = rng.uniform(0.25, 0.4) * N
+    img[(rad > ring) & (rad < ring + 2.0)] = amp
+    pts = rng.integers(0, N, size=(npoints, 2))
+    img[pts[:, 0], pts[:, 1]] = amp
+    return img, img + sigma * rng.standard_normal((N, N))

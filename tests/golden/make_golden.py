@@ -23,6 +23,12 @@ It writes two kinds of fixtures, both small enough to commit:
   the demo's data size), flattened to the band order level, cone, l2, l1.
   They pin the 3-D pyramid windows, the Meyer filters and the band order to
   within the Monte-Carlo and data-size spread.
+* ``rwt_ref_cases.npz``: inputs and outputs of the reference's Rice Wavelet
+  Toolbox templates (``shearcuda/src/mrdwt_r.h``, ``mirdwt_r.h``,
+  ``mdwt_r.h``, compiled unchanged behind ``oracle/rwt_ref_glue.cpp``) on
+  seeded random images with the MakeONFilter filters the separation loop uses
+  (Symmlet 4, Haar, Daubechies 4) and a long one (Coiflet 2), including a
+  level whose dilated chain is shorter than the filter.
 """
 import argparse
 import json
@@ -143,6 +149,29 @@ def scalar_tables3(reference):
     return out
 
 
+RWT_SHAPES = [(8, 16, 'Symmlet', 4, 3), (8, 8, 'Symmlet', 4, 3), (16, 8, 'Haar', 0, 2),
+              (16, 16, 'Daubechies', 4, 2), (16, 16, 'Coiflet', 2, 2)]
+
+
+def rwt_cases(seed=4321):
+    sys.path.insert(0, ROOT)
+    from oracle import rwt, rwt_ref  # noqa: E402
+    if not rwt_ref.available():
+        raise SystemExit('oracle/_ref not built: run python oracle/build_oracle.py first')
+    rng = np.random.default_rng(seed)
+    cases = {'n': np.array([len(RWT_SHAPES)])}
+    for i, (H, W, fam, par, L) in enumerate(RWT_SHAPES):
+        h = rwt.make_on_filter(fam, par)
+        x = rng.standard_normal((H, W))
+        yl, yh = rwt_ref.mrdwt(x, h, L)
+        # the inverse of perturbed coefficients, so that mirdwt is pinned off the identity
+        yh2 = yh + 0.1 * rng.standard_normal(yh.shape)
+        cases.update({'x_%d' % i: x, 'h_%d' % i: h, 'L_%d' % i: np.array([L]), 'yl_%d' % i: yl, 'yh_%d' % i: yh,
+                      'yh2_%d' % i: yh2, 'inv_%d' % i: rwt_ref.mirdwt(yl, yh2, h, L),
+                      'mdwt_%d' % i: rwt_ref.mdwt(x, h, min(L, 2))})
+    return cases
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference')
@@ -153,6 +182,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, 'atrousc_ref_cases.npz'), **atrousc_cases())
     with open(os.path.join(HERE, 'nsst3_scalar_tables.json'), 'w') as f:
         json.dump(scalar_tables3(args.reference), f, indent=1)
+    np.savez_compressed(os.path.join(HERE, 'rwt_ref_cases.npz'), **rwt_cases())
     print('wrote', os.listdir(HERE))
 
 

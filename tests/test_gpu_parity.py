@@ -223,5 +223,10 @@ def test_re_weight_band_matches_oracle(built_lib, cuda):
     assert rel_l2(got, ref) <= 1e-5
     ones = sc.re_weight_band(x, [1.0] * 5, shear).cpu().numpy()
     assert rel_l2(ones, noisy) <= 1e-5  # perfect reconstruction
-    with pytest.raises(sc.NsstError):
-        sc.re_weight_band(x, [1.0] * 4, shear)
+    # fewer levels than the plan: the separation demo's four weights (three levels)
+    w3 = [0.1, 0.1, 1.5, 1.5]
+    got3 = sc.re_weight_band(x, w3, shear).cpu().numpy().astype(np.float64)
+    assert rel_l2(got3, nsst2d.re_weight_band(noisy.astype(np.float32).astype(np.float64), w3)) <= 1e-5
+    for bad in ([1.0], [1.0] * 6):
+        with pytest.raises(sc.NsstError):
+            sc.re_weight_band(x, bad, shear)

@@ -56,6 +56,34 @@ def test_level_spectra_match_oracle(built_lib, HW):
         assert np.abs(got - ref).max() < 1e-13
 
 
+# Sizes that are not powers of two put Meyer-grid coordinates on rounding
+# boundaries: the host build must not fuse multiply-adds (aarch64 gcc does by
+# default), or the filter bank differs between machines.
+HOST_SPECTRA_CASES = [(48, 4), (80, 3), (80, 4), (40, 2)]
+
+
+def _check_host_spectra(n1, level):
+    import shearcuda_gb300 as sc
+    np.testing.assert_allclose(sc.shearing_filters(n1, level), nsst2d.shearing_filters_Myer(n1, level),
+                               rtol=0, atol=1e-15)
+    got = sc.level_spectra(n1, level, 256, 256)
+    ref = nsst2d.shear_spectra(256, 256, [level], [n1])[0][:, :, :129]
+    assert np.abs(got - ref).max() < 1e-13
+
+
+@pytest.mark.parametrize('n1,level', HOST_SPECTRA_CASES)
+def test_host_filters_non_power_of_two_sizes(built_lib, n1, level):
+    _check_host_spectra(n1, level)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('n1,level', HOST_SPECTRA_CASES)
+def test_host_filters_non_power_of_two_sizes_on_gpu_machine(built_lib, n1, level):
+    # the same host-only check, run with the GPU suite so that the GPU
+    # machine's own build of the host code is compared with the oracle
+    _check_host_spectra(n1, level)
+
+
 def test_status_codes_without_gpu(built_lib):
     import shearcuda_gb300 as sc
     from shearcuda_gb300._lib import NsstError
