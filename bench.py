@@ -43,8 +43,9 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
     ap.add_argument('--batch', type=int, default=BATCH, help='images per batched pass (smaller for profiling)')
-    ap.add_argument('--workload', default='2d', choices=['2d', 'v3'],
-                    help="v3: only the 3-D volume extra (for profiling its kernels)")
+    ap.add_argument('--workload', default='2d', choices=['2d', 'v3', 'sep'],
+                    help="v3 / sep: only the 3-D volume or the image-separation extra (for profiling their kernels)")
+    ap.add_argument('--sep-batch', type=int, default=8, help='images per batched separation call')
     ap.add_argument('--v3-sizes', default='128,192', help='volume edge lengths of the v3 workload')
     ap.add_argument('--v3-batch', type=int, default=4, help='volumes per batched v3 pass')
     return ap.parse_args()
@@ -269,6 +270,83 @@ def volume_bench(sc, torch, dev, stream, flush, rank, reps=3, sizes=(128, 192), 
     return out
 
 
+SEP_DCOMP, SEP_DSIZE, SEP_N = [3, 3, 4, 4], [80, 80, 80, 80], 256
+SEP_ARGS = dict(level2=4, itermax=10, stop=3.0, gamma=3.0, coeff=[.1, .1, 1.5, 1.5])
+
+
+def separation_bench(sc, torch, dev, stream, flush, rank, reps=5, batch=8, cpu_sample=True):
+    """The separation demo's configuration (separation_demo01_gpu.m:19-41, 80):
+    256x256 points + curves images (150 points, sigma 20), shearlets dcomp
+    [3 3 4 4] dsize [80 80 80 80], level2 4, itermax 10, stop 3, gamma 3,
+    coeff [.1 .1 1.5 1.5]; one batched nsst_separate call per step (setup with
+    its host reductions + the 10 iterations)."""
+    from shearcuda_gb300.synth import points_and_curves
+    host = [points_and_curves(SEP_N, npoints=150, sigma=20.0, seed=700 * rank + i)[1].astype(np.float32)
+            for i in range(batch)]
+    plan = sc.prepare_shearing_filters_cuda(SEP_DCOMP, SEP_DSIZE, SEP_N, SEP_N, batch=batch)
+    x = torch.tensor(np.stack(host), device=dev)
+    out = {'batch': batch, 'H': SEP_N, 'W': SEP_N, 'dcomp': SEP_DCOMP, 'dsize': SEP_DSIZE, **SEP_ARGS}
+    c0 = sc.launch_count()
+    sc.separate(x, shear=plan, **SEP_ARGS)
+    torch.cuda.synchronize()
+    out['kernels_per_call'] = sc.launch_count() - c0
+    for _ in range(2):
+        sc.separate(x, shear=plan, **SEP_ARGS)
+    torch.cuda.synchronize()
+    tt = 0.0
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sc.separate(x, shear=plan, **SEP_ARGS)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tt += e0.elapsed_time(e1)
+    out['ms_per_call'] = tt / reps
+    out['images_per_s'] = batch / (out['ms_per_call'] / 1000.0)
+    # split: one iteration's cost from itermax 10 vs 1, the rest is the setup
+    one = dict(SEP_ARGS, itermax=1)
+    sc.separate(x, shear=plan, **one)
+    t1 = 0.0
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sc.separate(x, shear=plan, **one)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t1 += e0.elapsed_time(e1)
+    t1 /= reps
+    out['ms_per_iteration'] = (out['ms_per_call'] - t1) / (SEP_ARGS['itermax'] - 1)
+    out['ms_setup'] = t1 - out['ms_per_iteration']
+    # e2e: pinned host images in, both parts out, inside the timed region
+    pin_in = torch.from_numpy(np.stack(host)).pin_memory()
+    pin_c = torch.empty_like(pin_in).pin_memory()
+    pin_p = torch.empty_like(pin_in).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        x.copy_(pin_in, non_blocking=True)
+        C, P, _ = sc.separate(x, shear=plan, **SEP_ARGS)
+        pin_c.copy_(C, non_blocking=True)
+        pin_p.copy_(P, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / reps
+    out['e2e'] = {'value': batch / (e2e_ms / 1000.0), 'unit': 'images/s', 'ms_per_call': e2e_ms,
+                  'h2d_bytes_per_step': batch * SEP_N * SEP_N * 4, 'd2h_bytes_per_step': 2 * batch * SEP_N * SEP_N * 4}
+    if cpu_sample and rank == 0:
+        from oracle import rwt
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        rwt.separate(host[0].astype(np.float64), SEP_DCOMP, SEP_DSIZE, nthreads=cores, **SEP_ARGS)
+        dt = time.perf_counter() - t0
+        out['cpu_baseline'] = {'value': 1.0 / dt, 'unit': 'images/s', 'cores': cores, 'kind': 'port',
+                               'sample': 'one 256x256 image through the FP64 oracle of separate.m (%.1f s)' % dt}
+    plan.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     import shearcuda_gb300 as sc
@@ -485,6 +563,9 @@ def run_gpu(args):
         # bands, numDir 2, 2, 4), hard threshold, forward vs forward + adjoint
         line['volume_v3'] = volume_bench(sc, torch, dev, stream, flush, rank)
 
+        # ---- image separation (points / curves), the demo's configuration, batch of 8
+        line['separation'] = separation_bench(sc, torch, dev, stream, flush, rank, batch=args.sep_batch)
+
     if rank == 0:
         cb = cpu_baseline()
         line['cpu_baseline'] = cb
@@ -506,6 +587,16 @@ def run_v3(args):
     print(json.dumps({'workload': 'v3', 'volume_v3': res}), flush=True)
 
 
+def run_sep(args):
+    import torch
+    import shearcuda_gb300 as sc
+    dev = torch.device('cuda', 0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    res = separation_bench(sc, torch, dev, torch.cuda.current_stream(), flush, 0, reps=max(1, args.steps),
+                           batch=args.sep_batch, cpu_sample=False)
+    print(json.dumps({'workload': 'sep', 'separation': res}), flush=True)
+
+
 def main():
     args = parse()
     global BATCH
@@ -514,6 +605,8 @@ def main():
         run_reference(args)
     elif args.workload == 'v3':
         run_v3(args)
+    elif args.workload == 'sep':
+        run_sep(args)
     else:
         run_gpu(args)
 

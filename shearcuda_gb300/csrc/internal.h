@@ -123,6 +123,10 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
                                  void* dst_base, const float2* twWh, const float2* twW, const float* tau, int mode,
                                  float* partials, size_t pstride, cudaStream_t st);
 cudaError_t launch_thresh_bands(float* data, size_t n, int nbands, const float* thr, int mode, cudaStream_t st);
+// Band row pass without a store: C2R of each band's rows and max |c| into
+// bits[th_index] (float bit patterns, atomicMax; bits zeroed first).
+cudaError_t launch_rows_max(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                            const float2* twWh, const float2* twW, unsigned* bits, cudaStream_t st);
 // per-plane reductions (k_reduce.cu): FP64 partial sums of squares,
 // partial[plane * blocks + block]; bit patterns of the largest |x| (maxbits zeroed first)
 cudaError_t launch_plane_sumsq(const float* data, size_t n, int nplanes, double* partial, int blocks,
@@ -275,9 +279,11 @@ bool rdwt_width_supported(int W);
 // gamma on the three highpass planes, mirdwt -- fused into one 3 x 3 stencil.
 cudaError_t launch_tv_haar(const float* x, float* y, size_t stride, int n, int H, int W, float a, float gamma,
                            cudaStream_t st);
-// mdwt_r.h:102-176 with L = 1, HH quadrant only, FP64: hh[k][l] =
-// sum_ij b[i] b[j] x[2k + i][2l + j] (periodic), (H/2) x (W/2).
-cudaError_t launch_dwt_hh(const float* x, int H, int W, const double* b, int lh, double* hh, cudaStream_t st);
+// mdwt_r.h:102-176 with L = 1, HH quadrant only, FP64, for n images (item
+// stride `stride` floats): hh[item][k][l] = sum_ij b[i] b[j] x[2k + i][2l + j]
+// (periodic), (H/2) x (W/2) per image.
+cudaError_t launch_dwt_hh(const float* x, size_t stride, int n, int H, int W, const double* b, int lh, double* hh,
+                          cudaStream_t st);
 // separate.m:146-155 on n items: r = (img - p1) - p2; ra1 = p1 + r; ra2 = p2 + r.
 cudaError_t launch_sep_residual(const float* img, const float* p1, const float* p2, float* ra1, float* ra2,
                                 size_t n, cudaStream_t st);

@@ -222,6 +222,34 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_thresh
   r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
 
+// Band maxima (thresh.m's opt == 1 maximum with a zero threshold): C2R of the
+// CTA's rows of one band, then max |c| over them into bits[job.th_index] as
+// the bit pattern of a non-negative float (atomicMax; bits zeroed first).
+template <int WH>
+__global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_max(const RowJob* __restrict__ jobs, int n_active,
+                                                             const float2* src_base,
+                                                             const float2* __restrict__ twWh,
+                                                             const float2* __restrict__ twW,
+                                                             unsigned* __restrict__ bits) {
+  using C = RowCfg<WH>;
+  extern __shared__ float2 smem[];
+  float2* A = smem;
+  const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  __syncthreads();
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW}, SmemSt<C::RS>{A});
+  __syncthreads();
+  float m = 0.0f;
+  for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {  // SmemSt wrote (i, s) at i * RS + s
+    const float2 v = A[e];
+    m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&bits[job.th_index], __float_as_uint(m));
+}
+
 // Backward band row pass (adjoint of the threshold step, rows of one band):
 // coefficients c = C2R(Qc) are recomputed, g = C2R(Qg) is the gradient w.r.t.
 // the thresholded coefficients; out = R2C(g * 1[|c| > t]) replaces Qg, and
@@ -440,6 +468,7 @@ cudaError_t prepare_row_kernels(int wh) {
     cudaError_t e = opt_in(k_rows_fwd<n>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
+    if (e == cudaSuccess) e = opt_in(k_rows_max<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * sm / 2);         \
     return e;                                                                 \
   }
@@ -488,6 +517,26 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
     else                                                                               \
       k_rows_thresh<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
+  }
+    NSST_ROW_SIZES(CASE)
+#undef CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_rows_max(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                            const float2* twWh, const float2* twW, unsigned* bits, cudaStream_t st) {
+  const int WH = W / 2;
+  if (njobs == 0) return cudaSuccess;
+  count_launch();
+  const float2* sb = static_cast<const float2*>(src_base);
+  switch (WH) {
+#define CASE(n)                                                                                   \
+  case n: {                                                                                       \
+    constexpr size_t sm = RowCfg<n>::smem() / 2;                                                  \
+    k_rows_max<n><<<dim3(H / RowCfg<n>::RS, njobs), RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, twWh, twW, bits); \
+    return cudaGetLastError();                                                                    \
   }
     NSST_ROW_SIZES(CASE)
 #undef CASE

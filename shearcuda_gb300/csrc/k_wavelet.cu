@@ -206,10 +206,12 @@ struct DTaps {
   double b[kMaxQmf];
   int lh;
 };
-__global__ void __launch_bounds__(256) k_dwt_hh(const float* __restrict__ x, int H, int W, DTaps t,
-                                                double* __restrict__ hh) {
+__global__ void __launch_bounds__(256) k_dwt_hh(const float* __restrict__ xb, size_t stride, int H, int W, DTaps t,
+                                                double* __restrict__ hhb) {
   const int l = blockIdx.x * 32 + threadIdx.x, k = blockIdx.y * 8 + threadIdx.y;
   if (l >= W / 2 || k >= H / 2) return;
+  const float* x = xb + blockIdx.z * stride;
+  double* hh = hhb + (size_t)blockIdx.z * (H / 2) * (W / 2);
   double acc = 0.0;
   int rr = 2 * k;
   for (int i = 0; i < t.lh; i++) {
@@ -291,13 +293,14 @@ cudaError_t launch_tv_haar(const float* x, float* y, size_t stride, int n, int H
   return cudaGetLastError();
 }
 
-cudaError_t launch_dwt_hh(const float* x, int H, int W, const double* b, int lh, double* hh, cudaStream_t st) {
-  if (lh < 1 || lh > kMaxQmf) return cudaErrorInvalidValue;
+cudaError_t launch_dwt_hh(const float* x, size_t stride, int n, int H, int W, const double* b, int lh, double* hh,
+                          cudaStream_t st) {
+  if (lh < 1 || lh > kMaxQmf || n < 1 || n > 65535) return cudaErrorInvalidValue;
   DTaps t{};
   t.lh = lh;
   for (int i = 0; i < lh; i++) t.b[i] = b[i];
   count_launch();
-  k_dwt_hh<<<dim3((W / 2 + 31) / 32, (H / 2 + 7) / 8), dim3(32, 8), 0, st>>>(x, H, W, t, hh);
+  k_dwt_hh<<<dim3((W / 2 + 31) / 32, (H / 2 + 7) / 8, n), dim3(32, 8), 0, st>>>(x, stride, H, W, t, hh);
   return cudaGetLastError();
 }
 

@@ -72,6 +72,11 @@ struct nsst_plan {
   float* th = nullptr;     // B x nbands thresholds
   float* th_host = nullptr;  // pinned staging for th
   cudaEvent_t th_done = nullptr;
+  // separation loop: the wavelet branch runs on a second stream beside the shearlet branch
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  void* sep_host = nullptr;  // pinned staging of the setup's reductions
+  size_t sep_host_bytes = 0;
 
   RowJob* j_rows_lev_fwd = nullptr;   // pyr[1..] -> lev           (B*nlev)
   ColJob* j_cols_lev = nullptr;       // lev in place              (B*nlev)
@@ -84,6 +89,7 @@ struct nsst_plan {
 
   std::vector<double> scalars;
   bool has_scalars = false;
+  std::vector<double> norms;  // exact band norms (nsst_band_norms), computed on first use
 
   // CUDA graph replay of the batched denoise launch sequence
   bool use_graphs = false;
@@ -556,6 +562,10 @@ nsst_status nsst_plan_destroy(nsst_plan* p) {
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->th_done) cudaEventDestroy(p->th_done);
+  if (p->side) cudaStreamDestroy(p->side);
+  if (p->fork_ev) cudaEventDestroy(p->fork_ev);
+  if (p->join_ev) cudaEventDestroy(p->join_ev);
+  if (p->sep_host) cudaFreeHost(p->sep_host);
   if (p->th_host) cudaFreeHost(p->th_host);
   if (p->garena) cudaFree(p->garena);
   if (p->arena) cudaFree(p->arena);
@@ -767,6 +777,49 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   return run_atrousrec(p, n, yr.data(), low.data(), out, st);
 }
 
+// Per image the largest |c| of every coefficient plane of shear_trans(x_i),
+// as float bit patterns in bits[i * nbands + b] (zeroed here): the pyramid
+// and the directional analysis of the fused pipeline, then band rows C2R'd
+// and reduced without being stored; the lowpass plane reduced directly.  The
+// plan must be locked.
+nsst_status enqueue_band_maxima(nsst_plan* p, int n, const float* const* x, unsigned* bits, cudaStream_t st) {
+  char* A = p->arena;
+  float2* A2 = (float2*)A;
+  const int B = p->B, H = p->H, W = p->W;
+  const size_t HW = (size_t)H * W;
+  std::vector<float*> ys(n);
+  for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
+  NSST_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * n * p->nbands, st));
+  NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
+  NSST_CUDA(launch_rows_max(p->j_rows_bands, B * p->ndir_total, n, H, W, A, p->twWh, p->twW, bits, st));
+  for (int i = 0; i < n; i++)
+    NSST_CUDA(launch_plane_maxabs(ys[(size_t)i], HW, 1, bits + (size_t)i * p->nbands, kRedBlocks, st));
+  return NSST_OK;
+}
+
+// shear_trans of one image into nbands caller planes; the plan must be locked.
+nsst_status enqueue_shear_trans(nsst_plan* p, const float* x, float* coeffs, cudaStream_t st) {
+  char* A = p->arena;
+  float2* A2 = (float2*)A;
+  float* yb = p->pyr;
+  // the lowpass goes straight to coefficient plane 0
+  NSST_TRY(run_atrousdec(p, 1, &x, &yb, coeffs, st));
+  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+                        st));
+  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
+  // the job list covers every item; n_active = 1 skips the others
+  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, p->B * p->ndir_total, 1, p->H, p->W, A2, A2, p->spec, 0,
+                        p->twH, st));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Inv, p->j_band_to_coeff, p->ndir_total, 1, p->H, p->W, A, coeffs, p->twWh, p->twW,
+                        nullptr, 0, st));
+  timer_mark(p, "band_rows_inv", st);
+  return NSST_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -797,22 +850,7 @@ nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* 
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
-  char* A = p->arena;
-  float2* A2 = (float2*)A;
-  float* yb = p->pyr;
-  // the lowpass goes straight to coefficient plane 0
-  NSST_TRY(run_atrousdec(p, 1, &x, &yb, coeffs, st));
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
-                        st));
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
-  // the job list covers every item; n_active = 1 skips the others
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, p->B * p->ndir_total, 1, p->H, p->W, A2, A2, p->spec, 0,
-                        p->twH, st));
-  timer_mark(p, "band_analysis_cols", st);
-  NSST_CUDA(launch_rows(RowOp::Inv, p->j_band_to_coeff, p->ndir_total, 1, p->H, p->W, A, coeffs, p->twWh, p->twW,
-                        nullptr, 0, st));
-  timer_mark(p, "band_rows_inv", st);
-  return NSST_OK;
+  return enqueue_shear_trans(p, x, coeffs, st);
 }
 
 nsst_status nsst_thresh(nsst_plan* p, float* coeffs, double sigma, const double* K, const double* scalars, int mode,
@@ -878,6 +916,13 @@ nsst_status nsst_re_weight_band(nsst_plan* p, const float* x, const double* weig
 
 nsst_status nsst_band_norms(nsst_plan* p, double* E) {
   if (!p || !E) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  {
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!p->norms.empty()) {  // deterministic: computed once per plan
+      std::copy(p->norms.begin(), p->norms.end(), E);
+      return NSST_OK;
+    }
+  }
   const size_t HW = (size_t)p->H * p->W;
   // com_norm.m:37-40: X = fftshift(real(ifft2(ones))) * sqrt(HW), an impulse
   // of height sqrt(HW) at (H/2, W/2)
@@ -911,6 +956,8 @@ nsst_status nsst_band_norms(nsst_plan* p, double* E) {
     for (int k = 0; k < kRedBlocks; k++) t += part[(size_t)b * kRedBlocks + k];
     E[b] = std::sqrt(t / (double)HW);
   }
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->norms.assign(E, E + p->nbands);
   return NSST_OK;
 }
 
@@ -1792,19 +1839,20 @@ nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int
     const int i = l4 - 1 - j;
     bd4[(size_t)j] = (i % 2 == 0) ? -d4[(size_t)i] : d4[(size_t)i];
   }
-  // separate.m:66: exact band norms
+  // separate.m:66: exact band norms (cached in the plan after the first call)
   std::vector<double> E((size_t)nb);
   NSST_TRY(nsst_band_norms(p, E.data()));
 
   // workspace, 256-byte aligned segments
   auto seg = [](size_t bytes) { return align_up(bytes, 256); };
+  const size_t nbits = (size_t)n * (nb + 3 * L);
   const size_t b_plane = seg(sizeof(float) * n * HW), b_yh = seg(sizeof(float) * n * 3 * L * HW),
-               b_coef = seg(sizeof(float) * nb * HW), b_ths = seg(sizeof(float) * itermax * n * nb),
-               b_thw = seg(sizeof(float) * itermax * n), b_bits = seg(sizeof(unsigned) * 3 * L),
-               b_hh = seg(sizeof(double) * HW / 4);
+               b_ths = seg(sizeof(float) * itermax * n * nb),
+               b_thw = seg(sizeof(float) * itermax * n), b_bits = seg(sizeof(unsigned) * nbits),
+               b_hh = seg(sizeof(double) * n * (HW / 4));
   AsyncScratch ws;
   ws.st = st;
-  NSST_CUDA(cudaMallocAsync(&ws.ptr, 5 * b_plane + b_yh + b_coef + b_ths + b_thw + b_bits + b_hh, st));
+  NSST_CUDA(cudaMallocAsync(&ws.ptr, 5 * b_plane + b_yh + b_ths + b_thw + b_bits + b_hh, st));
   char* q = (char*)ws.ptr;
   auto take = [&q](size_t b) {
     char* r = q;
@@ -1817,42 +1865,87 @@ nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int
   float* S = (float*)take(b_plane);
   float* yl = (float*)take(b_plane);
   float* yh = (float*)take(b_yh);
-  float* coef = (float*)take(b_coef);
   float* thS = (float*)take(b_ths);
   float* thW = (float*)take(b_thw);
-  unsigned* bits = (unsigned*)take(b_bits);
+  unsigned* bits = (unsigned*)take(b_bits);  // [n][nb] shearlet band maxima, then [n][3L] wavelet plane maxima
   double* hh = (double*)take(b_hh);
 
-  // separate.m:72-76: band re-weighting
-  for (int i = 0; i < n; i++)
-    NSST_TRY(nsst_re_weight_band(p, img + i * HW, coeff, ncoeff, imgw + i * HW, st));
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->saved_n = 0;
+  timer_begin(p, st);
+  if (!p->side) {
+    NSST_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+    NSST_CUDA(cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming));
+    NSST_CUDA(cudaEventCreateWithFlags(&p->join_ev, cudaEventDisableTiming));
+  }
+  const size_t host_bytes = sizeof(double) * n * (HW / 4) + sizeof(unsigned) * nbits;
+  if (p->sep_host_bytes < host_bytes) {
+    if (p->sep_host) cudaFreeHost(p->sep_host);
+    p->sep_host = nullptr;
+    p->sep_host_bytes = 0;
+    NSST_CUDA(cudaMallocHost(&p->sep_host, host_bytes));
+    p->sep_host_bytes = host_bytes;
+  }
+  double* hhh = (double*)p->sep_host;
+  unsigned* hb = (unsigned*)(hhh + (size_t)n * (HW / 4));
+  std::vector<const float*> xs((size_t)n);
+  std::vector<float*> os((size_t)n), ys((size_t)n);
+  // separate.m:72-76: band re-weighting of the n images (ncoeff - 1 pyramid levels)
+  PlaneWeights w{};
+  for (int k = 0; k < ncoeff; k++) {
+    if (!std::isfinite(coeff[k])) return fail(NSST_ERR_INVALID_ARG, "band weights must be finite");
+    w.w[k] = (float)coeff[k];
+  }
+  for (int i = 0; i < n; i++) {
+    xs[(size_t)i] = img + i * HW;
+    os[(size_t)i] = imgw + i * HW;
+    ys[(size_t)i] = p->pyr + i * p->s_pyr;
+  }
+  NSST_TRY(run_atrousdec(p, n, xs.data(), ys.data(), nullptr, st, ncoeff - 1));
+  for (int i = 0; i < n; i++) NSST_CUDA(launch_scale_planes(ys[(size_t)i], HW, ncoeff, w, st));
+  std::vector<const float*> ysc(ys.begin(), ys.end());
+  NSST_TRY(run_atrousrec(p, n, ysc.data(), nullptr, os.data(), st, ncoeff - 1));
+  // separate.m:82-102: HH quadrant of a one-level Daubechies-4 mdwt, per image
+  NSST_CUDA(launch_dwt_hh(imgw, HW, n, H, W, bd4.data(), l4, hh, st));
+  NSST_CUDA(cudaMemcpyAsync(hhh, hh, sizeof(double) * n * (HW / 4), cudaMemcpyDeviceToHost, st));
+  NSST_CUDA(cudaEventRecord(p->fork_ev, st));
+  // separate.m:104-114: per image the largest |c_b| of every shearlet band (buff(1) = max_b of that / E_b)
+  std::vector<const float*> xw((size_t)n);
+  for (int i = 0; i < n; i++) xw[(size_t)i] = imgw + i * HW;
+  NSST_TRY(enqueue_band_maxima(p, n, xw.data(), bits, st));
+  // separate.m:119-126: buff(2) = max |yh| of the Symmlet-4 mrdwt, per image
+  NSST_CUDA(cudaMemsetAsync(bits + (size_t)n * nb, 0, sizeof(unsigned) * n * 3 * L, st));
+  NSST_TRY(enqueue_mrdwt(imgw, HW, n, H, W, ta, L, yl, yh, nullptr, st));
+  NSST_CUDA(launch_plane_maxabs(yh, HW, n * 3 * L, bits + (size_t)n * nb, kRedBlocks, st));
+  NSST_CUDA(cudaMemcpyAsync(hb, bits, sizeof(unsigned) * nbits, cudaMemcpyDeviceToHost, st));
+  // the noise estimates on the host cores while the maxima are computed
+  NSST_CUDA(cudaEventSynchronize(p->fork_ev));
+  std::vector<double> sigmas((size_t)n);
+  {
+    const int nt = std::max(1, std::min(n, host_threads()));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; t++)
+      pool.emplace_back([&, t] {
+        for (int i = t; i < n; i += nt)
+          sigmas[(size_t)i] = mad(std::vector<double>(hhh + (size_t)i * (HW / 4), hhh + (size_t)(i + 1) * (HW / 4)));
+      });
+    for (auto& th : pool) th.join();
+  }
+  NSST_CUDA(cudaStreamSynchronize(st));
+  auto as_float = [](unsigned u) {
+    float v;
+    std::memcpy(&v, &u, sizeof(float));
+    return v;
+  };
 
   std::vector<float> hS((size_t)itermax * n * nb), hW((size_t)itermax * n);
-  std::vector<double> hhh(HW / 4), ones((size_t)p->nlev + 1, 1.0);
-  std::vector<unsigned> hb((size_t)3 * L);
   for (int i = 0; i < n; i++) {
-    const float* xi = imgw + i * HW;
-    // separate.m:82-102: sigma = MAD of the HH quadrant of a one-level Daubechies-4 mdwt
-    NSST_CUDA(launch_dwt_hh(xi, H, W, bd4.data(), l4, hh, st));
-    NSST_CUDA(cudaMemcpyAsync(hhh.data(), hh, sizeof(double) * hhh.size(), cudaMemcpyDeviceToHost, st));
-    NSST_CUDA(cudaStreamSynchronize(st));
-    const double sigma = mad(hhh), stop_i = stop * sigma;
-    // separate.m:104-114: buff(1), the largest |c_b| / E_b of the shearlet coefficients
-    double b1 = 0.0;
-    NSST_TRY(nsst_shear_trans(p, xi, coef, st));
-    NSST_TRY(nsst_thresh_max(p, coef, 0.0, ones.data(), E.data(), NSST_THRESH_HARD, &b1, st));
-    // separate.m:119-126: buff(2) = max |yh| of the Symmlet-4 mrdwt
-    NSST_TRY(enqueue_mrdwt(xi, HW, 1, H, W, ta, L, yl, yh, nullptr, st));
-    NSST_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * 3 * L, st));
-    NSST_CUDA(launch_plane_maxabs(yh, HW, 3 * L, bits, kRedBlocks, st));
-    NSST_CUDA(cudaMemcpyAsync(hb.data(), bits, sizeof(unsigned) * hb.size(), cudaMemcpyDeviceToHost, st));
-    NSST_CUDA(cudaStreamSynchronize(st));
+    const double sigma = sigmas[(size_t)i], stop_i = stop * sigma;
+    double b1 = 0.0;  // thresh.m:38-41 with lambda = 0: max_b max|c_b| / E_b
+    for (int b = 0; b < nb; b++)
+      if (E[(size_t)b] > 0) b1 = std::max(b1, (double)as_float(hb[(size_t)i * nb + b]) / E[(size_t)b]);
     float m2 = 0.0f;
-    for (unsigned u : hb) {
-      float v;
-      std::memcpy(&v, &u, sizeof(float));
-      m2 = std::max(m2, v);
-    }
+    for (int k = 0; k < 3 * L; k++) m2 = std::max(m2, as_float(hb[(size_t)n * nb + (size_t)i * 3 * L + k]));
     const double b2 = m2;
     // separate.m:128-131: exponential decrease from deltamax to stop
     const double deltamax = std::min(b1, b2);
@@ -1870,12 +1963,11 @@ nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int
   NSST_CUDA(cudaMemcpyAsync(thW, hW.data(), sizeof(float) * hW.size(), cudaMemcpyHostToDevice, st));
   NSST_CUDA(cudaStreamSynchronize(st));  // the host tables may go out of scope
 
-  // separate.m:144-256: the relaxation loop, queued without host waits
-  std::lock_guard<std::mutex> lk(p->mu);
-  p->saved_n = 0;
-  timer_begin(p, st);
-  std::vector<const float*> xs((size_t)n);
-  std::vector<float*> os((size_t)n);
+  // separate.m:144-256: the relaxation loop, queued without host waits.  The
+  // two parts of an iteration only share the residual, so the wavelet branch
+  // runs on the plan's second stream (fork after the residual, join before
+  // the next one and at the end).
+  cudaStream_t sd = p->side;
   for (int i = 0; i < n; i++) {
     xs[(size_t)i] = ra1 + i * HW;
     os[(size_t)i] = S + i * HW;
@@ -1884,13 +1976,17 @@ nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int
   NSST_CUDA(cudaMemsetAsync(P, 0, sizeof(float) * n * HW, st));
   for (int k = 0; k < itermax; k++) {
     NSST_CUDA(launch_sep_residual(imgw, C, P, ra1, ra2, n * HW, st));
+    NSST_CUDA(cudaEventRecord(p->fork_ev, st));
+    NSST_CUDA(cudaStreamWaitEvent(sd, p->fork_ev, 0));
+    // points: wavelet hard threshold (second stream)
+    NSST_TRY(enqueue_mrdwt(ra2, HW, n, H, W, ta, L, yl, yh, thW + (size_t)k * n, sd));
+    NSST_TRY(enqueue_mirdwt(yl, yh, nullptr, n, H, W, ts, L, P, sd));
+    NSST_CUDA(cudaEventRecord(p->join_ev, sd));
     // curves: shearlet hard threshold, then TV correction
     NSST_TRY(enqueue_denoise(p, n, xs.data(), os.data(), NSST_THRESH_HARD, true, st, false,
                              thS + (size_t)k * n * nb));
     NSST_CUDA(launch_tv_haar(S, C, HW, n, H, W, (float)haar[0], (float)gamma, st));
-    // points: wavelet hard threshold
-    NSST_TRY(enqueue_mrdwt(ra2, HW, n, H, W, ta, L, yl, yh, thW + (size_t)k * n, st));
-    NSST_TRY(enqueue_mirdwt(yl, yh, nullptr, n, H, W, ts, L, P, st));
+    NSST_CUDA(cudaStreamWaitEvent(st, p->join_ev, 0));
   }
   return NSST_OK;
 }
