@@ -499,8 +499,16 @@ __device__ __forceinline__ void block_fft_hook(float2* a, float2* b, const float
 // the thread's butterflies into registers, synchronises, then writes them
 // back (two barriers per pass, half the shared memory of the ping-pong form,
 // so more CTAs fit on an SM).  `st` of the last pass may write `buf`.
-template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT, class Rd, class Wr>
-__device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const float2* __restrict__ tw) {
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+// after_read runs once every thread has read the pass's inputs (after the
+// pass's first barrier): the point from which the source may be overwritten.
+template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT, class Rd, class Wr,
+          class Hook = NoHook>
+__device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const float2* __restrict__ tw,
+                                            const Hook& after_read = Hook{}) {
   constexpr int NB = N / R;
   constexpr int TOTAL = NB * NSEQ;
   constexpr int IPT = (TOTAL + T - 1) / T;
@@ -525,6 +533,7 @@ __device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const fl
     }
   }
   __syncthreads();
+  after_read();
 #pragma unroll
   for (int it = 0; it < IPT; it++) {
     const int w = threadIdx.x + it * T;
@@ -538,13 +547,13 @@ __device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const fl
   __syncthreads();
 }
 
-template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St>
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, class Hook>
 __device__ __forceinline__ void fft_hook_ip_passes(float2*, const float2* __restrict__, const Ld&, const St&,
-                                                   RadixList<>) {}
+                                                   const Hook&, RadixList<>) {}
 
-template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, int R, int... Rest>
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, class Hook, int R, int... Rest>
 __device__ __forceinline__ void fft_hook_ip_passes(float2* buf, const float2* __restrict__ tw, const Ld& ld,
-                                                   const St& st, RadixList<R, Rest...>) {
+                                                   const St& st, const Hook& hook, RadixList<R, Rest...>) {
   constexpr bool first = NS == 1;
   constexpr bool last = sizeof...(Rest) == 0;
   constexpr int SWZ_OUT = (first && !last && R % 2 == 0) ? R : 0;
@@ -560,15 +569,28 @@ __device__ __forceinline__ void fft_hook_ip_passes(float2* buf, const float2* __
     else
       buf[row * NSEQ + s] = v;
   };
-  stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
-  fft_hook_ip_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, st, RadixList<Rest...>{});
+  if constexpr (first)
+    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw, hook);
+  else
+    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+  fft_hook_ip_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, st, hook, RadixList<Rest...>{});
 }
 
-template <int N, int NSEQ, int T, int DIR, class Ld, class St>
+// after_first_read: called once the first pass has read all of its inputs
+// through ld (e.g. to start refilling the buffer ld reads from).
+template <int N, int NSEQ, int T, int DIR, class Ld, class St, class Hook = NoHook>
 __device__ __forceinline__ void block_fft_hook_ip(float2* buf, const float2* __restrict__ tw, const Ld& ld,
-                                                  const St& st) {
-  fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, typename FftPlan<N>::type{});
+                                                  const St& st, const Hook& after_first_read = Hook{}) {
+  fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, after_first_read, typename FftPlan<N>::type{});
 }
+
+// 16-byte asynchronous global -> shared copies (cp.async, sm_80+)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Out-of-place packed-real post-processing (after a forward FFT of the
 // W/2-point complex view); see r2c_post for the formulas.

@@ -86,7 +86,7 @@ inline void fill_taps(AtrousTaps<F>& t, const float* hflip) {
 inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
 
 enum class RowOp { Fwd, Inv, Thresh, Backward };
-enum class ColOp { Fwd, Inv, Analysis, Synthesis };
+enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis };  // AnalysisLevel: one job per level (all its bands)
 
 bool row_len_supported(int wh);
 bool col_len_supported(int h);

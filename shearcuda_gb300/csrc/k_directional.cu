@@ -53,10 +53,25 @@ struct ColCfg {  // N = H points per column
 // CTA keep that share at 8 complex values per thread.
 template <int N>
 struct SynCfg : ColCfg<N> {
-  // two column buffers (transform, running sum) and the DC column
-  static constexpr size_t smem() { return (2 * (size_t)N * ColCfg<N>::LD + N) * sizeof(float2); }
+  // two column buffers (transform, running sum), the DC column and the
+  // staging buffer that the next band streams into (cp.async) while the
+  // current one is transformed
+  static constexpr size_t smem() {
+    return (2 * (size_t)N * ColCfg<N>::LD + N + (size_t)N * ColCfg<N>::CS) * sizeof(float2);
+  }
   static constexpr int T = N >= 2048 ? 1024 : ((N * ColCfg<N>::CS) % 512 == 0 ? 512 : 256);
   static constexpr int MINB = 1024 / T;
+};
+
+// The multi-band analysis CTA keeps its column group of the level spectrum,
+// a staging buffer for the next band's filter spectrum and the transform.
+template <int N>
+struct AnaCfg : ColCfg<N> {
+  static constexpr size_t smem() { return 3 * (size_t)N * ColCfg<N>::CS * sizeof(float2); }
+  // the column kernels' thread count (every thread busy in the radix-16
+  // passes); shared memory allows two CTAs per SM below 2048 points
+  static constexpr int T = ColCfg<N>::T;
+  static constexpr int MINB = N >= 2048 ? 1 : 2;
 };
 
 __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
@@ -378,6 +393,57 @@ __global__ void __launch_bounds__(ColCfg<H>::T, ColCfg<H>::MINB) k_band_analysis
       ColGlobalSt{dst_base + job.dst + col0, WH});
 }
 
+// analysis of all bands of one level: dst_k = colIFFT( Wk .* Y ) for the
+// job.nbands consecutive bands (spectra, side arrays and outputs at k *
+// band_stride, k * H, k * band_stride).  The CTA's column group of Y is
+// staged once; each band's filter columns stream into a staging buffer with
+// cp.async while the previous band is transformed.
+template <int H>
+__global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB) k_band_analysis_ml(const ColJob* __restrict__ jobs, int n_active,
+                                                                  int WH, const float2* src_base, float2* dst_base,
+                                                                  const float2* __restrict__ spec_base,
+                                                                  size_t band_stride,
+                                                                  const float2* __restrict__ twH) {
+  using C = AnaCfg<H>;
+  constexpr int CS = C::CS, CH = CS / 2;  // 16-byte chunks per row of the column group
+  extern __shared__ float2 smem[];
+  float2* A = smem;            // transform, in place
+  float2* Y = A + H * CS;      // level spectrum column group [row][column]
+  float2* Wb = Y + H * CS;     // staged filter spectrum of the current band
+  const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const int col0 = blockIdx.x * CS;
+  const bool dc = col0 == 0;
+  auto stage = [&](float2* dst, const float2* src) {
+    for (int e = threadIdx.x; e < H * CH; e += C::T) {
+      const int i = e / CH, c = e - (e / CH) * CH;
+      cp_async16(dst + i * CS + 2 * c, src + (size_t)i * WH + 2 * c);
+    }
+  };
+  stage(Y, src_base + job.src + col0);
+  stage(Wb, spec_base + job.spec + col0);
+  cp_async_commit();
+  for (int k = 0; k < job.nbands; k++) {
+    cp_async_wait_all();
+    __syncthreads();
+    const float2* m0 = spec_base + job.m0 + (size_t)k * H;
+    // Wk .* Y, with the packed DC/Nyquist column's M term (see AnalysisLd)
+    auto ld = [&](int i, int s) -> float2 {
+      float2 r = cmul(Wb[i * CS + s], Y[i * CS + s]);
+      if (dc && s == 0) r = cadd(r, cmul(__ldg(&m0[i]), cconj(Y[((H - i) % H) * CS])));
+      return r;
+    };
+    auto next = [&]() {
+      if (k + 1 < job.nbands) {
+        stage(Wb, spec_base + job.spec + (size_t)(k + 1) * band_stride + col0);
+        cp_async_commit();
+      }
+    };
+    block_fft_hook_ip<H, CS, C::T, +1>(A, twH, ld, ColGlobalSt{dst_base + job.dst + (size_t)k * band_stride + col0, WH},
+                                      next);
+  }
+}
+
 // synthesis: dst = colIFFT( sum_k conj(Wk) .* colFFT(src_k) ) over job.nbands
 // bands stored at src + k * band_stride, spectra at spec + k * band_stride,
 // side arrays at m0 + k * H.  Each band's column FFT runs in place in A; its
@@ -395,12 +461,23 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
   using C = SynCfg<H>;
   extern __shared__ float2 smem[];
   float2 *A = smem, *S = smem + (size_t)H * C::LD, *D = smem + 2 * (size_t)H * C::LD;
+  float2* P = D + H;  // staging: the band's H x CS column group, [row][column]
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * C::CS;
   const bool dc = col0 == 0;
+  // band k's column group -> P with 16-byte cp.async (rows are CS float2 = 64 or 32 contiguous bytes)
+  auto prefetch = [&](int k) {
+    constexpr int CH = C::CS / 2;
+    const float2* src = src_base + job.src + (size_t)k * band_stride + col0;
+    for (int e = threadIdx.x; e < H * CH; e += C::T) {
+      const int i = e / CH, c = e - (e / CH) * CH;
+      cp_async16(P + i * C::CS + 2 * c, src + (size_t)i * WH + 2 * c);
+    }
+    cp_async_commit();
+  };
+  prefetch(0);
   for (int k = 0; k < job.nbands; k++) {
-    const float2* src = src_base + job.src + k * band_stride;
     const float2* spec = spec_base + job.spec + k * band_stride + col0;
     const bool first = k == 0;
     auto acc_st = [&](int i, int sq, float2 z) {
@@ -409,7 +486,13 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
       *t = first ? p : cadd(*t, p);
       if (dc && sq == 0) D[i] = z;
     };
-    block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, ColGlobalLd{src + col0, WH}, acc_st);
+    cp_async_wait_all();
+    __syncthreads();
+    // the first pass reads band k from P; once it has, band k + 1 starts streaming in
+    auto next = [&]() {
+      if (k + 1 < job.nbands) prefetch(k + 1);
+    };
+    block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, SmemLd<C::CS>{P}, acc_st, next);
     if (dc) {
       for (int i = threadIdx.x; i < H; i += C::T) {
         const float2 m = __ldg(&spec_base[job.m0 + (size_t)k * H + i]);
@@ -487,6 +570,7 @@ cudaError_t prepare_col_kernels(int h) {
     cudaError_t e = opt_in(k_cols<n, -1>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_cols<n, 1>, sm);                       \
     if (e == cudaSuccess) e = opt_in(k_band_analysis<n>, sm);                 \
+    if (e == cudaSuccess) e = opt_in(k_band_analysis_ml<n>, AnaCfg<n>::smem()); \
     if (e == cudaSuccess) e = opt_in(k_band_synthesis<n>, SynCfg<n>::smem());  \
     return e;                                                                 \
   }
@@ -587,6 +671,9 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
     else if (op == ColOp::Analysis)                                                                   \
       k_band_analysis<n><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,     \
                                                          twH);                                        \
+    else if (op == ColOp::AnalysisLevel)                                                              \
+      k_band_analysis_ml<n><<<grid, AnaCfg<n>::T, AnaCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base, dst_base, \
+                                                                        spec_base, band_stride, twH); \
     else                                                                                              \
       k_band_synthesis<n><<<grid, SynCfg<n>::T, SynCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base, dst_base,   \
                                                                        spec_base,                     \

@@ -81,6 +81,7 @@ struct nsst_plan {
   RowJob* j_rows_lev_fwd = nullptr;   // pyr[1..] -> lev           (B*nlev)
   ColJob* j_cols_lev = nullptr;       // lev in place              (B*nlev)
   ColJob* j_analysis = nullptr;       // lev -> band, band-major in groups of 8 items (B*ndir_total)
+  ColJob* j_analysis_lev = nullptr;   // lev -> all bands of the level, level-major (B*nlev)
   RowJob* j_rows_bands = nullptr;     // band in place, same order (B*ndir_total)
   ColJob* j_synthesis = nullptr;      // band -> sum, level-major  (B*nlev)
   RowJob* j_rows_lev_inv = nullptr;   // sum -> rec[1..]           (B*nlev)
@@ -336,6 +337,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_j3 = take(sizeof(ColJob) * nD), o_j4 = take(sizeof(RowJob) * nD);
   size_t o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
   size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
+  size_t o_j9 = take(sizeof(ColJob) * nL);
   p->arena_bytes = off;
   ce = dev_alloc((void**)&p->arena, p->arena_bytes);
   if (ce != cudaSuccess) {
@@ -366,6 +368,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->j_rows_lev_fwd = (RowJob*)(A + o_j1);
   p->j_cols_lev = (ColJob*)(A + o_j2);
   p->j_analysis = (ColJob*)(A + o_j3);
+  p->j_analysis_lev = (ColJob*)(A + o_j9);
   p->j_rows_bands = (RowJob*)(A + o_j4);
   p->j_synthesis = (ColJob*)(A + o_j5);
   p->j_rows_lev_inv = (RowJob*)(A + o_j6);
@@ -445,6 +448,16 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
                             i});
       }
     }
+    // one analysis job per (level, item), level-major: the CTAs running
+    // together stream the same filter spectra through L2
+    std::vector<ColJob> j9;
+    for (int l = 0; l < p->nlev; l++) {
+      for (int i = 0; i < B; i++) {
+        const size_t lev = f2(p->lev + i * p->s_lev), band = f2(p->band + i * p->s_band);
+        j9.push_back(ColJob{lev + (size_t)l * HWh, band + (size_t)p->first_band[l] * HWh,
+                            (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], i});
+      }
+    }
     for (int b = 0; b < p->ndir_total; b++) {
       const size_t band0 = f2(p->band);
       // coefficient plane 1+b of the caller's buffer <-> band scratch of item 0
@@ -457,6 +470,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     ce = up(p->j_rows_lev_fwd, j1.data(), j1.size() * sizeof(RowJob));
     if (ce == cudaSuccess) ce = up(p->j_cols_lev, j2.data(), j2.size() * sizeof(ColJob));
     if (ce == cudaSuccess) ce = up(p->j_analysis, j3.data(), j3.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->j_analysis_lev, j9.data(), j9.size() * sizeof(ColJob));
     if (ce == cudaSuccess) ce = up(p->j_rows_bands, j4.data(), j4.size() * sizeof(RowJob));
     if (ce == cudaSuccess) ce = up(p->j_synthesis, j5.data(), j5.size() * sizeof(ColJob));
     if (ce == cudaSuccess) ce = up(p->j_rows_lev_inv, j6.data(), j6.size() * sizeof(RowJob));
@@ -741,7 +755,8 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   timer_mark(p, "fft_rows_fwd", st);
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
   timer_mark(p, "fft_cols_fwd", st);
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
+                        (size_t)H * p->WH, p->twH, st));
   timer_mark(p, "band_analysis_cols", st);
   if (keep) {
     NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW,
@@ -793,7 +808,8 @@ nsst_status enqueue_band_maxima(nsst_plan* p, int n, const float* const* x, unsi
   NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
   NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
+                        (size_t)H * p->WH, p->twH, st));
   NSST_CUDA(launch_rows_max(p->j_rows_bands, B * p->ndir_total, n, H, W, A, p->twWh, p->twW, bits, st));
   for (int i = 0; i < n; i++)
     NSST_CUDA(launch_plane_maxabs(ys[(size_t)i], HW, 1, bits + (size_t)i * p->nbands, kRedBlocks, st));
