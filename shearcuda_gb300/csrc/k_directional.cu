@@ -49,8 +49,8 @@ struct ColCfg {  // N = H points per column
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 
-// The synthesis CTA keeps its running band sum in registers: more threads per
-// CTA keep that share at 8 complex values per thread.
+// The synthesis CTA keeps its running band sum in shared memory next to the
+// transform buffer and the next band's staging buffer.
 template <int N>
 struct SynCfg : ColCfg<N> {
   // two column buffers (transform, running sum), the DC column and the
@@ -59,8 +59,9 @@ struct SynCfg : ColCfg<N> {
   static constexpr size_t smem() {
     return (2 * (size_t)N * ColCfg<N>::LD + N + (size_t)N * ColCfg<N>::CS) * sizeof(float2);
   }
-  static constexpr int T = N >= 2048 ? 1024 : ((N * ColCfg<N>::CS) % 512 == 0 ? 512 : 256);
-  static constexpr int MINB = 1024 / T;
+  // the column kernels' thread count; shared memory allows two CTAs per SM below 2048 points
+  static constexpr int T = ColCfg<N>::T;
+  static constexpr int MINB = N >= 2048 ? 1 : 2;
 };
 
 // The multi-band analysis CTA keeps its column group of the level spectrum,
