@@ -344,14 +344,18 @@ typedef struct nsst_separate_info {
 } nsst_separate_info;
 
 /* Points / curves separation of n images (n <= the plan's batch capacity):
- * separate.m:1-289 with the plan's shearlets, the 'maxflat' pyramid of the
- * plan, level2 Symmlet-4 wavelet levels, itermax iterations, the stopping
+ * separate.m:1-289 with the plan's shearlets and pyramid filters (the
+ * reference hard-codes 'maxflat', separate.m:61; a 'maxflat' plan matches it),
+ * level2 Symmlet-4 wavelet levels, itermax iterations, the stopping
  * factor stop, the TV soft threshold gamma and the ncoeff band weights coeff
  * (re_weight_band; 2 <= ncoeff <= nlevels + 1).  img: n x H x W device;
  * writes the curve part to C and the point part to P (n x H x W device) and,
  * if info is not NULL, n nsst_separate_info records.  The per-image setup
  * (band norms, MAD, the two maxima) waits for the stream; the iterations are
  * then queued on it without host waits. */
+/* The noise estimate uses the HH quadrant (rows H/2.., columns W/2..) of the
+ * one-level DWT; for the square images the reference accepts that is its
+ * wc(N/2+1:N, N/2+1:N) (separate.m:101). */
 nsst_status nsst_separate(nsst_plan* plan, const float* img, int n, int level2, int itermax, double stop,
                           double gamma, const double* coeff, int ncoeff, float* C, float* P,
                           nsst_separate_info* info, void* stream);
