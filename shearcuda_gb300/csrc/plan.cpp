@@ -95,9 +95,18 @@ struct nsst_plan {
   // CUDA graph replay of the batched denoise launch sequence
   bool use_graphs = false;
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  std::vector<const void*> gkey;
-  int gkey_n = -1, gkey_mode = -1;
+  // a few instantiated graphs, least recently used replaced first: callers
+  // that alternate buffer sets (copies of one batch overlapping the compute of
+  // the next) replay without re-capturing
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void*> key;
+    int n = -1, mode = -1;
+    uint64_t used = 0;
+  };
+  static constexpr int kGraphCache = 4;
+  GraphEntry graphs[kGraphCache];
+  uint64_t graph_clock = 0;
 
   // gradient workspace (nsst_plan_enable_grad), one allocation
   char* garena = nullptr;
@@ -573,7 +582,8 @@ nsst_status nsst_plan_destroy(nsst_plan* p) {
   if (p->arena || p->th_host) cudaDeviceSynchronize();  // outstanding work may still use the buffers
   for (cudaEvent_t e : p->ev)
     if (e) cudaEventDestroy(e);
-  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  for (auto& g : p->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->th_done) cudaEventDestroy(p->th_done);
   if (p->side) cudaStreamDestroy(p->side);
@@ -1023,10 +1033,16 @@ nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const
     key.push_back(out[i]);
   }
   const int kmode = mode * 2 + (lowpass_th ? 1 : 0);
-  if (!p->gexec || n != p->gkey_n || kmode != p->gkey_mode || key != p->gkey) {
-    if (p->gexec) {
-      cudaGraphExecDestroy(p->gexec);
-      p->gexec = nullptr;
+  nsst_plan::GraphEntry* hit = nullptr;
+  for (auto& g : p->graphs)
+    if (g.exec && g.n == n && g.mode == kmode && g.key == key) hit = &g;
+  if (!hit) {
+    hit = &p->graphs[0];
+    for (auto& g : p->graphs)
+      if (!g.exec || g.used < hit->used) hit = &g;
+    if (hit->exec) {
+      cudaGraphExecDestroy(hit->exec);
+      hit->exec = nullptr;
     }
     NSST_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
     nsst_status s = enqueue_denoise(p, n, x, out, mode, lowpass_th, p->cap_stream);
@@ -1037,18 +1053,19 @@ nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const
       return s;
     }
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-    ce = cudaGraphInstantiate(&p->gexec, g, 0);
+    ce = cudaGraphInstantiate(&hit->exec, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) {
-      p->gexec = nullptr;
+      hit->exec = nullptr;
       return cuda_fail(ce, "cudaGraphInstantiate");
     }
-    p->gkey = key;
-    p->gkey_n = n;
-    p->gkey_mode = kmode;
+    hit->key = key;
+    hit->n = n;
+    hit->mode = kmode;
   }
+  hit->used = ++p->graph_clock;
   count_launch(0);
-  NSST_CUDA(cudaGraphLaunch(p->gexec, st));
+  NSST_CUDA(cudaGraphLaunch(hit->exec, st));
   return NSST_OK;
 }
 
