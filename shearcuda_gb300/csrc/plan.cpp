@@ -125,6 +125,7 @@ struct nsst_plan {
   RowJob* gj_rows_lev_fwd = nullptr;   // gyp[1..] -> lev2
   ColJob* gj_cols_lev = nullptr;       // lev2 in place
   ColJob* gj_analysis = nullptr;       // lev2 -> band2
+  ColJob* gj_analysis_lev = nullptr;   // lev2 -> all bands of the level in band2, level-major (B*nlev)
   // differentiable forward: thresholded bands go to bandT so that band keeps
   // the coefficients the backward needs (valid for saved_n items)
   float2* bandT = nullptr;
@@ -1290,6 +1291,7 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
   size_t o_bandT = take(sizeof(float2) * NB * p->ndir_total * HWh);
   size_t o_jT = take(sizeof(RowJob) * nD), o_jS = take(sizeof(ColJob) * nL);
+  size_t o_jA = take(sizeof(ColJob) * nL);
   cudaError_t ce = dev_alloc((void**)&p->garena, off);
   if (ce != cudaSuccess) {
     p->garena = nullptr;
@@ -1316,6 +1318,7 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   p->bandT = (float2*)(G + o_bandT);
   p->gj_rows_T = (RowJob*)(G + o_jT);
   p->gj_synth_T = (ColJob*)(G + o_jS);
+  p->gj_analysis_lev = (ColJob*)(G + o_jA);
   auto g2 = [&](const void* ptr) { return (size_t)((const char*)ptr - G) / sizeof(float2); };
   auto a2 = [&](const void* ptr) { return (size_t)((const char*)ptr - p->arena) / sizeof(float2); };
   std::vector<RowJob> j1, j4, j6, j7, j8;
@@ -1339,10 +1342,14 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
       j4.push_back(RowJob{band + (size_t)b * HWh, band2 + (size_t)b * HWh, 1 + b, i});
     }
   }
+  std::vector<ColJob> jA;
   for (int l = 0; l < p->nlev; l++)
     for (int i = 0; i < B; i++) {
       const size_t band2 = g2(p->band2 + i * p->s_band), sum = g2(p->sum2 + i * p->s_sum);
+      const size_t lev = g2(p->lev2 + i * p->s_lev);
       j5.push_back(ColJob{band2 + (size_t)p->first_band[l] * HWh, sum + (size_t)l * HWh,
+                          (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], i});
+      jA.push_back(ColJob{lev + (size_t)l * HWh, band2 + (size_t)p->first_band[l] * HWh,
                           (size_t)p->first_band[l] * HWh, p->m0_off + (size_t)p->first_band[l] * H, p->ndir[l], i});
     }
   for (int b = 0; b < p->ndir_total; b++) {
@@ -1374,6 +1381,7 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   ce = up(p->gj_rows_lev_fwd, j1.data(), j1.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_cols_lev, j2.data(), j2.size() * sizeof(ColJob));
   if (ce == cudaSuccess) ce = up(p->gj_analysis, j3.data(), j3.size() * sizeof(ColJob));
+  if (ce == cudaSuccess) ce = up(p->gj_analysis_lev, jA.data(), jA.size() * sizeof(ColJob));
   if (ce == cudaSuccess) ce = up(p->gj_rows_backward, j4.data(), j4.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_synthesis, j5.data(), j5.size() * sizeof(ColJob));
   if (ce == cudaSuccess) ce = up(p->gj_rows_lev_inv, j6.data(), j6.size() * sizeof(RowJob));
@@ -1486,15 +1494,16 @@ nsst_status tau_backward(nsst_plan* p, const float* const* x, const float* const
     NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0,
                           st));
     NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
-    NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, B * p->ndir_total, n, H, W, A2, A2, p->spec, 0, p->twH,
-                          st));
+    NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
+                          (size_t)H * p->WH, p->twH, st));
     timer_mark(p, "recompute_coefficients", st);
   }
   // 2. d loss / d thresholded coefficients = D P_s^T grad_out
   NSST_TRY(run_atrousrec_adjoint(p, n, grad_out, gyp.data(), st));
   NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_rows_lev_fwd, B * p->nlev, n, H, W, G, G, p->twWh, p->twW, nullptr, 0, st));
   NSST_CUDA(launch_cols(ColOp::Fwd, p->gj_cols_lev, B * p->nlev, n, H, W, G2, G2, nullptr, 0, p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::Analysis, p->gj_analysis, B * p->ndir_total, n, H, W, G2, G2, p->spec, 0, p->twH, st));
+  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->gj_analysis_lev, B * p->nlev, n, H, W, G2, G2, p->spec,
+                        (size_t)H * p->WH, p->twH, st));
   timer_mark(p, "gradient_analysis", st);
   // 3. threshold subgradient per band (+ tau partials), then D^T
   const size_t pstride = (size_t)B * p->ntiles;
