@@ -41,6 +41,51 @@ template <int DIR>
 __device__ __forceinline__ float2 mul_i(float2 a) {
   return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
 }
+// a + c t (the radix-3 butterfly's mean term)
+__device__ __forceinline__ float2 caxc(float2 a, float c, float2 t) { return make_float2(a.x + c * t.x, a.y + c * t.y); }
+// a (c + i sg sn)
+__device__ __forceinline__ float2 crot(float2 a, float c, float sg, float sn) {
+  return make_float2(a.x * c - sg * sn * a.y, a.y * c + sg * sn * a.x);
+}
+// a W8^1 and a W8^3 (forward: exp(-2 pi i k / 8), inverse: exp(+2 pi i k / 8))
+template <int DIR>
+__device__ __forceinline__ float2 rot8_1(float2 o, float r) {
+  return DIR < 0 ? make_float2((o.x + o.y) * r, (o.y - o.x) * r) : make_float2((o.x - o.y) * r, (o.y + o.x) * r);
+}
+template <int DIR>
+__device__ __forceinline__ float2 rot8_3(float2 o, float r) {
+  return DIR < 0 ? make_float2((-o.x + o.y) * r, (-o.y - o.x) * r) : make_float2((-o.x - o.y) * r, (-o.y + o.x) * r);
+}
+
+// Two complex values of two sequences at one index, as one 16-byte element
+// (float4 = (re0, im0, re1, im1)): the butterflies below then move two
+// sequences per shared-memory access and per twiddle load.
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 pk4(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+__device__ __forceinline__ float4 cadd(float4 a, float4 b) { return pk4(cadd(lo2(a), lo2(b)), cadd(hi2(a), hi2(b))); }
+__device__ __forceinline__ float4 csub(float4 a, float4 b) { return pk4(csub(lo2(a), lo2(b)), csub(hi2(a), hi2(b))); }
+__device__ __forceinline__ float4 cmul(float4 a, float2 b) { return pk4(cmul(lo2(a), b), cmul(hi2(a), b)); }
+__device__ __forceinline__ float4 cmulc(float4 a, float2 b) { return pk4(cmulc(lo2(a), b), cmulc(hi2(a), b)); }
+__device__ __forceinline__ float4 cscale(float4 a, float s) { return pk4(cscale(lo2(a), s), cscale(hi2(a), s)); }
+template <int DIR>
+__device__ __forceinline__ float4 mul_i(float4 a) {
+  return pk4(mul_i<DIR>(lo2(a)), mul_i<DIR>(hi2(a)));
+}
+__device__ __forceinline__ float4 caxc(float4 a, float c, float4 t) {
+  return pk4(caxc(lo2(a), c, lo2(t)), caxc(hi2(a), c, hi2(t)));
+}
+__device__ __forceinline__ float4 crot(float4 a, float c, float sg, float sn) {
+  return pk4(crot(lo2(a), c, sg, sn), crot(hi2(a), c, sg, sn));
+}
+template <int DIR>
+__device__ __forceinline__ float4 rot8_1(float4 o, float r) {
+  return pk4(rot8_1<DIR>(lo2(o), r), rot8_1<DIR>(hi2(o), r));
+}
+template <int DIR>
+__device__ __forceinline__ float4 rot8_3(float4 o, float r) {
+  return pk4(rot8_3<DIR>(lo2(o), r), rot8_3<DIR>(hi2(o), r));
+}
 
 // ---------------------------------------------------------------------------
 // R-point DFTs in registers.  DIR = -1 forward (exp(-2 pi i ...)), +1 inverse.
@@ -50,8 +95,9 @@ struct Dft;
 
 template <int DIR>
 struct Dft<2, DIR> {
-  __device__ __forceinline__ static void run(float2* v) {
-    float2 a = v[0], b = v[1];
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
+    E a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
   }
@@ -59,16 +105,17 @@ struct Dft<2, DIR> {
 
 template <int DIR>
 struct Dft<3, DIR> {
-  __device__ __forceinline__ static void run(float2* v) {
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
     const float c = -0.5f;
     const float s = 0.86602540378443864676f;  // sin(2 pi / 3)
-    float2 a0 = v[0], a1 = v[1], a2 = v[2];
-    float2 t = cadd(a1, a2);
-    float2 d = csub(a1, a2);
+    E a0 = v[0], a1 = v[1], a2 = v[2];
+    E t = cadd(a1, a2);
+    E d = csub(a1, a2);
     v[0] = cadd(a0, t);
-    float2 m = make_float2(a0.x + c * t.x, a0.y + c * t.y);
+    E m = caxc(a0, c, t);
     // forward: -i * s * d ; inverse: +i * s * d
-    float2 u = mul_i<DIR>(cscale(d, s));
+    E u = mul_i<DIR>(cscale(d, s));
     v[1] = cadd(m, u);
     v[2] = csub(m, u);
   }
@@ -76,9 +123,10 @@ struct Dft<3, DIR> {
 
 template <int DIR>
 struct Dft<4, DIR> {
-  __device__ __forceinline__ static void run(float2* v) {
-    float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-    float2 s13 = cadd(v[1], v[3]), d13 = mul_i<DIR>(csub(v[1], v[3]));
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
+    E s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    E s13 = cadd(v[1], v[3]), d13 = mul_i<DIR>(csub(v[1], v[3]));
     v[0] = cadd(s02, s13);
     v[2] = csub(s02, s13);
     v[1] = cadd(d02, d13);
@@ -88,21 +136,17 @@ struct Dft<4, DIR> {
 
 template <int DIR>
 struct Dft<8, DIR> {
-  __device__ __forceinline__ static void run(float2* v) {
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
     const float r = 0.70710678118654752440f;
-    float2 e[4] = {v[0], v[2], v[4], v[6]};
-    float2 o[4] = {v[1], v[3], v[5], v[7]};
+    E e[4] = {v[0], v[2], v[4], v[6]};
+    E o[4] = {v[1], v[3], v[5], v[7]};
     Dft<4, DIR>::run(e);
     Dft<4, DIR>::run(o);
-    // twiddle o[k] by exp(DIR * 2 pi i k / 8)
-    float2 o1 = o[1], o2 = o[2], o3 = o[3];
-    // k=1: (1 + DIR*i) * r   (forward: (1 - i) r)
-    o[1] = DIR < 0 ? make_float2((o1.x + o1.y) * r, (o1.y - o1.x) * r)
-                   : make_float2((o1.x - o1.y) * r, (o1.y + o1.x) * r);
-    o[2] = mul_i<DIR>(o2);
-    // k=3: forward (-1 - i) r ; inverse (-1 + i) r
-    o[3] = DIR < 0 ? make_float2((-o3.x + o3.y) * r, (-o3.y - o3.x) * r)
-                   : make_float2((-o3.x - o3.y) * r, (-o3.y + o3.x) * r);
+    // twiddle o[k] by exp(DIR * 2 pi i k / 8): k=1 (1 + DIR i) r, k=2 DIR i, k=3 (-1 + DIR i) r
+    o[1] = rot8_1<DIR>(o[1], r);
+    o[2] = mul_i<DIR>(o[2]);
+    o[3] = rot8_3<DIR>(o[3], r);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       v[k] = cadd(e[k], o[k]);
@@ -115,23 +159,22 @@ struct Dft<8, DIR> {
 // 4-point DFTs over n1 -> X[k2 + 4 k1].
 template <int DIR>
 struct Dft<16, DIR> {
-  __device__ __forceinline__ static void run(float2* v) {
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
     const float r = 0.70710678118654752440f;   // cos(pi/4)
     const float c1 = 0.92387953251128675613f;  // cos(pi/8)
     const float s1 = 0.38268343236508977173f;  // sin(pi/8)
-    float2 y[4][4];
+    E y[4][4];
 #pragma unroll
     for (int n1 = 0; n1 < 4; n1++) {
-      float2 t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+      E t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
       Dft<4, DIR>::run(t);
 #pragma unroll
       for (int k2 = 0; k2 < 4; k2++) y[n1][k2] = t[k2];
     }
     // W16^m = exp(DIR * 2 pi i m / 16) for m = n1 * k2 in {1, 2, 3, 4, 6, 9}
     const float sg = DIR < 0 ? -1.f : 1.f;
-    auto rot = [&](float2 a, float c, float sn) {  // a * (c + i sg sn)
-      return make_float2(a.x * c - sg * sn * a.y, a.y * c + sg * sn * a.x);
-    };
+    auto rot = [&](E a, float c, float sn) { return crot(a, c, sg, sn); };  // a * (c + i sg sn)
     y[1][1] = rot(y[1][1], c1, s1);
     y[1][2] = rot(y[1][2], r, r);
     y[1][3] = rot(y[1][3], s1, c1);
@@ -143,7 +186,7 @@ struct Dft<16, DIR> {
     y[3][3] = rot(y[3][3], -c1, -s1);
 #pragma unroll
     for (int k2 = 0; k2 < 4; k2++) {
-      float2 t[4] = {y[0][k2], y[1][k2], y[2][k2], y[3][k2]};
+      E t[4] = {y[0][k2], y[1][k2], y[2][k2], y[3][k2]};
       Dft<4, DIR>::run(t);
 #pragma unroll
       for (int k1 = 0; k1 < 4; k1++) v[k2 + 4 * k1] = t[k1];
@@ -507,22 +550,26 @@ struct NoHook {
 
 // after_read runs once every thread has read the pass's inputs (after the
 // pass's first barrier): the point from which the source may be overwritten.
+// E: the element type, float2 (one sequence) or float4 (two sequences per
+// element, NSEQ counting elements); the row swizzle is chosen for the row's
+// width in bytes, so both forms place rows in the same banks.
 template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, int SWZ_OUT, class Rd, class Wr,
-          class Hook = NoHook>
+          class Hook = NoHook, class E = float2>
 __device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const float2* __restrict__ tw,
                                             const Hook& after_read = Hook{}) {
   constexpr int NB = N / R;
   constexpr int TOTAL = NB * NSEQ;
   constexpr int IPT = (TOTAL + T - 1) / T;
   constexpr int STEP = N / (NS * R);
-  float2 v[IPT][R];
+  constexpr int NSW = NSEQ * (int)(sizeof(E) / sizeof(float2));  // row width in float2 units
+  E v[IPT][R];
 #pragma unroll
   for (int it = 0; it < IPT; it++) {
     const int w = threadIdx.x + it * T;
     if (TOTAL % T == 0 || w < TOTAL) {
       const int s = w % NSEQ, j = w / NSEQ;
 #pragma unroll
-      for (int r = 0; r < R; r++) v[it][r] = rd(swz_row<NSEQ, SWZ_IN>(j + r * NB), s);
+      for (int r = 0; r < R; r++) v[it][r] = rd(swz_row<NSW, SWZ_IN>(j + r * NB), s);
       const int k = j % NS;
       if (NS > 1) {
 #pragma unroll
@@ -543,45 +590,47 @@ __device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const fl
       const int s = w % NSEQ, j = w / NSEQ, k = j % NS;
       const int base = (j / NS) * NS * R + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) wr(swz_row<NSEQ, SWZ_OUT>(base + r * NS), s, v[it][r]);
+      for (int r = 0; r < R; r++) wr(swz_row<NSW, SWZ_OUT>(base + r * NS), s, v[it][r]);
     }
   }
   __syncthreads();
 }
 
-template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, class Hook>
-__device__ __forceinline__ void fft_hook_ip_passes(float2*, const float2* __restrict__, const Ld&, const St&,
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class E, class Ld, class St, class Hook>
+__device__ __forceinline__ void fft_hook_ip_passes(E*, const float2* __restrict__, const Ld&, const St&,
                                                    const Hook&, RadixList<>) {}
 
-template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class St, class Hook, int R, int... Rest>
-__device__ __forceinline__ void fft_hook_ip_passes(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class E, class Ld, class St, class Hook, int R,
+          int... Rest>
+__device__ __forceinline__ void fft_hook_ip_passes(E* buf, const float2* __restrict__ tw, const Ld& ld,
                                                    const St& st, const Hook& hook, RadixList<R, Rest...>) {
   constexpr bool first = NS == 1;
   constexpr bool last = sizeof...(Rest) == 0;
   constexpr int SWZ_OUT = (first && !last && R % 2 == 0) ? R : 0;
-  auto rd = [&](int row, int s) -> float2 {
+  auto rd = [&](int row, int s) -> E {
     if constexpr (first)
       return ld(row, s);
     else
       return buf[row * NSEQ + s];
   };
-  auto wr = [&](int row, int s, float2 v) {
+  auto wr = [&](int row, int s, E v) {
     if constexpr (last)
       st(row, s, v);
     else
       buf[row * NSEQ + s] = v;
   };
   if constexpr (first)
-    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw, hook);
+    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT, decltype(rd), decltype(wr), Hook, E>(rd, wr, tw, hook);
   else
-    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+    stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT, decltype(rd), decltype(wr), NoHook, E>(rd, wr, tw);
   fft_hook_ip_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, st, hook, RadixList<Rest...>{});
 }
 
 // after_first_read: called once the first pass has read all of its inputs
-// through ld (e.g. to start refilling the buffer ld reads from).
-template <int N, int NSEQ, int T, int DIR, class Ld, class St, class Hook = NoHook>
-__device__ __forceinline__ void block_fft_hook_ip(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+// through ld (e.g. to start refilling the buffer ld reads from).  buf holds
+// float2 (NSEQ sequences) or float4 (2 NSEQ sequences, two per element).
+template <int N, int NSEQ, int T, int DIR, class E, class Ld, class St, class Hook = NoHook>
+__device__ __forceinline__ void block_fft_hook_ip(E* buf, const float2* __restrict__ tw, const Ld& ld,
                                                   const St& st, const Hook& after_first_read = Hook{}) {
   fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, after_first_read, typename FftPlan<N>::type{});
 }

@@ -170,6 +170,61 @@ __device__ __forceinline__ void r2c_post_store(float2* __restrict__ dst, const f
   }
 }
 
+// Row-major staging of a CTA's RS rows with rows padded to WH + 2 elements:
+// the tile's global loads and stores then run along the rows (each warp a
+// contiguous 256-byte stretch), and the FFT's first and last passes, which
+// reach it through the functors below, see no bank conflicts.
+template <int WH, int RS, int T>
+__device__ __forceinline__ void fetch_rows_rm(float2* P, const float2* src) {
+  constexpr int WHP = WH + 2, CH = WH / 2;  // 16-byte chunks per row
+  for (int e = threadIdx.x; e < RS * CH; e += T) {
+    const int s = e / CH, c = e - s * CH;
+    cp_async16(P + s * WHP + 2 * c, src + (size_t)s * WH + 2 * c);
+  }
+  cp_async_commit();
+}
+template <int WH>
+struct C2RPreLdRM {  // C2RPreLd reading the padded row-major staging
+  const float2* X;
+  const float2* twW;
+  __device__ __forceinline__ float2 operator()(int k, int s) const {
+    const float2* row = X + s * (WH + 2);
+    const float2 xk = row[k];
+    if (k == 0) return make_float2(xk.x + xk.y, xk.x - xk.y);
+    const float2 xmc = cconj(row[WH - k]);
+    const float2 E = cadd(xk, xmc);
+    const float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));
+    return make_float2(E.x - O.y, E.y + O.x);
+  }
+};
+template <int WH>
+struct SmemStRM {  // element (i, s) -> padded row-major
+  float2* p;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[s * (WH + 2) + i] = v; }
+};
+// r2c_post_store from the padded row-major layout, along the rows
+template <int WH, int RS, int T>
+__device__ __forceinline__ void r2c_post_store_rm(float2* __restrict__ dst, const float2* Z,
+                                                  const float2* __restrict__ twW) {
+#pragma unroll 4
+  for (int e = threadIdx.x; e < WH * RS; e += T) {
+    const int k = e % WH, s = e / WH;
+    const float2* row = Z + s * (WH + 2);
+    const float2 zk = row[k];
+    float2 out;
+    if (k == 0) {
+      out = make_float2(zk.x + zk.y, zk.x - zk.y);
+    } else {
+      const float2 zmc = cconj(row[WH - k]);
+      const float2 E = cscale(cadd(zk, zmc), 0.5f);
+      const float2 d = cscale(csub(zk, zmc), 0.5f);
+      const float2 To = cmul(__ldg(&twW[k]), make_float2(d.y, -d.x));
+      out = cadd(E, To);
+    }
+    dst[(size_t)s * WH + k] = out;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Row kernels.  grid = (H / RS, njobs).
 // ---------------------------------------------------------------------------
@@ -226,16 +281,20 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_thresh
   if (job.item >= n_active) return;
   const float th = thr[job.th_index];
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
-  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  // the tile arrives row-major (padded); the first pass reads it from there
+  // and leaves the dense [index][row] layout in the same buffer
+  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  cp_async_wait_all();
   __syncthreads();
   // C2R (pre-processing in the first pass) with the threshold in the last pass
   // (both transforms in place on one buffer: every pass reads all of its
   // inputs, the pre-processing's mirrored ones included, before a barrier)
   (void)B;
-  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW}, ThreshSt<C::RS>{A, th, mode});
-  // R2C of the thresholded rows; post-processing fused with the store
-  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{A});
-  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshSt<C::RS>{A, th, mode});
+  // R2C of the thresholded rows, its last pass back to the padded row-major
+  // layout; post-processing fused with a store along the rows
+  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemStRM<WH>{A});
+  r2c_post_store_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
 
 // Band maxima (thresh.m's opt == 1 maximum with a zero threshold): C2R of the
@@ -599,8 +658,9 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
       k_rows_fwd<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
     else if (op == RowOp::Inv)                                                         \
       k_rows_inv<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
-    else                                                                               \
-      k_rows_thresh<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
+    else /* padded row-major staging: RS rows of WH + 2 */                             \
+      k_rows_thresh<n><<<grid, RowCfg<n>::T, RowCfg<n>::RS * (n + 2) * sizeof(float2), st>>>(                \
+          jobs, n_active, sb, db, twWh, twW, thr, mode);                                 \
     return cudaGetLastError();                                                         \
   }
     NSST_ROW_SIZES(CASE)
