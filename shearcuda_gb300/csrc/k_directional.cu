@@ -39,6 +39,8 @@ struct RowCfg {  // N = W/2 complex points per row
   static constexpr int MINB = 1024 / T;  // <= 64 registers: at least 32 warps per SM
   static constexpr int LD = RS;
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
+  // one tile staged row-major with rows padded to N + 2 (holds the dense layout too)
+  static constexpr size_t smem_rm() { return (size_t)RS * (N + 2) * sizeof(float2); }
 };
 template <int N>
 struct ColCfg {  // N = H points per column
@@ -202,6 +204,21 @@ struct SmemStRM {  // element (i, s) -> padded row-major
   float2* p;
   __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[s * (WH + 2) + i] = v; }
 };
+template <int WH>
+struct SmemLdRM {  // element (i, s) <- padded row-major
+  const float2* p;
+  __device__ __forceinline__ float2 operator()(int i, int s) const { return p[s * (WH + 2) + i]; }
+};
+// padded row-major rows -> global rows, 16 bytes per thread and step
+template <int WH, int RS, int T>
+__device__ __forceinline__ void store_rows_rm(float2* __restrict__ dst, const float2* P) {
+  constexpr int CH = WH / 2;
+  for (int e = threadIdx.x; e < RS * CH; e += T) {
+    const int s = e / CH, c = e - s * CH;
+    *reinterpret_cast<float4*>(dst + (size_t)s * WH + 2 * c) =
+        *reinterpret_cast<const float4*>(P + s * (WH + 2) + 2 * c);
+  }
+}
 // r2c_post_store from the padded row-major layout, along the rows
 template <int WH, int RS, int T>
 __device__ __forceinline__ void r2c_post_store_rm(float2* __restrict__ dst, const float2* Z,
@@ -241,11 +258,12 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_fwd(co
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
-  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  cp_async_wait_all();
   __syncthreads();
   (void)B;
-  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemSt<C::RS>{A});
-  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
+  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLdRM<WH>{A}, SmemStRM<WH>{A});
+  r2c_post_store_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
 
 // packed rows -> real rows (inverse C2R along W, unnormalised: x W)
@@ -260,11 +278,12 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_inv(co
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
-  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  cp_async_wait_all();
   __syncthreads();
   (void)B;
-  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW},
-                                         RowGlobalSt<WH>{dst_base + job.dst + off});
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, SmemStRM<WH>{A});
+  store_rows_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A);
 }
 
 // packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
@@ -312,9 +331,10 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_max(co
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
-  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
+  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  cp_async_wait_all();
   __syncthreads();
-  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLd<WH, C::RS>{A, twW}, SmemSt<C::RS>{A});
+  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, SmemSt<C::RS>{A});
   __syncthreads();
   float m = 0.0f;
   for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {  // SmemSt wrote (i, s) at i * RS + s
@@ -338,18 +358,21 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
                                                                   float* __restrict__ partials, size_t pstride) {
   using C = RowCfg<WH>;
   extern __shared__ float2 smem[];
-  float2 *A = smem, *B = smem + (size_t)WH * C::LD, *Cb = smem + 2 * (size_t)WH * C::LD;
+  // three buffers of the padded row-major size (the dense layouts fit in them)
+  constexpr int BUF = C::RS * (WH + 2);
+  float2 *A = smem, *B = smem + BUF, *Cb = smem + 2 * BUF;
   __shared__ float red[32];
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const float th = tau[job.th_index];
   const size_t off = (size_t)blockIdx.x * C::RS * WH;
-  load_rows<WH, C::RS, C::LD, C::T>(A, src_base + job.src + off);
-  load_rows<WH, C::RS, C::LD, C::T>(Cb, dst_base + job.dst + off);
+  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  fetch_rows_rm<WH, C::RS, C::T>(Cb, dst_base + job.dst + off);
+  cp_async_wait_all();
   __syncthreads();
   // coefficients c = C2R(Qc) (pre-processing in the first pass)
   float2* const Xc = fft_hook_target<WH>(A, B);
-  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLd<WH, C::RS>{A, twW}, SmemSt<C::RS>{Xc});
+  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLdRM<WH>{A, twW}, SmemSt<C::RS>{Xc});
   // gradient g = C2R(Qg), masked by 1[|c| > t] in the last pass, which also
   // accumulates this thread's share of -sum g sign(c) 1[|c| > t] (soft)
   float2* const S = (Xc == A) ? B : A;
@@ -364,7 +387,7 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
     }
     Xg[i * C::RS + sq] = make_float2(kx ? g.x : 0.0f, ky ? g.y : 0.0f);
   };
-  block_fft_hook<WH, C::RS, C::T, +1>(Cb, S, twWh, C2RPreLd<WH, C::RS>{Cb, twW}, mask_st);
+  block_fft_hook<WH, C::RS, C::T, +1>(Cb, S, twWh, C2RPreLdRM<WH>{Cb, twW}, mask_st);
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
   __syncthreads();
@@ -377,8 +400,8 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
   // R2C of the masked gradient; post-processing fused with the store
   float2* const Y = (Xg == Cb) ? S : Cb;
   float2* const Z = fft_hook_target<WH>(Xg, Y);
-  block_fft_hook<WH, C::RS, C::T, -1>(Xg, Y, twWh, SmemLd<C::RS>{Xg}, SmemSt<C::RS>{Z});
-  r2c_post_store<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
+  block_fft_hook<WH, C::RS, C::T, -1>(Xg, Y, twWh, SmemLd<C::RS>{Xg}, SmemStRM<WH>{Z});
+  r2c_post_store_rm<WH, C::RS, C::T>(dst_base + job.dst + off, Z, twW);
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +635,7 @@ cudaError_t prepare_row_kernels(int wh) {
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
     if (e == cudaSuccess) e = opt_in(k_rows_max<n>, sm);                      \
-    if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * sm / 2);         \
+    if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * RowCfg<n>::smem_rm()); \
     return e;                                                                 \
   }
     NSST_ROW_SIZES(CASE)
@@ -654,13 +677,15 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
   case n: {                                                                            \
     constexpr size_t sm = RowCfg<n>::smem() / 2; /* in place: one buffer */            \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                               \
+    /* one tile staged row-major, rows padded to WH + 2 */                           \
+    constexpr size_t smr = RowCfg<n>::smem_rm();                                       \
+    (void)sm;                                                                          \
     if (op == RowOp::Fwd)                                                              \
-      k_rows_fwd<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
+      k_rows_fwd<n><<<grid, RowCfg<n>::T, smr, st>>>(jobs, n_active, sb, db, twWh, twW);             \
     else if (op == RowOp::Inv)                                                         \
-      k_rows_inv<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW);              \
-    else /* padded row-major staging: RS rows of WH + 2 */                             \
-      k_rows_thresh<n><<<grid, RowCfg<n>::T, RowCfg<n>::RS * (n + 2) * sizeof(float2), st>>>(                \
-          jobs, n_active, sb, db, twWh, twW, thr, mode);                                 \
+      k_rows_inv<n><<<grid, RowCfg<n>::T, smr, st>>>(jobs, n_active, sb, db, twWh, twW);             \
+    else                                                                               \
+      k_rows_thresh<n><<<grid, RowCfg<n>::T, smr, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
   }
     NSST_ROW_SIZES(CASE)
@@ -679,7 +704,7 @@ cudaError_t launch_rows_max(const RowJob* jobs, int njobs, int n_active, int H, 
   switch (WH) {
 #define CASE(n)                                                                                   \
   case n: {                                                                                       \
-    constexpr size_t sm = RowCfg<n>::smem() / 2;                                                  \
+    constexpr size_t sm = RowCfg<n>::smem_rm();                                                   \
     k_rows_max<n><<<dim3(H / RowCfg<n>::RS, njobs), RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, twWh, twW, bits); \
     return cudaGetLastError();                                                                    \
   }
@@ -701,7 +726,7 @@ cudaError_t launch_rows_backward(const RowJob* jobs, int njobs, int n_active, in
   switch (WH) {
 #define CASE(n)                                                                                      \
   case n: {                                                                                          \
-    constexpr size_t sm = 3 * RowCfg<n>::smem() / 2;                                                 \
+    constexpr size_t sm = 3 * RowCfg<n>::smem_rm();                                                  \
     dim3 grid(H / RowCfg<n>::RS, njobs);                                                             \
     k_rows_backward<n><<<grid, RowCfg<n>::T, sm, st>>>(jobs, n_active, sb, db, twWh, twW, tau, mode, \
                                                       partials, pstride);                           \
