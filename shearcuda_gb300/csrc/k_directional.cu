@@ -83,26 +83,6 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
   return a > 0.0f ? copysignf(a, v) : 0.0f;
 }
 
-// global rows [row0, row0+RS) of a packed/real-as-complex H x WH array -> smem [i][s]
-// Sequence-fastest staging: a warp reads 32/RS consecutive elements of each of
-// its RS rows (full 32-byte sectors) and writes consecutive shared rows.
-template <int WH, int RS, int LD, int T>
-__device__ __forceinline__ void load_rows(float2* buf, const float2* __restrict__ src) {
-#pragma unroll 4
-  for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int s = e % RS, i = e / RS;
-    buf[i * LD + s] = src[(size_t)s * WH + i];
-  }
-}
-template <int WH, int RS, int LD, int T>
-__device__ __forceinline__ void store_rows(float2* __restrict__ dst, const float2* buf) {
-#pragma unroll 4
-  for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int s = e % RS, i = e / RS;
-    dst[(size_t)s * WH + i] = buf[i * LD + s];
-  }
-}
-
 // FFT hooks (see block_fft_hook).
 template <int NSEQ>
 struct SmemLd {
@@ -114,22 +94,9 @@ struct SmemSt {
   float2* p;
   __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[i * NSEQ + s] = v; }
 };
-// packed-real pre-processing of index k (see c2r_pre): Z[k] = E + iO with
-// E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k; k = 0 unpacks
-// the two real bins.
-template <int WH, int NSEQ>
-struct C2RPreLd {
-  const float2* X;
-  const float2* twW;
-  __device__ __forceinline__ float2 operator()(int k, int s) const {
-    const float2 xk = X[k * NSEQ + s];
-    if (k == 0) return make_float2(xk.x + xk.y, xk.x - xk.y);
-    const float2 xmc = cconj(X[(WH - k) * NSEQ + s]);
-    const float2 E = cadd(xk, xmc);
-    const float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));
-    return make_float2(E.x - O.y, E.y + O.x);
-  }
-};
+// packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM below:
+// Z[k] = E + iO with E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k;
+// k = 0 unpacks the two real bins.
 template <int NSEQ>
 struct ThreshSt {
   float2* p;
@@ -141,37 +108,6 @@ struct ThreshSt {
     p[i * NSEQ + s] = v;
   }
 };
-// rows of the CTA straight to global memory: element (i, s) -> dst[s * WH + i]
-template <int WH>
-struct RowGlobalSt {
-  float2* dst;
-  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { dst[(size_t)s * WH + i] = v; }
-};
-
-// packed-real post-processing of every index k (see r2c_post) fused with the
-// store of the CTA's rows: X[k] = E + w^k O, E = (Z[k] + conj(Z[WH-k]))/2,
-// O = (Z[k] - conj(Z[WH-k]))/(2i); k = 0 packs the two real bins.
-template <int WH, int RS, int T>
-__device__ __forceinline__ void r2c_post_store(float2* __restrict__ dst, const float2* Z,
-                                               const float2* __restrict__ twW) {
-#pragma unroll 4
-  for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int s = e % RS, k = e / RS;
-    const float2 zk = Z[k * RS + s];
-    float2 out;
-    if (k == 0) {
-      out = make_float2(zk.x + zk.y, zk.x - zk.y);
-    } else {
-      const float2 zmc = cconj(Z[(WH - k) * RS + s]);
-      const float2 E = cscale(cadd(zk, zmc), 0.5f);
-      const float2 d = cscale(csub(zk, zmc), 0.5f);
-      const float2 To = cmul(__ldg(&twW[k]), make_float2(d.y, -d.x));
-      out = cadd(E, To);
-    }
-    dst[(size_t)s * WH + k] = out;
-  }
-}
-
 // Row-major staging of a CTA's RS rows with rows padded to WH + 2 elements:
 // the tile's global loads and stores then run along the rows (each warp a
 // contiguous 256-byte stretch), and the FFT's first and last passes, which
@@ -219,7 +155,10 @@ __device__ __forceinline__ void store_rows_rm(float2* __restrict__ dst, const fl
         *reinterpret_cast<const float4*>(P + s * (WH + 2) + 2 * c);
   }
 }
-// r2c_post_store from the padded row-major layout, along the rows
+// packed-real post-processing of every index k (see r2c_post) fused with the
+// store of the CTA's rows, from the padded row-major layout along the rows:
+// X[k] = E + w^k O, E = (Z[k] + conj(Z[WH-k]))/2, O = (Z[k] - conj(Z[WH-k]))/(2i);
+// k = 0 packs the two real bins.
 template <int WH, int RS, int T>
 __device__ __forceinline__ void r2c_post_store_rm(float2* __restrict__ dst, const float2* Z,
                                                   const float2* __restrict__ twW) {
