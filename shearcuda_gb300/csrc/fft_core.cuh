@@ -540,6 +540,22 @@ __device__ __forceinline__ void block_fft_hook(float2* a, float2* b, const float
   fft_hook_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, ld, st, typename FftPlan<N>::type{});
 }
 
+// block_fft_hook with an explicit radix plan; the last pass's default target
+// is plan_target<Plan>(a, b)
+template <int N, int NSEQ, int T, int DIR, class Plan, class Ld, class St>
+__device__ __forceinline__ void block_fft_hook_plan(float2* a, float2* b, const float2* __restrict__ tw,
+                                                    const Ld& ld, const St& st) {
+  fft_hook_passes<N, NSEQ, T, DIR, 1, 0>(a, b, tw, ld, st, Plan{});
+}
+template <int... Rs>
+__host__ __device__ constexpr int plan_passes(RadixList<Rs...>) {
+  return (int)sizeof...(Rs);
+}
+template <class Plan>
+__device__ __forceinline__ float2* plan_target(float2* a, float2* b) {
+  return (plan_passes(Plan{}) & 1) ? b : a;
+}
+
 // In-place variant of block_fft_hook on one buffer: every pass loads all of
 // the thread's butterflies into registers, synchronises, then writes them
 // back (two barriers per pass, half the shared memory of the ping-pong form,

@@ -55,9 +55,11 @@ template <> struct FftPlan3<256> { using type = RadixList<4, 8, 8>; };
 template <int N, int DIR, int LD, int ST>
 __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, const float2* __restrict__ in,
                                                      const V3Pass P, const float2* __restrict__ tw) {
+  using Plan = typename FftPlan3<N>::type;
+  constexpr int NP = N + 2;  // padded row length of the row-major staging
   extern __shared__ float2 smem[];
   float2* A = smem;
-  float2* Bf = smem + (size_t)N * kSeq;
+  float2* Bf = smem + (size_t)NP * kSeq;
   const int groups_b = P.b_n / kSeq;
   const int a = P.a_lo + (int)blockIdx.x / groups_b;
   const int b0 = P.b_lo + ((int)blockIdx.x % groups_b) * kSeq;
@@ -73,8 +75,8 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
   }
   const size_t wbase = item * P.item_stride;
 
-  for (int e = threadIdx.x; e < N * kSeq; e += kThreads) {
-    const int s = e & (kSeq - 1), i = e / kSeq;
+  // the prologue for element i of sequence s
+  auto load_elem = [&](int i, int s) -> float2 {
     float2 v = make_float2(0.f, 0.f);
     if (i >= P.in_lo && i < P.in_lo + P.in_n) {
       const size_t g = off + (size_t)(i * si + s * ss);
@@ -97,13 +99,72 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
         }
       }
     }
-    A[i * kSeq + s] = v;
+    return v;
+  };
+  // the epilogues other than the threshold, for element i of sequence s
+  auto store_elem = [&](int i, int s, float2 v) {
+    if (i < P.out_lo || i >= P.out_lo + P.out_n) return;
+    const size_t g = off + (size_t)(i * si + s * ss);
+    if (ST == V3_ST_CPLX) {
+      out[wbase + g] = v;
+    } else if (ST == V3_ST_SPEC) {
+      const float2 c = __ldg(&P.spec[g]);
+      const float2 prod = make_float2(c.x * v.x + c.y * v.y, c.x * v.y - c.y * v.x);  // conj(c) * v
+      float2 o = prod;
+      if (!P.first) {
+        const float2 q = out[wbase + g];
+        o = make_float2(q.x + prod.x, q.y + prod.y);
+      }
+      out[wbase + g] = o;
+    } else {
+      int x, y, z;
+      pass_coords(P.axis, a, b0 + s, i, x, y, z);
+      const size_t r = ((size_t)(x - P.o0) * P.r1 + (y - P.o1)) * P.r2 + (z - P.o2);
+      if (ST == V3_ST_REAL) {
+        P.rdst[item * P.r_stride + r] = v.x * P.scale;
+      } else if (ST == V3_ST_PAIR) {
+        P.rdst[item * P.r_stride + r] = v.x * P.scale;
+        if (P.rdst2) P.rdst2[item * P.r_stride + r] = v.y * P.scale;
+      }
+    }
+  };
+
+  if (ST != V3_ST_THRESH && P.axis == 2) {
+    // z-rows are contiguous in memory: stage them row-major (rows padded to
+    // N + 2) with each warp loading consecutive elements of one row, let the
+    // FFT's first and last passes read and write that layout, store along the rows
+    for (int e = threadIdx.x; e < N * kSeq; e += kThreads) {
+      const int s = e / N, i = e - s * N;
+      A[s * NP + i] = load_elem(i, s);
+    }
+    __syncthreads();
+    float2* const Z = plan_target<Plan>(A, Bf);
+    block_fft_hook_plan<N, kSeq, kThreads, DIR, Plan>(
+        A, Bf, tw, [&](int i, int s) { return A[s * NP + i]; }, [&](int i, int s, float2 v) { Z[s * NP + i] = v; });
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * kSeq; e += kThreads) {
+      const int s = e / N, i = e - s * N;
+      store_elem(i, s, Z[s * NP + i]);
+    }
+    return;
+  }
+
+  for (int e = threadIdx.x; e < N * kSeq; e += kThreads) {
+    const int s = e & (kSeq - 1), i = e / kSeq;
+    A[i * kSeq + s] = load_elem(i, s);
   }
   __syncthreads();
-  float2* X = block_fft_pp_plan<N, kSeq, kThreads, DIR, typename FftPlan3<N>::type>(A, Bf, tw);
+  float2* X = block_fft_pp_plan<N, kSeq, kThreads, DIR, Plan>(A, Bf, tw);
 
+  if (ST != V3_ST_THRESH) {
+    for (int e = threadIdx.x; e < N * kSeq; e += kThreads) {
+      const int s = e & (kSeq - 1), i = e / kSeq;
+      store_elem(i, s, X[i * kSeq + s]);
+    }
+    return;
+  }
   float ta = -1.f, tb = -1.f;
-  if (ST == V3_ST_THRESH && P.th) {
+  if (P.th) {
     ta = P.th[item * P.nb_item + P.ia];
     if (P.ib >= 0) tb = P.th[item * P.nb_item + P.ib];
   }
@@ -111,50 +172,26 @@ __global__ void __launch_bounds__(kThreads) k_v3_pass(float2* __restrict__ out, 
     const int s = e & (kSeq - 1), i = e / kSeq;
     const bool st = i >= P.out_lo && i < P.out_lo + P.out_n;
     const float2 v = X[i * kSeq + s];
-    const size_t g = off + (size_t)(i * si + s * ss);
-    if (ST == V3_ST_CPLX) {
-      if (st) out[wbase + g] = v;
-    } else if (ST == V3_ST_SPEC) {
-      if (st) {
-        const float2 c = __ldg(&P.spec[g]);
-        const float2 prod = make_float2(c.x * v.x + c.y * v.y, c.x * v.y - c.y * v.x);  // conj(c) * v
-        float2 o = prod;
-        if (!P.first) {
-          const float2 q = out[wbase + g];
-          o = make_float2(q.x + prod.x, q.y + prod.y);
-        }
-        out[wbase + g] = o;
-      }
-    } else {
-      int x, y, z;
-      pass_coords(P.axis, a, b0 + s, i, x, y, z);
-      const size_t r = ((size_t)(x - P.o0) * P.r1 + (y - P.o1)) * P.r2 + (z - P.o2);
-      if (ST == V3_ST_REAL) {
-        if (st) P.rdst[item * P.r_stride + r] = v.x * P.scale;
-      } else if (ST == V3_ST_PAIR) {
-        if (st) {
-          P.rdst[item * P.r_stride + r] = v.x * P.scale;
-          if (P.rdst2) P.rdst2[item * P.r_stride + r] = v.y * P.scale;
-        }
-      } else {  // V3_ST_THRESH (ThresholdShCoeff.m:7 zeroes |c| <= t)
-        const float ca = v.x * P.scale;
-        const float cb = P.ib >= 0 ? v.y * P.scale : 0.f;
-        const bool ka = st && !(fabsf(ca) <= ta);
-        const bool kb = st && P.ib >= 0 && !(fabsf(cb) <= tb);
-        if (st) {
-          float* acc = P.rdst + item * P.r_stride + r;
-          *acc += (ka ? ca : 0.f) + (kb ? cb : 0.f);
-        }
-        if (P.mwa) {  // uniform across the grid: every lane reaches the ballots
-          const unsigned lane = threadIdx.x & 31;
-          const unsigned ba = __ballot_sync(0xffffffffu, ka);
-          const unsigned bb = __ballot_sync(0xffffffffu, kb);
-          if (st && s == 0) {
-            const size_t mb = item * P.m_stride + (r >> 3);
-            P.mwa[mb] = (uint8_t)((ba >> (lane & 24)) & 0xffu);
-            if (P.mwb) P.mwb[mb] = (uint8_t)((bb >> (lane & 24)) & 0xffu);
-          }
-        }
+    int x, y, z;
+    pass_coords(P.axis, a, b0 + s, i, x, y, z);
+    const size_t r = ((size_t)(x - P.o0) * P.r1 + (y - P.o1)) * P.r2 + (z - P.o2);
+    // V3_ST_THRESH (ThresholdShCoeff.m:7 zeroes |c| <= t)
+    const float ca = v.x * P.scale;
+    const float cb = P.ib >= 0 ? v.y * P.scale : 0.f;
+    const bool ka = st && !(fabsf(ca) <= ta);
+    const bool kb = st && P.ib >= 0 && !(fabsf(cb) <= tb);
+    if (st) {
+      float* acc = P.rdst + item * P.r_stride + r;
+      *acc += (ka ? ca : 0.f) + (kb ? cb : 0.f);
+    }
+    if (P.mwa) {  // uniform across the grid: every lane reaches the ballots
+      const unsigned lane = threadIdx.x & 31;
+      const unsigned ba = __ballot_sync(0xffffffffu, ka);
+      const unsigned bb = __ballot_sync(0xffffffffu, kb);
+      if (st && s == 0) {
+        const size_t mb = item * P.m_stride + (r >> 3);
+        P.mwa[mb] = (uint8_t)((ba >> (lane & 24)) & 0xffu);
+        if (P.mwb) P.mwb[mb] = (uint8_t)((bb >> (lane & 24)) & 0xffu);
       }
     }
   }
@@ -186,7 +223,7 @@ bool v3_pass_len_supported(int n) {
 }
 
 cudaError_t prepare_v3_pass(int n) {
-  const int sm = (int)(2 * (size_t)n * kSeq * sizeof(float2));
+  const int sm = (int)(2 * (size_t)(n + 2) * kSeq * sizeof(float2));
   cudaError_t e = cudaSuccess;
   switch (n) {
 #define ONE(n, d, l, s)                                                                                  \
@@ -207,7 +244,7 @@ cudaError_t launch_v3_pass(int N, int dir, int ld, int st, float2* out, const fl
                            const float2* tw, int nitems, cudaStream_t stream) {
   if (P.b_n <= 0 || P.b_n % kSeq || P.a_n <= 0) return cudaErrorInvalidValue;
   const dim3 grid((unsigned)(P.a_n * (P.b_n / kSeq)), (unsigned)nitems);
-  const size_t sm = 2 * (size_t)N * kSeq * sizeof(float2);
+  const size_t sm = 2 * (size_t)(N + 2) * kSeq * sizeof(float2);
   count_launch();
   switch (N) {
 #define ONE(n, d, l, s)                                                 \
