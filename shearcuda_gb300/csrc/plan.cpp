@@ -132,6 +132,7 @@ struct nsst_plan {
   RowJob* gj_rows_T = nullptr;         // band -> bandT, threshold
   ColJob* gj_synth_T = nullptr;        // bandT -> sum
   int saved_n = 0;
+  int sm_count = 152;  // streaming multiprocessors of the plan's device
   RowJob* gj_rows_backward = nullptr;  // band (plan arena) + band2 -> band2
   ColJob* gj_synthesis = nullptr;      // band2 -> sum2
   RowJob* gj_rows_lev_inv = nullptr;   // sum2 -> gy[1..]
@@ -358,6 +359,12 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   if (ce != cudaSuccess) {
     p->th_host = nullptr;
     return destroy(cuda_fail(ce, "pinned threshold staging"));
+  }
+  {
+    int dev = 0, smc = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && smc > 0)
+      p->sm_count = smc;
   }
   ce = cudaEventCreateWithFlags(&p->th_done, cudaEventDisableTiming);
   if (ce != cudaSuccess) return destroy(cuda_fail(ce, "cudaEventCreate"));
@@ -748,6 +755,23 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
   return NSST_OK;
 }
 
+// The band analysis of n active items: one CTA per (level, item) column
+// group streams all bands of the level when that grid fills the GPU once (two
+// CTAs per SM); smaller batches (a single image) keep one CTA per (band,
+// item) column group, which has ndir times more CTAs.
+nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st) {
+  float2* base = (float2*)(grad ? p->garena : p->arena);
+  const size_t ctas = (size_t)n * p->nlev * (p->WH / 8);
+  if (ctas >= (size_t)2 * p->sm_count) {
+    NSST_CUDA(launch_cols(ColOp::AnalysisLevel, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
+                          p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, p->twH, st));
+  } else {
+    NSST_CUDA(launch_cols(ColOp::Analysis, grad ? p->gj_analysis : p->j_analysis, p->B * p->ndir_total, n, p->H,
+                          p->W, base, base, p->spec, 0, p->twH, st));
+  }
+  return NSST_OK;
+}
+
 // The fused batched pipeline (no host work, no allocation): capturable.
 // keep: the differentiable forward writes the thresholded bands to bandT,
 // leaving the pre-threshold band spectra (and the pyramid's lowpass) for
@@ -766,8 +790,7 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   timer_mark(p, "fft_rows_fwd", st);
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
   timer_mark(p, "fft_cols_fwd", st);
-  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
-                        (size_t)H * p->WH, p->twH, st));
+  NSST_TRY(enqueue_band_analysis(p, n, false, st));
   timer_mark(p, "band_analysis_cols", st);
   if (keep) {
     NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW,
@@ -819,8 +842,7 @@ nsst_status enqueue_band_maxima(nsst_plan* p, int n, const float* const* x, unsi
   NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
   NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
-                        (size_t)H * p->WH, p->twH, st));
+  NSST_TRY(enqueue_band_analysis(p, n, false, st));
   NSST_CUDA(launch_rows_max(p->j_rows_bands, B * p->ndir_total, n, H, W, A, p->twWh, p->twW, bits, st));
   for (int i = 0; i < n; i++)
     NSST_CUDA(launch_plane_maxabs(ys[(size_t)i], HW, 1, bits + (size_t)i * p->nbands, kRedBlocks, st));
@@ -1494,16 +1516,14 @@ nsst_status tau_backward(nsst_plan* p, const float* const* x, const float* const
     NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0,
                           st));
     NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
-    NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->j_analysis_lev, B * p->nlev, n, H, W, A2, A2, p->spec,
-                          (size_t)H * p->WH, p->twH, st));
+    NSST_TRY(enqueue_band_analysis(p, n, false, st));
     timer_mark(p, "recompute_coefficients", st);
   }
   // 2. d loss / d thresholded coefficients = D P_s^T grad_out
   NSST_TRY(run_atrousrec_adjoint(p, n, grad_out, gyp.data(), st));
   NSST_CUDA(launch_rows(RowOp::Fwd, p->gj_rows_lev_fwd, B * p->nlev, n, H, W, G, G, p->twWh, p->twW, nullptr, 0, st));
   NSST_CUDA(launch_cols(ColOp::Fwd, p->gj_cols_lev, B * p->nlev, n, H, W, G2, G2, nullptr, 0, p->twH, st));
-  NSST_CUDA(launch_cols(ColOp::AnalysisLevel, p->gj_analysis_lev, B * p->nlev, n, H, W, G2, G2, p->spec,
-                        (size_t)H * p->WH, p->twH, st));
+  NSST_TRY(enqueue_band_analysis(p, n, true, st));
   timer_mark(p, "gradient_analysis", st);
   // 3. threshold subgradient per band (+ tau partials), then D^T
   const size_t pstride = (size_t)B * p->ntiles;
