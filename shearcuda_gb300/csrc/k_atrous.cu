@@ -33,6 +33,9 @@ constexpr int kAtP = 8;     // outputs per thread and column (poly rows)
 constexpr int kAtTY = 8;    // thread rows
 constexpr int kAtRows = kAtP * kAtTY;  // poly rows per tile
 constexpr int kAtThreads = kAtHX * kAtTY;
+// Launches whose 64-row grid would not fill the GPU (a single image, a few
+// small images) use tiles of half the height: P = 4 outputs per thread.
+constexpr int kAtPSmall = 4;
 
 __device__ __forceinline__ int mirror_index(int i, int n) {
   if (i < 0) i = -1 - i;
@@ -44,13 +47,13 @@ __device__ __forceinline__ int mirror_index(int i, int n) {
 // out[r][c] += sum_{a,b} taps[a][b] * X[r + M(a - ORG)][c + M(b - ORG)] for this
 // thread's 16 rows.  Forward steps: ORG = (F-1)/2 and X mirror-extended;
 // adjoint steps (ZERO): ORG = F-1 and X zero-extended.
-template <int F, bool ZERO>
+template <int F, bool ZERO, int P>
 __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
                                                   int prow0, int col0, const float* __restrict__ taps,
                                                   const int* __restrict__ tapcols, int ntapcols, float* tile,
-                                                  float2 (&acc)[kAtP]) {
+                                                  float2 (&acc)[P]) {
   constexpr int C0 = ZERO ? F - 1 : (F - 1) / 2;
-  constexpr int TR = kAtRows + F - 1;
+  constexpr int TR = P * kAtTY + F - 1;
   const int TC = kAtTX + M * (F - 1);
   const int tid = threadIdx.x;
   // halo tile: one warp per tile row at a time (the row's source index and
@@ -74,12 +77,12 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
   }
   __syncthreads();
   const int tx = tid % kAtHX, ty = tid / kAtHX;
-  const float* base = tile + (ty * kAtP) * TC + tx;
+  const float* base = tile + (ty * P) * TC + tx;
   for (int ib = 0; ib < ntapcols; ib++) {
     const int b = tapcols[ib];
-    float2 col[kAtP + F - 1];
+    float2 col[P + F - 1];
 #pragma unroll
-    for (int t = 0; t < kAtP + F - 1; t++) {
+    for (int t = 0; t < P + F - 1; t++) {
       const float* q = base + t * TC + M * b;
       col[t] = make_float2(q[0], q[kAtHX]);
     }
@@ -88,14 +91,14 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
       const float w = taps[a * F + b];
       const float2 w2 = make_float2(w, w);
 #pragma unroll
-      for (int p = 0; p < kAtP; p++) acc[p] = __ffma2_rn(w2, col[p + a], acc[p]);
+      for (int p = 0; p < P; p++) acc[p] = __ffma2_rn(w2, col[p + a], acc[p]);
     }
   }
   __syncthreads();
 }
 
-// out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/64), njobs)
-template <int FA, int FB, bool ZERO = false>
+// out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/(8 P)), njobs)
+template <int FA, int FB, bool ZERO = false, int P = kAtP>
 __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
                                                         const __grid_constant__ AtrousTaps<FA> ta,
                                                         const __grid_constant__ AtrousTaps<FB> tb) {
@@ -107,29 +110,29 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
   const int Ho = job.Ho > 0 ? job.Ho : H, Wo = job.Wo > 0 ? job.Wo : W;  // 0: same as the input
   const int col0 = blockIdx.x * kAtTX;
   const int phase = blockIdx.y % M;
-  const int prow0 = (blockIdx.y / M) * kAtRows;
+  const int prow0 = (blockIdx.y / M) * (P * kAtTY);
   const int nprow = (Ho - phase + M - 1) / M;  // output poly rows of this phase
   if (col0 >= Wo || prow0 >= nprow) return;
-  float2 acc[kAtP];
+  float2 acc[P];
 #pragma unroll
-  for (int p = 0; p < kAtP; p++) acc[p] = make_float2(0.f, 0.f);
+  for (int p = 0; p < P; p++) acc[p] = make_float2(0.f, 0.f);
 
   for (int e = threadIdx.x; e < FA * FA; e += kAtThreads) s_taps[e] = ta.w[e];
   for (int e = threadIdx.x; e < ta.ncols; e += kAtThreads) s_cols[e] = ta.cols[e];
   __syncthreads();
-  atrous_accumulate<FA, ZERO>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
+  atrous_accumulate<FA, ZERO, P>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
   if (FB > 0 && job.xb != nullptr) {
     for (int e = threadIdx.x; e < FB * FB; e += kAtThreads) s_taps[e] = tb.w[e];
     for (int e = threadIdx.x; e < tb.ncols; e += kAtThreads) s_cols[e] = tb.cols[e];
     __syncthreads();
-    atrous_accumulate<(FB > 0 ? FB : 1), ZERO>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
-                                                at_smem, acc);
+    atrous_accumulate<(FB > 0 ? FB : 1), ZERO, P>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
+                                                   at_smem, acc);
   }
   const int tx = threadIdx.x % kAtHX, ty = threadIdx.x / kAtHX;
   const int c = col0 + tx;
 #pragma unroll
-  for (int p = 0; p < kAtP; p++) {
-    const int pr = prow0 + ty * kAtP + p;
+  for (int p = 0; p < P; p++) {
+    const int pr = prow0 + ty * P + p;
     if (pr < nprow) {
       float* o = job.out + (size_t)(phase + M * pr) * Wo;
       if (c < Wo) o[c] = acc[p].x;
@@ -165,10 +168,24 @@ static cudaError_t prepare_atrous_t(int Mmax) {
   std::lock_guard<std::mutex> lk(mu);
   if (dev >= 0 && dev < kDevs && configured[dev] >= want) return cudaSuccess;
   e = cudaFuncSetAttribute(k_atrous<FA, FB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_atrous<FA, FB, false, kAtPSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)want);
   if (e == cudaSuccess && FB == 0)
     e = cudaFuncSetAttribute(k_atrous<FA, FB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
   if (e == cudaSuccess && dev >= 0 && dev < kDevs) configured[dev] = want;
   return e;
+}
+
+static int sm_count() {
+  static const int n = [] {
+    int dev = 0, c = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || c <= 0)
+      return 152;
+    return c;
+  }();
+  return n;
 }
 
 template <int FA, int FB>
@@ -182,7 +199,12 @@ static cudaError_t launch_atrous_t(const AtrousJobs& jobs, int njobs, int maxH, 
   const int nprow_max = (maxH + M - 1) / M;
   dim3 grid((maxW + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
   count_launch();
-  k_atrous<FA, FB, false><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  if ((size_t)grid.x * grid.y * grid.z < (size_t)2 * sm_count()) {  // half-height tiles: twice the CTAs
+    grid.y = M * ((nprow_max + kAtPSmall * kAtTY - 1) / (kAtPSmall * kAtTY));
+    k_atrous<FA, FB, false, kAtPSmall><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  } else {
+    k_atrous<FA, FB, false><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  }
   return cudaGetLastError();
 }
 
