@@ -47,7 +47,9 @@ __device__ __forceinline__ int mirror_index(int i, int n) {
 // out[r][c] += sum_{a,b} taps[a][b] * X[r + M(a - ORG)][c + M(b - ORG)] for this
 // thread's 16 rows.  Forward steps: ORG = (F-1)/2 and X mirror-extended;
 // adjoint steps (ZERO): ORG = F-1 and X zero-extended.
-template <int F, bool ZERO, int P>
+// ZR: tap rows 1 and F-2 are zero (the 'maxflat' filters, atrousfilters.m:
+// the quadrant tables' second row is zero) and are skipped at compile time.
+template <int F, bool ZERO, int P, bool ZR = false>
 __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
                                                   int prow0, int col0, const float* __restrict__ taps,
                                                   const int* __restrict__ tapcols, int ntapcols, float* tile,
@@ -88,6 +90,7 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
     }
 #pragma unroll
     for (int a = 0; a < F; a++) {
+      if (ZR && (a == 1 || a == F - 2)) continue;
       const float w = taps[a * F + b];
       const float2 w2 = make_float2(w, w);
 #pragma unroll
@@ -98,7 +101,7 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
 }
 
 // out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/(8 P)), njobs)
-template <int FA, int FB, bool ZERO = false, int P = kAtP>
+template <int FA, int FB, bool ZERO = false, int P = kAtP, bool ZR = false>
 __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
                                                         const __grid_constant__ AtrousTaps<FA> ta,
                                                         const __grid_constant__ AtrousTaps<FB> tb) {
@@ -120,13 +123,13 @@ __global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ A
   for (int e = threadIdx.x; e < FA * FA; e += kAtThreads) s_taps[e] = ta.w[e];
   for (int e = threadIdx.x; e < ta.ncols; e += kAtThreads) s_cols[e] = ta.cols[e];
   __syncthreads();
-  atrous_accumulate<FA, ZERO, P>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
+  atrous_accumulate<FA, ZERO, P, ZR>(job.xa, H, W, M, phase, prow0, col0, s_taps, s_cols, ta.ncols, at_smem, acc);
   if (FB > 0 && job.xb != nullptr) {
     for (int e = threadIdx.x; e < FB * FB; e += kAtThreads) s_taps[e] = tb.w[e];
     for (int e = threadIdx.x; e < tb.ncols; e += kAtThreads) s_cols[e] = tb.cols[e];
     __syncthreads();
-    atrous_accumulate<(FB > 0 ? FB : 1), ZERO, P>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols, tb.ncols,
-                                                   at_smem, acc);
+    atrous_accumulate<(FB > 0 ? FB : 1), ZERO, P, ZR>(job.xb, H, W, M, phase, prow0, col0, s_taps, s_cols,
+                                                       tb.ncols, at_smem, acc);
   }
   const int tx = threadIdx.x % kAtHX, ty = threadIdx.x / kAtHX;
   const int c = col0 + tx;
@@ -171,6 +174,12 @@ static cudaError_t prepare_atrous_t(int Mmax) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_atrous<FA, FB, false, kAtPSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)want);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_atrous<FA, FB, false, kAtP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)want);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_atrous<FA, FB, false, kAtPSmall, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)want);
   if (e == cudaSuccess && FB == 0)
     e = cudaFuncSetAttribute(k_atrous<FA, FB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
   if (e == cudaSuccess && dev >= 0 && dev < kDevs) configured[dev] = want;
@@ -188,6 +197,14 @@ static int sm_count() {
   return n;
 }
 
+// rows 1 and F-2 of an F x F filter all zero (F >= 5)
+static bool zero_rows_1(const float* h, int F) {
+  if (!h || F < 5) return false;
+  for (int b = 0; b < F; b++)
+    if (h[F + b] != 0.0f || h[(F - 2) * F + b] != 0.0f) return false;
+  return true;
+}
+
 template <int FA, int FB>
 static cudaError_t launch_atrous_t(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, const float* ha,
                                    const float* hb, cudaStream_t st) {
@@ -199,11 +216,18 @@ static cudaError_t launch_atrous_t(const AtrousJobs& jobs, int njobs, int maxH, 
   const int nprow_max = (maxH + M - 1) / M;
   dim3 grid((maxW + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
   count_launch();
+  const bool zr = zero_rows_1(ha, FA) && (FB == 0 || zero_rows_1(hb, FB));
   if ((size_t)grid.x * grid.y * grid.z < (size_t)2 * sm_count()) {  // half-height tiles: twice the CTAs
     grid.y = M * ((nprow_max + kAtPSmall * kAtTY - 1) / (kAtPSmall * kAtTY));
-    k_atrous<FA, FB, false, kAtPSmall><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+    if (zr)
+      k_atrous<FA, FB, false, kAtPSmall, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+    else
+      k_atrous<FA, FB, false, kAtPSmall><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
   } else {
-    k_atrous<FA, FB, false><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+    if (zr)
+      k_atrous<FA, FB, false, kAtP, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+    else
+      k_atrous<FA, FB, false><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
   }
   return cudaGetLastError();
 }
