@@ -47,8 +47,11 @@ __device__ __forceinline__ int mirror_index(int i, int n) {
 // out[r][c] += sum_{a,b} taps[a][b] * X[r + M(a - ORG)][c + M(b - ORG)] for this
 // thread's 16 rows.  Forward steps: ORG = (F-1)/2 and X mirror-extended;
 // adjoint steps (ZERO): ORG = F-1 and X zero-extended.
-// ZR: tap rows 1 and F-2 are zero (the 'maxflat' filters, atrousfilters.m:
-// the quadrant tables' second row is zero) and are skipped at compile time.
+// ZR: tap rows 1 and F-2 are zero and symmetric columns (tap column b equals
+// column F-1-b) -- the mirrored-quadrant filters of atrousfilters.m
+// ('maxflat').  The zero rows are skipped at compile time, and each pair of
+// mirrored input columns is added once (FADD2) before the shared taps
+// multiply it: half the packed FMAs of the column pairs.
 template <int F, bool ZERO, int P, bool ZR = false>
 __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, int H, int W, int M, int phase,
                                                   int prow0, int col0, const float* __restrict__ taps,
@@ -82,11 +85,22 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
   const float* base = tile + (ty * P) * TC + tx;
   for (int ib = 0; ib < ntapcols; ib++) {
     const int b = tapcols[ib];
+    if (ZR && b > (F - 1) / 2) break;  // tapcols ascend; the mirrored half came with its partner
     float2 col[P + F - 1];
+    if (ZR && b < (F - 1) / 2) {
+      const int bm = F - 1 - b;
 #pragma unroll
-    for (int t = 0; t < P + F - 1; t++) {
-      const float* q = base + t * TC + M * b;
-      col[t] = make_float2(q[0], q[kAtHX]);
+      for (int t = 0; t < P + F - 1; t++) {
+        const float* q = base + t * TC + M * b;
+        const float* qm = base + t * TC + M * bm;
+        col[t] = __fadd2_rn(make_float2(q[0], q[kAtHX]), make_float2(qm[0], qm[kAtHX]));
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < P + F - 1; t++) {
+        const float* q = base + t * TC + M * b;
+        col[t] = make_float2(q[0], q[kAtHX]);
+      }
     }
 #pragma unroll
     for (int a = 0; a < F; a++) {
@@ -102,7 +116,7 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
 
 // out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/(8 P)), njobs)
 template <int FA, int FB, bool ZERO = false, int P = kAtP, bool ZR = false>
-__global__ void __launch_bounds__(kAtThreads) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
+__global__ void __launch_bounds__(kAtThreads, 3) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
                                                         const __grid_constant__ AtrousTaps<FA> ta,
                                                         const __grid_constant__ AtrousTaps<FB> tb) {
   extern __shared__ float at_smem[];
@@ -197,11 +211,15 @@ static int sm_count() {
   return n;
 }
 
-// rows 1 and F-2 of an F x F filter all zero (F >= 5)
+// rows 1 and F-2 of an F x F filter all zero (F >= 5) and its columns
+// mirror-symmetric (column b equals column F-1-b, nonzero together)
 static bool zero_rows_1(const float* h, int F) {
   if (!h || F < 5) return false;
   for (int b = 0; b < F; b++)
     if (h[F + b] != 0.0f || h[(F - 2) * F + b] != 0.0f) return false;
+  for (int a = 0; a < F; a++)
+    for (int b = 0; b < F; b++)
+      if (h[a * F + b] != h[a * F + (F - 1 - b)]) return false;
   return true;
 }
 
