@@ -116,7 +116,7 @@ __device__ __forceinline__ void atrous_accumulate(const float* __restrict__ x, i
 
 // out = conv(xa, filter A) [+ conv(xb, filter B)].  grid = (W/64, M * ceil(ceil(H/M)/(8 P)), njobs)
 template <int FA, int FB, bool ZERO = false, int P = kAtP, bool ZR = false>
-__global__ void __launch_bounds__(kAtThreads, 3) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
+__global__ void __launch_bounds__(kAtThreads, (FA <= 13 && FB == 0) ? 4 : 3) k_atrous(const __grid_constant__ AtrousJobs jobs, int M,
                                                         const __grid_constant__ AtrousTaps<FA> ta,
                                                         const __grid_constant__ AtrousTaps<FB> tb) {
   extern __shared__ float at_smem[];
