@@ -196,6 +196,9 @@ static cudaError_t prepare_atrous_t(int Mmax) {
                              (int)want);
   if (e == cudaSuccess && FB == 0)
     e = cudaFuncSetAttribute(k_atrous<FA, FB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+  if (e == cudaSuccess && FB == 0)
+    e = cudaFuncSetAttribute(k_atrous<FA, FB, true, kAtP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)want);
   if (e == cudaSuccess && dev >= 0 && dev < kDevs) configured[dev] = want;
   return e;
 }
@@ -261,7 +264,10 @@ static cudaError_t launch_atrous_full_t(const AtrousJobs& jobs, int njobs, int m
   const int nprow_max = (maxHo + M - 1) / M;
   dim3 grid((maxWo + kAtTX - 1) / kAtTX, M * ((nprow_max + kAtRows - 1) / kAtRows), njobs);
   count_launch();
-  k_atrous<F, 0, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  if (zero_rows_1(h, F))  // the same filter structure as the forward steps
+    k_atrous<F, 0, true, kAtP, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
+  else
+    k_atrous<F, 0, true><<<grid, kAtThreads, sm, st>>>(jobs, M, ta, tb);
   return cudaGetLastError();
 }
 
