@@ -208,6 +208,10 @@ def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
         # read every band once, write the level sum
         'band_synthesis_cols': 4 * N * nbands_dir + 4 * N * nlev,
         'fft_rows_fwd': 8 * N * nlev, 'fft_cols_fwd': 8 * N * nlev, 'fft_rows_inv': 8 * N * nlev,
+        # the spectral pyramid (FP32 planes, 4 B/px; packed spectra 4 B/px)
+        'dct_rows_image': 8 * N, 'dct_cols_image': 8 * N, 'dct_cols_image_out': 8 * N,
+        'dct_rows_levels': 8 * N * nlev, 'dct_cols_levels': 8 * N * nlev, 'dct_cols_sums': 8 * N * nlev,
+        'dct_rows_synthesis': (4 * nlev + 8) * N,
     }
     if stage.startswith('atrous_dec'):
         return 8 * N * nimg  # read the lowpass, write one output
@@ -217,6 +221,11 @@ def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
     # spectra: read once per launch (shared by the batch) where used
     if stage in ('band_analysis_cols', 'band_synthesis_cols'):
         b += 4 * N * nbands_dir
+    # level response tables: read once per launch
+    if stage == 'dct_rows_levels':
+        b += 4 * N * nlev
+    if stage == 'dct_rows_synthesis':
+        b += 4 * N * (nlev + 1)
     return b
 
 

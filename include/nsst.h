@@ -47,8 +47,18 @@ typedef struct nsst_config {
   int dcomp[NSST_MAX_LEVELS];   /* level i has 2^dcomp[i] directions, coarse -> fine */
   int dsize[NSST_MAX_LEVELS];   /* local support of level i's shearing filter */
   char lpfilt[16];              /* pyramid filter name, NUL-terminated */
-  int pyramid;                  /* NSST_PYRAMID_AUTO or _DIRECT: the dilated direct
-                                   convolution; _SPECTRAL is reserved and rejected */
+  int pyramid;                  /* how nsst_denoise(_batch) runs the pyramid:
+                                   _DIRECT: dilated direct convolutions;
+                                   _SPECTRAL: in the 2-D DCT-II domain, where each
+                                   atrousdec.m / atrousrec.m step is a pointwise
+                                   product merged into the directional FFT passes
+                                   (same results to FP32 rounding; needs pyramid
+                                   filters symmetric in both axes, as all of
+                                   atrousfilters.m's sets are, else the plan is
+                                   rejected); _AUTO: spectral where the filters
+                                   allow it.  Calls that threshold the lowpass band
+                                   or pass images not 16-byte aligned, and every
+                                   other entry point, use the direct pyramid. */
 } nsst_config;
 
 typedef struct nsst_plan nsst_plan;

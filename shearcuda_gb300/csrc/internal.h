@@ -49,6 +49,16 @@ struct AtrousJobs {  // passed by value
   AtrousJob j[kMaxAtrousJobs];
 };
 
+// Per-item image pointers of the DCT pyramid's first and last passes (the
+// caller's buffers), passed by value; rows of W floats, 16-byte aligned.
+struct DctIo {
+  const float* src[kMaxAtrousJobs];
+  float* dst[kMaxAtrousJobs];
+};
+// column transforms of the DCT pyramid (k_dct.cu): DCT-II, DCT-III, and
+// DCT-III followed by the forward FFT
+enum { kDct2 = 0, kDct3 = 1, kDctAna = 2 };
+
 struct FoldJob {
   const float* z1;  // first source (extended domain) / or c for the lowpass mask
   const float* z2;  // optional second source / or g for the lowpass mask
@@ -104,6 +114,21 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
                         cudaStream_t st);
 cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,
                           int FB, const float* hb, cudaStream_t st);
+// The DCT-domain pyramid of the fused pipeline (k_dct.cu).
+cudaError_t prepare_dct_kernels(int H, int WH);
+cudaError_t launch_dct_rows_fwd(const DctIo& io, int n, int H, int W, const float2* twWh, const float4* twD,
+                                cudaStream_t st);
+cudaError_t launch_dct_rows_ana(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                                void* dst_base, const float* resp, size_t resp_stride, const float2* twWh,
+                                const float2* twW, const float4* twD, cudaStream_t st);
+cudaError_t launch_dct_rows_syn(const RowJob* jobs, int njobs, int n_active, int nlev, size_t lev_stride, int H,
+                                int W, const void* src_base, void* dst_base, const float* xbase, size_t xstride,
+                                const float* resp, size_t resp_stride, const float* tlow, const float2* twWh,
+                                const float2* twW, const float4* twD, cudaStream_t st);
+cudaError_t launch_dct_cols(int mode, const ColJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                            void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st);
+cudaError_t launch_dct_cols_out(const DctIo& io, int n, int H, int W, const float2* twH, const float2* wdH,
+                                cudaStream_t st);
 // Adjoint helper: out (Ho x Wo, extended domain) = zero-extended full
 // correlation of x with the *unflipped* filter h, Ho = H + M(F-1).
 cudaError_t launch_atrous_full(const AtrousJobs& jobs, int njobs, int maxHo, int maxWo, int M, int F, const float* h,
@@ -241,6 +266,16 @@ bool level_spectra(const std::vector<double>& filters, int ndir, int n1, int H, 
 
 std::vector<float2> twiddle_table(int n);            // exp(-2 pi i t / n), t < n
 std::vector<float2> half_twiddle_table(int n);       // exp(-2 pi i k / n), k < n/2
+
+// DCT-domain pyramid tables (host_dct.cpp): whether all four pyramid filters
+// are symmetric in both axes with odd sizes; the (2 L + 1) response planes
+// (H x W each: analysis per directional level, synthesis per directional
+// level, lowpass); row twiddles (exp(-i pi k / (2W)), exp(-2 pi i k / W)) for
+// k = 0..W/2; column twiddles exp(-i pi k / (2H)), k < H.
+bool filters_symmetric(const PyramidFilters& pf);
+void dct_pyramid_tables(const PyramidFilters& pf, int L, int H, int W, std::vector<float>* out);
+std::vector<float4> dct_row_twiddles(int W);
+std::vector<float2> dct_col_twiddles(int H);
 
 // -------------------------------------------- undecimated wavelets (k_wavelet.cu)
 // MakeONFilter.m: the orthonormal QMF of a family, f / norm(f); false if the

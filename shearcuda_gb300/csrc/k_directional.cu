@@ -22,34 +22,10 @@
 // Every kernel takes a job list (one job per image / level / band) in device
 // memory plus a tile index, so one launch covers a whole batch of images of
 // one size.
-#include "fft_core.cuh"
 #include "internal.h"
+#include "tiles.cuh"
 
 namespace nsst {
-
-// Tile shapes: a row CTA owns RS rows, a column CTA owns CS columns, each as two
-// ping-pong shared buffers [index][sequence] (dense, see block_fft_pp).  They keep a thread's share of a tile at <= 16 complex values and the
-// shared memory low enough for 2-3 resident CTAs per SM: the kernels are bound
-// by global-memory latency, so resident CTAs are what hides it.
-template <int N>
-struct RowCfg {  // N = W/2 complex points per row
-  static constexpr int RS = N >= 1024 ? 4 : 8;
-  // 256 = 16 x 16: a radix-16 pass has 16 butterflies per row, one per thread
-  static constexpr int T = N == 256 ? 128 : 256;
-  static constexpr int MINB = 1024 / T;  // <= 64 registers: at least 32 warps per SM
-  static constexpr int LD = RS;
-  static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
-  // one tile staged row-major with rows padded to N + 2 (holds the dense layout too)
-  static constexpr size_t smem_rm() { return (size_t)RS * (N + 2) * sizeof(float2); }
-};
-template <int N>
-struct ColCfg {  // N = H points per column
-  static constexpr int CS = N >= 1024 ? 4 : 8;
-  static constexpr int T = N >= 2048 ? 512 : 256;
-  static constexpr int LD = CS;
-  static constexpr int MINB = 1024 / T;  // in-place column passes: 4 CTAs of 256 threads per SM
-  static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
-};
 
 // The synthesis CTA keeps its running band sum in shared memory next to the
 // transform buffer and the next band's staging buffer.
@@ -83,18 +59,7 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
   return a > 0.0f ? copysignf(a, v) : 0.0f;
 }
 
-// FFT hooks (see block_fft_hook).
-template <int NSEQ>
-struct SmemLd {
-  const float2* p;
-  __device__ __forceinline__ float2 operator()(int i, int s) const { return p[i * NSEQ + s]; }
-};
-template <int NSEQ>
-struct SmemSt {
-  float2* p;
-  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[i * NSEQ + s] = v; }
-};
-// packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM below:
+// packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM (tiles.cuh):
 // Z[k] = E + iO with E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k;
 // k = 0 unpacks the two real bins.
 template <int NSEQ>
@@ -108,79 +73,6 @@ struct ThreshSt {
     p[i * NSEQ + s] = v;
   }
 };
-// Row-major staging of a CTA's RS rows with rows padded to WH + 2 elements:
-// the tile's global loads and stores then run along the rows (each warp a
-// contiguous 256-byte stretch), and the FFT's first and last passes, which
-// reach it through the functors below, see no bank conflicts.
-template <int WH, int RS, int T>
-__device__ __forceinline__ void fetch_rows_rm(float2* P, const float2* src) {
-  constexpr int WHP = WH + 2, CH = WH / 2;  // 16-byte chunks per row
-  for (int e = threadIdx.x; e < RS * CH; e += T) {
-    const int s = e / CH, c = e - s * CH;
-    cp_async16(P + s * WHP + 2 * c, src + (size_t)s * WH + 2 * c);
-  }
-  cp_async_commit();
-}
-template <int WH>
-struct C2RPreLdRM {  // C2RPreLd reading the padded row-major staging
-  const float2* X;
-  const float2* twW;
-  __device__ __forceinline__ float2 operator()(int k, int s) const {
-    const float2* row = X + s * (WH + 2);
-    const float2 xk = row[k];
-    if (k == 0) return make_float2(xk.x + xk.y, xk.x - xk.y);
-    const float2 xmc = cconj(row[WH - k]);
-    const float2 E = cadd(xk, xmc);
-    const float2 O = cmulc(csub(xk, xmc), __ldg(&twW[k]));
-    return make_float2(E.x - O.y, E.y + O.x);
-  }
-};
-template <int WH>
-struct SmemStRM {  // element (i, s) -> padded row-major
-  float2* p;
-  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[s * (WH + 2) + i] = v; }
-};
-template <int WH>
-struct SmemLdRM {  // element (i, s) <- padded row-major
-  const float2* p;
-  __device__ __forceinline__ float2 operator()(int i, int s) const { return p[s * (WH + 2) + i]; }
-};
-// padded row-major rows -> global rows, 16 bytes per thread and step
-template <int WH, int RS, int T>
-__device__ __forceinline__ void store_rows_rm(float2* __restrict__ dst, const float2* P) {
-  constexpr int CH = WH / 2;
-  for (int e = threadIdx.x; e < RS * CH; e += T) {
-    const int s = e / CH, c = e - s * CH;
-    *reinterpret_cast<float4*>(dst + (size_t)s * WH + 2 * c) =
-        *reinterpret_cast<const float4*>(P + s * (WH + 2) + 2 * c);
-  }
-}
-// packed-real post-processing of every index k (see r2c_post) fused with the
-// store of the CTA's rows, from the padded row-major layout along the rows:
-// X[k] = E + w^k O, E = (Z[k] + conj(Z[WH-k]))/2, O = (Z[k] - conj(Z[WH-k]))/(2i);
-// k = 0 packs the two real bins.
-template <int WH, int RS, int T>
-__device__ __forceinline__ void r2c_post_store_rm(float2* __restrict__ dst, const float2* Z,
-                                                  const float2* __restrict__ twW) {
-#pragma unroll 4
-  for (int e = threadIdx.x; e < WH * RS; e += T) {
-    const int k = e % WH, s = e / WH;
-    const float2* row = Z + s * (WH + 2);
-    const float2 zk = row[k];
-    float2 out;
-    if (k == 0) {
-      out = make_float2(zk.x + zk.y, zk.x - zk.y);
-    } else {
-      const float2 zmc = cconj(row[WH - k]);
-      const float2 E = cscale(cadd(zk, zmc), 0.5f);
-      const float2 d = cscale(csub(zk, zmc), 0.5f);
-      const float2 To = cmul(__ldg(&twW[k]), make_float2(d.y, -d.x));
-      out = cadd(E, To);
-    }
-    dst[(size_t)s * WH + k] = out;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Row kernels.  grid = (H / RS, njobs).
 // ---------------------------------------------------------------------------
@@ -347,18 +239,6 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
 // Column kernels.  grid = (WH / CS, njobs).
 // ---------------------------------------------------------------------------
 
-// Column hooks: element (i, s) of the CTA's column group is image element
-// (row i, column col0 + s) of an H x WH packed array.
-struct ColGlobalLd {
-  const float2* src;
-  int WH;
-  __device__ __forceinline__ float2 operator()(int i, int s) const { return src[(size_t)i * WH + s]; }
-};
-struct ColGlobalSt {
-  float2* dst;
-  int WH;
-  __device__ __forceinline__ void operator()(int i, int s, float2 v) const { dst[(size_t)i * WH + s] = v; }
-};
 // Wk .* Z for the analysis, with the packed DC/Nyquist column's
 // Z'[u] = P[u] Z[u] + M[u] conj(Z[-u]) (src, spec: column group origin)
 template <int H>

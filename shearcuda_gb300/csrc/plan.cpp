@@ -88,6 +88,20 @@ struct nsst_plan {
   RowJob* j_coeff_fwd = nullptr;      // caller coeffs -> band (item 0)
   RowJob* j_band_to_coeff = nullptr;  // band -> caller coeffs (item 0)
 
+  // DCT-domain pyramid of the fused pipeline (k_dct.cu).  X = DCT2(x) in pyr
+  // plane 0, the row-transformed intermediates in pyr plane 1.
+  bool dct_ok = false;         // the mode and the filters allow it: tables below allocated
+  bool dct_on = false;         // the fused pipeline uses it
+  float* dct_ra = nullptr;     // nlev x H x W analysis responses (directional level order)
+  float* dct_rs = nullptr;     // nlev x H x W synthesis responses
+  float* dct_tl = nullptr;     // H x W lowpass response
+  float4* twDW = nullptr;      // row twiddles, WH + 1
+  float2* wdH = nullptr;       // column twiddles, H
+  ColJob* j_dct_x = nullptr;   // pyr plane 1 -> pyr plane 0          (B)
+  RowJob* j_dct_ana = nullptr; // pyr plane 0 -> lev, item-major       (B*nlev)
+  ColJob* j_dct_sum = nullptr; // sum in place                         (B*nlev)
+  RowJob* j_dct_syn = nullptr; // sum (all levels) -> pyr plane 1      (B)
+
   std::vector<double> scalars;
   bool has_scalars = false;
   std::vector<double> norms;  // exact band norms (nsst_band_norms), computed on first use
@@ -189,8 +203,9 @@ int host_threads() {
 
 nsst_status validate_config(const nsst_config* cfg, int H, int W) {
   if (!cfg) return fail(NSST_ERR_INVALID_ARG, "config is NULL");
-  if (cfg->pyramid != NSST_PYRAMID_AUTO && cfg->pyramid != NSST_PYRAMID_DIRECT)
-    return fail(NSST_ERR_INVALID_ARG, "only the direct (dilated convolution) pyramid is implemented");
+  if (cfg->pyramid != NSST_PYRAMID_AUTO && cfg->pyramid != NSST_PYRAMID_DIRECT &&
+      cfg->pyramid != NSST_PYRAMID_SPECTRAL)
+    return fail(NSST_ERR_INVALID_ARG, "unknown pyramid mode");
   // the dilated direct convolution stages a (64 + 2^(L-1)(F-1))-wide halo
   // tile in shared memory, which bounds the depth at 6 levels
   if (cfg->nlevels < 1 || cfg->nlevels > 6) return fail(NSST_ERR_INVALID_ARG, "nlevels must be in [1, 6]");
@@ -349,6 +364,19 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
   size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
   size_t o_j9 = take(sizeof(ColJob) * nL);
+  p->dct_ok = filters_symmetric(p->pf) && cfg->pyramid != NSST_PYRAMID_DIRECT;
+  if (cfg->pyramid == NSST_PYRAMID_SPECTRAL && !p->dct_ok)
+    return destroy(fail(NSST_ERR_INVALID_ARG, "the spectral pyramid needs pyramid filters symmetric in both axes"));
+  size_t o_dct = 0, o_twDW = 0, o_wdH = 0, o_jd1 = 0, o_jd2 = 0, o_jd3 = 0, o_jd4 = 0;
+  if (p->dct_ok) {
+    o_dct = take(sizeof(float) * HW * (2 * p->nlev + 1));
+    o_twDW = take(sizeof(float4) * (p->WH + 1));
+    o_wdH = take(sizeof(float2) * H);
+    o_jd1 = take(sizeof(ColJob) * NB);
+    o_jd2 = take(sizeof(RowJob) * nL);
+    o_jd3 = take(sizeof(ColJob) * nL);
+    o_jd4 = take(sizeof(RowJob) * NB);
+  }
   p->arena_bytes = off;
   ce = dev_alloc((void**)&p->arena, p->arena_bytes);
   if (ce != cudaSuccess) {
@@ -495,6 +523,44 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     if (ce == cudaSuccess) ce = up(p->j_band_to_coeff, j8.data(), j8.size() * sizeof(RowJob));
     if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload job lists"));
   }
+  if (p->dct_ok) {
+    p->dct_ra = (float*)(A + o_dct);
+    p->dct_rs = p->dct_ra + HW * p->nlev;
+    p->dct_tl = p->dct_rs + HW * p->nlev;
+    p->twDW = (float4*)(A + o_twDW);
+    p->wdH = (float2*)(A + o_wdH);
+    p->j_dct_x = (ColJob*)(A + o_jd1);
+    p->j_dct_ana = (RowJob*)(A + o_jd2);
+    p->j_dct_sum = (ColJob*)(A + o_jd3);
+    p->j_dct_syn = (RowJob*)(A + o_jd4);
+    std::vector<float> tab;
+    dct_pyramid_tables(p->pf, p->nlev, H, W, &tab);
+    auto tw = dct_row_twiddles(W);
+    auto wh = dct_col_twiddles(H);
+    auto f2 = [&](const void* ptr) { return (size_t)((const char*)ptr - A) / sizeof(float2); };
+    std::vector<ColJob> jx, js;
+    std::vector<RowJob> ja, jy;
+    for (int i = 0; i < B; i++) {
+      const size_t p0 = f2(p->pyr + i * p->s_pyr), p1 = f2(p->pyr + i * p->s_pyr + HW);
+      const size_t lev = f2(p->lev + i * p->s_lev), sum = f2(p->sum + i * p->s_sum);
+      jx.push_back(ColJob{p1, p0, 0, 0, 0, i});
+      jy.push_back(RowJob{sum, p1, 0, i});
+      for (int l = 0; l < p->nlev; l++) {
+        ja.push_back(RowJob{p0, lev + (size_t)l * HWh, l, i});
+        js.push_back(ColJob{sum + (size_t)l * HWh, sum + (size_t)l * HWh, 0, 0, 0, i});
+      }
+    }
+    ce = cudaMemcpy(p->dct_ra, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->twDW, tw.data(), tw.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->wdH, wh.data(), wh.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_x, jx.data(), jx.size() * sizeof(ColJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_ana, ja.data(), ja.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_sum, js.data(), js.size() * sizeof(ColJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_syn, jy.data(), jy.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = prepare_dct_kernels(H, p->WH);
+    if (ce != cudaSuccess) return destroy(cuda_fail(ce, "DCT pyramid tables"));
+    p->dct_on = true;
+  }
   ce = prepare_row_kernels(p->WH);
   if (ce == cudaSuccess) ce = prepare_col_kernels(H);
   if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[0], 0, Mmax);
@@ -530,7 +596,7 @@ nsst_status nsst_plan_create_from_file(const char* path, int H, int W, int B, ns
     cfg.dsize[l] = fs.dsize[l];
   }
   std::strcpy(cfg.lpfilt, "file");
-  cfg.pyramid = NSST_PYRAMID_DIRECT;
+  cfg.pyramid = NSST_PYRAMID_AUTO;
   return create_plan(&cfg, H, W, B, &fs, out);
 }
 
@@ -772,6 +838,68 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
   return NSST_OK;
 }
 
+// Whether a fused pipeline call can take the DCT-domain pyramid: symmetric
+// filters, an unthresholded lowpass (it never leaves the DCT domain), no saved
+// forward state (the adjoint reads the spatial pyramid), 16-byte aligned images.
+bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* out, bool lowpass_th, bool keep) {
+  if (!p->dct_on || lowpass_th || keep) return false;
+  for (int i = 0; i < n; i++)
+    if (!aligned16(x[i]) || !aligned16(out[i])) return false;
+  return true;
+}
+
+// The fused pipeline with the pyramid in the DCT-II domain (k_dct.cu): the
+// pyramid's analysis merges with the level FFTs, its synthesis with the
+// inverse level FFTs; the directional stage is the same.
+nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, float* const* out, int mode,
+                                const float* TH, cudaStream_t st) {
+  char* A = p->arena;
+  float2* A2 = (float2*)A;
+  const int B = p->B, H = p->H, W = p->W;
+  const size_t HW = (size_t)H * W;
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    DctIo io{};
+    for (int t = 0; t < cn; t++) {
+      io.src[t] = x[c0 + t];
+      io.dst[t] = p->pyr + (size_t)(c0 + t) * p->s_pyr + HW;
+    }
+    NSST_CUDA(launch_dct_rows_fwd(io, cn, H, W, p->twWh, p->twDW, st));
+  }
+  timer_mark(p, "dct_rows_image", st);
+  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_x, B, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_image", st);
+  NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, B * p->nlev, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW,
+                                st));
+  timer_mark(p, "dct_rows_levels", st);
+  NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_levels", st);
+  NSST_TRY(enqueue_band_analysis(p, n, false, st));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH, mode,
+                        st));
+  timer_mark(p, "band_rows_threshold", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
+                        p->twH, st));
+  timer_mark(p, "band_synthesis_cols", st);
+  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_sums", st);
+  NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A, p->pyr, p->s_pyr,
+                                p->dct_rs, HW, p->dct_tl, p->twWh, p->twW, p->twDW, st));
+  timer_mark(p, "dct_rows_synthesis", st);
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    DctIo io{};
+    for (int t = 0; t < cn; t++) {
+      io.src[t] = p->pyr + (size_t)(c0 + t) * p->s_pyr + HW;
+      io.dst[t] = out[c0 + t];
+    }
+    NSST_CUDA(launch_dct_cols_out(io, cn, H, W, p->twH, p->wdH, st));
+  }
+  timer_mark(p, "dct_cols_image_out", st);
+  return NSST_OK;
+}
+
 // The fused batched pipeline (no host work, no allocation): capturable.
 // keep: the differentiable forward writes the thresholded bands to bandT,
 // leaving the pre-threshold band spectra (and the pyramid's lowpass) for
@@ -783,6 +911,7 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
   const size_t HW = (size_t)H * W;
+  if (dct_path(p, n, x, out, lowpass_th, keep)) return enqueue_denoise_dct(p, n, x, out, mode, TH, st);
   std::vector<float*> ys(n);
   for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
   NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));

@@ -1,0 +1,142 @@
+"""The fused denoise pipeline with its pyramid in the DCT-II domain
+(NSST_PYRAMID_SPECTRAL, the default where the filters allow it) against the
+same pipeline with the direct dilated-convolution pyramid and against the
+FP64 oracle.
+
+Both compute atrousdec.m / atrousrec.m exactly in real arithmetic (each step
+is a pointwise product in the DCT-II domain of the symmetric extension); in
+FP32 they differ by rounding.  Tolerances:
+  * zero thresholds (perfect reconstruction): relative L2 <= 1e-5 to the input
+  * soft threshold (a 1-Lipschitz map): relative L2 <= 1e-5 between the paths
+  * hard threshold: relative L2 <= 1e-3 (coefficients within rounding of their
+    threshold flip), |PSNR difference| <= 0.01 dB to the oracle
+  * one image alone and the same image in a batch: bit-identical
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import DCOMP, DSIZE, K_DEMO, flat_scalars, rel_l2
+from oracle import nsst2d
+
+pytestmark = pytest.mark.gpu
+
+_plans = {}
+
+
+def _plan(H, W, pyramid, lpfilt='maxflat', batch=1):
+    import shearcuda_gb300 as sc
+    key = (H, W, pyramid, lpfilt, batch)
+    if key not in _plans:
+        p = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, lpfilt=lpfilt, pyramid=pyramid, batch=batch)
+        p.set_scalars(np.linspace(0.5, 1.5, p.nbands))
+        _plans[key] = p
+    return _plans[key]
+
+
+def _img(H, W, seed, cuda):
+    from shearcuda_gb300.synth import noisy_image
+    _, noisy = noisy_image(H, W, 20.0, seed)
+    return torch.tensor(noisy.astype(np.float32), device=cuda)
+
+
+def _stages(plan, x, K, mode=0):
+    import shearcuda_gb300 as sc
+    plan.enable_timers(True)
+    try:
+        sc.nsst_denoise(x, plan, 20.0, K, None, mode=mode)
+        return [n for n, _ in plan.read_timers(40)]
+    finally:
+        plan.enable_timers(False)
+
+
+@pytest.mark.parametrize('HW', [(256, 256), (256, 384), (384, 512), (512, 512), (768, 1024)])
+@pytest.mark.parametrize('lpfilt', ['maxflat', '9-7', 'pyr', 'pyrexc'])
+def test_spectral_pyramid_reconstructs(built_lib, cuda, HW, lpfilt):
+    import shearcuda_gb300 as sc
+    H, W = HW
+    if lpfilt != 'maxflat' and HW not in [(256, 384), (512, 512)]:
+        pytest.skip('other filter sets on two sizes')
+    p = _plan(H, W, sc.PYRAMID_SPECTRAL, lpfilt)
+    x = _img(H, W, 3, cuda)
+    assert 'dct_rows_levels' in _stages(p, x, [0] * 5)  # the spectral path ran
+    out = sc.nsst_denoise(x, p, 0.0, [0] * 5, None)
+    assert rel_l2(out.cpu().numpy(), x.cpu().numpy()) <= 1e-5
+
+
+@pytest.mark.parametrize('HW', [(256, 256), (384, 512), (512, 512)])
+@pytest.mark.parametrize('lpfilt', ['maxflat', '9-7'])
+def test_spectral_equals_direct(built_lib, cuda, HW, lpfilt):
+    import shearcuda_gb300 as sc
+    H, W = HW
+    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL, lpfilt), _plan(H, W, sc.PYRAMID_DIRECT, lpfilt)
+    x = _img(H, W, 4, cuda)
+    assert 'dct_rows_levels' not in _stages(pd, x, K_DEMO)
+    for mode, tol in [(sc.THRESH_SOFT, 1e-5), (sc.THRESH_HARD, 1e-3)]:
+        a = sc.nsst_denoise(x, ps, 20.0, K_DEMO, None, mode=mode).cpu().numpy()
+        b = sc.nsst_denoise(x, pd, 20.0, K_DEMO, None, mode=mode).cpu().numpy()
+        assert rel_l2(a, b) <= tol, (mode, rel_l2(a, b))
+
+
+def test_spectral_matches_oracle_psnr(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300.synth import noisy_image
+    H, W = 256, 384
+    clean, noisy = noisy_image(H, W, 20.0, 9)
+    n32 = noisy.astype(np.float32)
+    p = _plan(H, W, sc.PYRAMID_SPECTRAL)
+    sf = nsst2d.shear_spectra(H, W, DCOMP, DSIZE)
+    scal = nsst2d.nsst_scalars(H, W, sf, seed=100, nthreads=8)
+    out = sc.nsst_denoise(torch.tensor(n32, device=cuda), p, 20.0, K_DEMO, flat_scalars(scal)).cpu().numpy()
+    ref, _ = nsst2d.denoise(n32.astype(np.float64), 20.0, K_DEMO, scal, DCOMP, DSIZE, shear_f=sf, nthreads=8)
+    assert abs(nsst2d.psnr(clean, out) - nsst2d.psnr(clean, ref)) <= 0.01
+    assert rel_l2(out, ref) <= 1e-3
+
+
+def test_spectral_batch_equals_single_and_graphs(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    H, W = 256, 384
+    single = _plan(H, W, sc.PYRAMID_SPECTRAL)
+    batch = _plan(H, W, sc.PYRAMID_SPECTRAL, batch=3)
+    xs = [_img(H, W, 20 + i, cuda) for i in range(3)]
+    sig = [12.0, 20.0, 35.0]
+    outs = sc.nsst_denoise_batch(xs, batch, sig, K_DEMO, None)
+    for x, o, s in zip(xs, outs, sig):
+        ref = sc.nsst_denoise(x, single, s, K_DEMO, None)
+        np.testing.assert_array_equal(o.cpu().numpy(), ref.cpu().numpy())
+    batch.use_graphs(True)
+    try:
+        outs2 = sc.nsst_denoise_batch(xs, batch, sig, K_DEMO, None)
+        for o, o2 in zip(outs, outs2):
+            np.testing.assert_array_equal(o.cpu().numpy(), o2.cpu().numpy())
+    finally:
+        batch.use_graphs(False)
+
+
+def test_direct_fallbacks(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    H, W = 256, 256
+    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL), _plan(H, W, sc.PYRAMID_DIRECT)
+    x = _img(H, W, 5, cuda)
+    # a thresholded lowpass band takes the direct pyramid: the same bits as a direct plan
+    K = [1.0] + list(K_DEMO[1:])
+    assert 'dct_rows_levels' not in _stages(ps, x, K)
+    np.testing.assert_array_equal(sc.nsst_denoise(x, ps, 20.0, K, None).cpu().numpy(),
+                                  sc.nsst_denoise(x, pd, 20.0, K, None).cpu().numpy())
+    # an image 4 bytes off a 16-byte boundary takes it too
+    buf = torch.zeros(H * W + 1, device=cuda)
+    buf[1:] = x.reshape(-1)
+    xm = buf[1:].view(H, W)
+    a = sc.nsst_denoise(xm, ps, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    b = sc.nsst_denoise(x, ps, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    assert rel_l2(a, b) <= 1e-5
+
+
+def test_pyramid_modes(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    with pytest.raises(sc.NsstError):
+        sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256, pyramid=3)
+    # the default (auto) plan takes the spectral path for atrousfilters.m's sets
+    p = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256)
+    p.set_scalars(np.ones(p.nbands))
+    assert 'dct_rows_levels' in _stages(p, _img(256, 256, 6, cuda), K_DEMO)

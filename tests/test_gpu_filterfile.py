@@ -37,7 +37,7 @@ def test_plan_from_file_matches_constructed_plan(built_lib, cuda, tmp_path):
     assert rel_l2(rec.cpu().numpy(), noisy) <= 1e-5
 
 
-def test_spectral_pyramid_is_rejected(built_lib, cuda):
+def test_unknown_pyramid_mode_is_rejected(built_lib, cuda):
     import shearcuda_gb300 as sc
     with pytest.raises(sc.NsstError):
-        sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256, pyramid=sc.PYRAMID_SPECTRAL)
+        sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256, pyramid=7)

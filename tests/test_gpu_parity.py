@@ -115,8 +115,11 @@ def test_denoise_matches_oracle_psnr(built_lib, cuda, HW, mode):
 
 
 def test_fused_denoise_equals_materialised_chain(built_lib, cuda):
+    # with the direct pyramid the fused pass runs the chain's kernels
+    # (test_gpu_dct_pyramid.py covers the spectral pyramid)
     import shearcuda_gb300 as sc
-    clean, noisy32, shear, sf, scal = _setup(512, 512)
+    clean, noisy32, _, sf, scal = _setup(512, 512)
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 512, 512, pyramid=sc.PYRAMID_DIRECT)
     x = torch.tensor(noisy32, device=cuda)
     flat = flat_scalars(scal)
     fused = sc.nsst_denoise(x, shear, 20.0, K_DEMO, flat)
