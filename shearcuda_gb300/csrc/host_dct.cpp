@@ -66,7 +66,7 @@ void level_response(const std::vector<double>& h, int F, int M, int H, int W, st
 
 void dct_pyramid_tables(const PyramidFilters& pf, int L, int H, int W, std::vector<float>* out) {
   const size_t HW = (size_t)H * W;
-  out->assign((size_t)(2 * L + 1) * HW, 0.0f);
+  out->assign((size_t)(2 * L + 3) * HW, 0.0f);
   const double s = 1.0 / ((double)H * W);
   std::vector<double> ch(HW, 1.0), cg(HW, 1.0);  // running products of the h0 / g0 responses
   std::vector<double> G[4];
@@ -85,7 +85,13 @@ void dct_pyramid_tables(const PyramidFilters& pf, int L, int H, int W, std::vect
     }
   }
   float* tl = out->data() + (size_t)2 * L * HW;
-  for (size_t e = 0; e < HW; e++) tl[e] = (float)(s * ch[e] * cg[e]);  // lowpass: L h0 steps, L g0 steps
+  float* rl = tl + HW;
+  float* gl = rl + HW;
+  for (size_t e = 0; e < HW; e++) {
+    tl[e] = (float)(s * ch[e] * cg[e]);  // lowpass round trip: L h0 steps, L g0 steps
+    rl[e] = (float)(s * ch[e]);          // lowpass band (atrousdec.m's y{1})
+    gl[e] = (float)(s * cg[e]);          // lowpass synthesis (atrousrec.m's L g0 steps)
+  }
 }
 
 std::vector<float4> dct_row_twiddles(int W) {

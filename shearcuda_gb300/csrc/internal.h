@@ -55,9 +55,9 @@ struct DctIo {
   const float* src[kMaxAtrousJobs];
   float* dst[kMaxAtrousJobs];
 };
-// column transforms of the DCT pyramid (k_dct.cu): DCT-II, DCT-III, and
-// DCT-III followed by the forward FFT
-enum { kDct2 = 0, kDct3 = 1, kDctAna = 2 };
+// column transforms of the DCT pyramid (k_dct.cu): DCT-II, DCT-III, DCT-III
+// followed by the forward FFT, and DCT-III -> threshold -> DCT-II
+enum { kDct2 = 0, kDct3 = 1, kDctAna = 2, kDctThresh = 3 };
 
 struct FoldJob {
   const float* z1;  // first source (extended domain) / or c for the lowpass mask
@@ -120,13 +120,14 @@ cudaError_t launch_dct_rows_fwd(const DctIo& io, int n, int H, int W, const floa
                                 cudaStream_t st);
 cudaError_t launch_dct_rows_ana(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                                 void* dst_base, const float* resp, size_t resp_stride, const float2* twWh,
-                                const float2* twW, const float4* twD, cudaStream_t st);
+                                const float2* twW, const float4* twD, bool real_out, cudaStream_t st);
 cudaError_t launch_dct_rows_syn(const RowJob* jobs, int njobs, int n_active, int nlev, size_t lev_stride, int H,
                                 int W, const void* src_base, void* dst_base, const float* xbase, size_t xstride,
                                 const float* resp, size_t resp_stride, const float* tlow, const float2* twWh,
                                 const float2* twW, const float4* twD, cudaStream_t st);
 cudaError_t launch_dct_cols(int mode, const ColJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
-                            void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st);
+                            void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st,
+                            const float* thr = nullptr, int th_stride = 0, int th_mode = 0);
 cudaError_t launch_dct_cols_out(const DctIo& io, int n, int H, int W, const float2* twH, const float2* wdH,
                                 cudaStream_t st);
 // Adjoint helper: out (Ho x Wo, extended domain) = zero-extended full
@@ -268,9 +269,10 @@ std::vector<float2> twiddle_table(int n);            // exp(-2 pi i t / n), t < 
 std::vector<float2> half_twiddle_table(int n);       // exp(-2 pi i k / n), k < n/2
 
 // DCT-domain pyramid tables (host_dct.cpp): whether all four pyramid filters
-// are symmetric in both axes with odd sizes; the (2 L + 1) response planes
-// (H x W each: analysis per directional level, synthesis per directional
-// level, lowpass); row twiddles (exp(-i pi k / (2W)), exp(-2 pi i k / W)) for
+// are symmetric in both axes with odd sizes; the (2 L + 3) response planes
+// (H x W each, 1/(H W) folded in: analysis per directional level, synthesis
+// per directional level, the lowpass round trip, the lowpass analysis, the
+// lowpass synthesis); row twiddles (exp(-i pi k / (2W)), exp(-2 pi i k / W)) for
 // k = 0..W/2; column twiddles exp(-i pi k / (2H)), k < H.
 bool filters_symmetric(const PyramidFilters& pf);
 void dct_pyramid_tables(const PyramidFilters& pf, int L, int H, int W, std::vector<float>* out);

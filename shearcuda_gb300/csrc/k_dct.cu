@@ -61,6 +61,19 @@ struct DctShufLd {
   }
 };
 
+// The same order written by the last pass of a C2R whose element m is
+// (y[2m], y[2m+1]): v[m] = y[2m], v[W-1-m] = y[2m+1] (stride-1 stores, where
+// DctShufLd's reads are four floats apart)
+template <int WH>
+struct DctShufStRM {
+  float2* P;
+  __device__ __forceinline__ void operator()(int m, int s, float2 y) const {
+    float* v = reinterpret_cast<float*>(P + s * (WH + 2));
+    v[m] = y.x;
+    v[2 * WH - 1 - m] = y.y;
+  }
+};
+
 // The DCT-III output order undone: y[2m] = v[m], y[2m+1] = v[W-1-m]; element
 // m of y's complex view.
 template <int WH>
@@ -169,9 +182,9 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
 }
 
 // level analysis rows: (X .* R_level) -> DCT-III -> R2C -> packed half
-// spectrum rows.  job.src: X plane, job.dst: level spectrum, job.th_index:
-// the response plane.
-template <int WH>
+// spectrum rows; REAL: (X .* R) -> DCT-III -> real rows (the lowpass band).
+// job.src: X plane, job.dst: output plane, job.th_index: the response plane.
+template <int WH, bool REAL>
 __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
     k_dct_rows_ana(const RowJob* __restrict__ jobs, int n_active, const float2* src_base, float2* dst_base,
                    const float* __restrict__ resp, size_t resp_stride, const float2* __restrict__ twWh,
@@ -193,6 +206,15 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
   }
   __syncthreads();
   block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, SmemLdRM<WH>{A}, SmemStRM<WH>{A});
+  if (REAL) {
+    float2* dst = dst_base + job.dst + off;
+    for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
+      const int m = e % WH, s = e / WH;
+      const float* v = rowf<WH>(A, s);
+      dst[(size_t)s * WH + m] = make_float2(v[m], v[2 * WH - 1 - m]);
+    }
+    return;
+  }
   block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, DctUnshufLd<WH>{A}, SmemStRM<WH>{A});
   r2c_post_store_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
 }
@@ -226,12 +248,15 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
       *reinterpret_cast<float4*>(S + s * (WH + 2) + 2 * c) = make_float4(x.x * t.x, x.y * t.y, x.z * t.z, x.w * t.w);
     }
   }
+  // (a prefetch of the next level into a third buffer measured no faster:
+  // fewer CTAs per SM)
   for (int l = 0; l < nlev; l++) {
     fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + (size_t)l * lev_stride + off);
     cp_async_wait_all();
     __syncthreads();
-    block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, SmemStRM<WH>{A});
-    block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, DctShufLd<WH>{A}, SmemStRM<WH>{A});
+    // C2R stored in the DCT-II input order, then the DCT-II's FFT
+    block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, DctShufStRM<WH>{A});
+    block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLdRM<WH>{A}, SmemStRM<WH>{A});
     const float* Q = resp + (size_t)l * resp_stride + 2 * off;
     for (int e = threadIdx.x; e < WH * C::RS; e += C::T) {
       const int k = e % WH, s = e / WH;
@@ -265,21 +290,42 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
 // ---------------------------------------------------------------------------
 // Column kernels, grid = (WH / CS, jobs): CS columns of a packed H x WH array.
 // ---------------------------------------------------------------------------
-// kDct2: DCT-II; kDct3: DCT-III; kDctAna: DCT-III then the forward FFT
+// DCT-II post-processing of the FFT V (dense [row][column] in A):
+// C[k] = (wd[k] V[k] + conj(wd[k]) V[H-k]) / 2, stored down the columns
+template <int H>
+__device__ __forceinline__ void dct2_cols_store(const float2* A, float2* dst, int WH, const float2* __restrict__ wd) {
+  using C = ColCfg<H>;
+  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
+    const int s = e % C::CS, k = e / C::CS;
+    const float2 w = __ldg(&wd[k]);
+    const float2 a = A[k * C::CS + s], b = A[((H - k) % H) * C::CS + s];
+    dst[(size_t)k * WH + s] = cscale(cadd(cmul(w, a), cmulc(b, w)), 0.5f);
+  }
+}
+
+// kDct2: DCT-II; kDct3: DCT-III; kDctAna: DCT-III then the forward FFT;
+// kDctThresh: DCT-III, the threshold (th, tmode) of both real columns of each
+// element, DCT-II (the DCT-II input order undoes the DCT-III output order, so
+// the threshold applies to the inverse FFT's output in place)
 template <int H, int MODE>
 __device__ __forceinline__ void dct_cols_body(const float2* src, float2* dst, int WH, float2* A,
-                                              const float2* __restrict__ twH, const float2* __restrict__ wd) {
+                                              const float2* __restrict__ twH, const float2* __restrict__ wd,
+                                              float th = 0.0f, int tmode = 0) {
   using C = ColCfg<H>;
   auto row_of = [](int i) { return i < H / 2 ? 2 * i : 2 * H - 1 - 2 * i; };
   if (MODE == kDct2) {
-    block_fft_hook_ip<H, C::CS, C::T, -1>(
-        A, twH, [&](int i, int s) { return src[(size_t)row_of(i) * WH + s]; }, SmemSt<C::CS>{A});
-    for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-      const int s = e % C::CS, k = e / C::CS;
-      const float2 w = __ldg(&wd[k]);
-      const float2 a = A[k * C::CS + s], b = A[((H - k) % H) * C::CS + s];
-      dst[(size_t)k * WH + s] = cscale(cadd(cmul(w, a), cmulc(b, w)), 0.5f);
+    // the column group staged in the DCT-II input order: source row r is
+    // element r/2 (r even) or H-1-(r-1)/2 (r odd) of v
+    for (int e = threadIdx.x; e < H * (C::CS / 2); e += C::T) {
+      const int r = e / (C::CS / 2), c = e - r * (C::CS / 2);
+      const int i = (r & 1) ? H - 1 - (r >> 1) : (r >> 1);
+      cp_async16(A + i * C::CS + 2 * c, src + (size_t)r * WH + 2 * c);
     }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{A});
+    dct2_cols_store<H>(A, dst, WH, wd);
     return;
   }
   // the column group staged whole (the pre-processing pairs rows k and H-k)
@@ -304,6 +350,12 @@ __device__ __forceinline__ void dct_cols_body(const float2* src, float2* dst, in
   if (MODE == kDct3) {
     block_fft_hook_ip<H, C::CS, C::T, +1>(A, twH, SmemLd<C::CS>{A},
                                           [&](int i, int s, float2 v) { dst[(size_t)row_of(i) * WH + s] = v; });
+  } else if (MODE == kDctThresh) {
+    block_fft_hook_ip<H, C::CS, C::T, +1>(A, twH, SmemLd<C::CS>{A}, [&](int i, int s, float2 v) {
+      A[i * C::CS + s] = make_float2(apply_thresh(v.x, th, tmode), apply_thresh(v.y, th, tmode));
+    });
+    block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{A});
+    dct2_cols_store<H>(A, dst, WH, wd);
   } else {
     block_fft_hook_ip<H, C::CS, C::T, +1>(A, twH, SmemLd<C::CS>{A},
                                           [&](int i, int s, float2 v) { A[row_of(i) * C::CS + s] = v; });
@@ -314,12 +366,14 @@ __device__ __forceinline__ void dct_cols_body(const float2* src, float2* dst, in
 template <int H, int MODE>
 __global__ void __launch_bounds__(ColCfg<H>::T, DctMinB<ColCfg<H>::T>::value)
     k_dct_cols(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base, float2* dst_base,
-               const float2* __restrict__ twH, const float2* __restrict__ wd) {
+               const float2* __restrict__ twH, const float2* __restrict__ wd, const float* __restrict__ thr,
+               int th_stride, int tmode) {
   extern __shared__ float2 smem[];
   const ColJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const int col0 = blockIdx.x * ColCfg<H>::CS;
-  dct_cols_body<H, MODE>(src_base + job.src + col0, dst_base + job.dst + col0, WH, smem, twH, wd);
+  const float th = MODE == kDctThresh ? thr[(size_t)job.item * th_stride] : 0.0f;
+  dct_cols_body<H, MODE>(src_base + job.src + col0, dst_base + job.dst + col0, WH, smem, twH, wd, th, tmode);
 }
 
 // DCT-III down the columns into the caller's output images
@@ -350,7 +404,8 @@ cudaError_t prepare_dct_kernels(int H, int WH) {
 #define CASE(n)                                                                  \
   case n:                                                                        \
     e = dct_opt_in(k_dct_rows_fwd<n>, RowCfg<n>::smem_rm());                     \
-    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_ana<n>, RowCfg<n>::smem_rm()); \
+    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_ana<n, false>, RowCfg<n>::smem_rm()); \
+    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_ana<n, true>, RowCfg<n>::smem_rm()); \
     if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_syn<n>, 2 * RowCfg<n>::smem_rm()); \
     break;
     NSST_DCT_ROW_SIZES(CASE)
@@ -365,6 +420,7 @@ cudaError_t prepare_dct_kernels(int H, int WH) {
     constexpr size_t sm = ColCfg<n>::smem() / 2;                                        \
     e = dct_opt_in(k_dct_cols<n, kDct2>, sm);                                           \
     if (e == cudaSuccess) e = dct_opt_in(k_dct_cols<n, kDctAna>, sm);                   \
+    if (e == cudaSuccess) e = dct_opt_in(k_dct_cols<n, kDctThresh>, sm);                \
     if (e == cudaSuccess) e = dct_opt_in(k_dct_cols_out<n>, sm);                        \
     return e;                                                                           \
   }
@@ -394,17 +450,23 @@ cudaError_t launch_dct_rows_fwd(const DctIo& io, int n, int H, int W, const floa
 
 cudaError_t launch_dct_rows_ana(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                                 void* dst_base, const float* resp, size_t resp_stride, const float2* twWh,
-                                const float2* twW, const float4* twD, cudaStream_t st) {
+                                const float2* twW, const float4* twD, bool real_out, cudaStream_t st) {
   if (njobs == 0) return cudaSuccess;
   count_launch();
   const float2* sb = static_cast<const float2*>(src_base);
   float2* db = static_cast<float2*>(dst_base);
   switch (W / 2) {
 #define CASE(n_)                                                                                            \
-  case n_:                                                                                                  \
-    k_dct_rows_ana<n_><<<dim3(H / RowCfg<n_>::RS, njobs), RowCfg<n_>::T, RowCfg<n_>::smem_rm(), st>>>(       \
-        jobs, n_active, sb, db, resp, resp_stride, twWh, twW, twD);                                         \
-    return cudaGetLastError();
+  case n_: {                                                                                                \
+    const dim3 grid(H / RowCfg<n_>::RS, njobs);                                                             \
+    if (real_out)                                                                                           \
+      k_dct_rows_ana<n_, true><<<grid, RowCfg<n_>::T, RowCfg<n_>::smem_rm(), st>>>(                          \
+          jobs, n_active, sb, db, resp, resp_stride, twWh, twW, twD);                                       \
+    else                                                                                                    \
+      k_dct_rows_ana<n_, false><<<grid, RowCfg<n_>::T, RowCfg<n_>::smem_rm(), st>>>(                         \
+          jobs, n_active, sb, db, resp, resp_stride, twWh, twW, twD);                                       \
+    return cudaGetLastError();                                                                              \
+  }
     NSST_DCT_ROW_SIZES(CASE)
 #undef CASE
     default:
@@ -434,9 +496,11 @@ cudaError_t launch_dct_rows_syn(const RowJob* jobs, int njobs, int n_active, int
 }
 
 cudaError_t launch_dct_cols(int mode, const ColJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
-                            void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st) {
+                            void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st, const float* thr,
+                            int th_stride, int th_mode) {
   if (njobs == 0) return cudaSuccess;
-  if (mode != kDct2 && mode != kDctAna) return cudaErrorInvalidValue;
+  if (mode != kDct2 && mode != kDctAna && mode != kDctThresh) return cudaErrorInvalidValue;
+  if (mode == kDctThresh && !thr) return cudaErrorInvalidValue;
   count_launch();
   const int WH = W / 2;
   const float2* sb = static_cast<const float2*>(src_base);
@@ -447,9 +511,14 @@ cudaError_t launch_dct_cols(int mode, const ColJob* jobs, int njobs, int n_activ
     const dim3 grid(WH / ColCfg<n_>::CS, njobs);                                                   \
     constexpr size_t sm = ColCfg<n_>::smem() / 2;                                                  \
     if (mode == kDct2)                                                                             \
-      k_dct_cols<n_, kDct2><<<grid, ColCfg<n_>::T, sm, st>>>(jobs, n_active, WH, sb, db, twH, wdH);   \
+      k_dct_cols<n_, kDct2><<<grid, ColCfg<n_>::T, sm, st>>>(jobs, n_active, WH, sb, db, twH, wdH,     \
+                                                             thr, th_stride, th_mode);                 \
+    else if (mode == kDctAna)                                                                      \
+      k_dct_cols<n_, kDctAna><<<grid, ColCfg<n_>::T, sm, st>>>(jobs, n_active, WH, sb, db, twH, wdH,   \
+                                                               thr, th_stride, th_mode);               \
     else                                                                                           \
-      k_dct_cols<n_, kDctAna><<<grid, ColCfg<n_>::T, sm, st>>>(jobs, n_active, WH, sb, db, twH, wdH); \
+      k_dct_cols<n_, kDctThresh><<<grid, ColCfg<n_>::T, sm, st>>>(jobs, n_active, WH, sb, db, twH,     \
+                                                                  wdH, thr, th_stride, th_mode);       \
     return cudaGetLastError();                                                                     \
   }
     NSST_DCT_COL_SIZES(CASE)

@@ -53,12 +53,6 @@ struct AnaCfg : ColCfg<N> {
   static constexpr int MINB = N >= 2048 ? 1 : 2;
 };
 
-__device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
-  if (mode == THRESH_HARD) return fabsf(v) > th ? v : 0.0f;
-  float a = fabsf(v) - th;  // soft: sign(v) * max(|v| - th, 0)
-  return a > 0.0f ? copysignf(a, v) : 0.0f;
-}
-
 // packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM (tiles.cuh):
 // Z[k] = E + iO with E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k;
 // k = 0 unpacks the two real bins.

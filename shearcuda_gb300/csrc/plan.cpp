@@ -94,13 +94,17 @@ struct nsst_plan {
   bool dct_on = false;         // the fused pipeline uses it
   float* dct_ra = nullptr;     // nlev x H x W analysis responses (directional level order)
   float* dct_rs = nullptr;     // nlev x H x W synthesis responses
-  float* dct_tl = nullptr;     // H x W lowpass response
+  float* dct_tl = nullptr;     // H x W lowpass round-trip response
+  float* dct_gl = nullptr;     // H x W lowpass synthesis response (after a lowpass threshold)
+  int dct_rl_plane = 0;        // plane index of the lowpass analysis response from dct_ra
   float4* twDW = nullptr;      // row twiddles, WH + 1
   float2* wdH = nullptr;       // column twiddles, H
   ColJob* j_dct_x = nullptr;   // pyr plane 1 -> pyr plane 0          (B)
   RowJob* j_dct_ana = nullptr; // pyr plane 0 -> lev, item-major       (B*nlev)
   ColJob* j_dct_sum = nullptr; // sum in place                         (B*nlev)
   RowJob* j_dct_syn = nullptr; // sum (all levels) -> pyr plane 1      (B)
+  RowJob* j_dct_low = nullptr; // pyr plane 0 -> tmp plane 0: the lowpass band (B)
+  ColJob* j_dct_lowc = nullptr; // tmp plane 0 in place                 (B)
 
   std::vector<double> scalars;
   bool has_scalars = false;
@@ -367,15 +371,17 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->dct_ok = filters_symmetric(p->pf) && cfg->pyramid != NSST_PYRAMID_DIRECT;
   if (cfg->pyramid == NSST_PYRAMID_SPECTRAL && !p->dct_ok)
     return destroy(fail(NSST_ERR_INVALID_ARG, "the spectral pyramid needs pyramid filters symmetric in both axes"));
-  size_t o_dct = 0, o_twDW = 0, o_wdH = 0, o_jd1 = 0, o_jd2 = 0, o_jd3 = 0, o_jd4 = 0;
+  size_t o_dct = 0, o_twDW = 0, o_wdH = 0, o_jd1 = 0, o_jd2 = 0, o_jd3 = 0, o_jd4 = 0, o_jd5 = 0, o_jd6 = 0;
   if (p->dct_ok) {
-    o_dct = take(sizeof(float) * HW * (2 * p->nlev + 1));
+    o_dct = take(sizeof(float) * HW * (2 * p->nlev + 3));
     o_twDW = take(sizeof(float4) * (p->WH + 1));
     o_wdH = take(sizeof(float2) * H);
     o_jd1 = take(sizeof(ColJob) * NB);
     o_jd2 = take(sizeof(RowJob) * nL);
     o_jd3 = take(sizeof(ColJob) * nL);
     o_jd4 = take(sizeof(RowJob) * NB);
+    o_jd5 = take(sizeof(RowJob) * NB);
+    o_jd6 = take(sizeof(ColJob) * NB);
   }
   p->arena_bytes = off;
   ce = dev_alloc((void**)&p->arena, p->arena_bytes);
@@ -527,24 +533,31 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     p->dct_ra = (float*)(A + o_dct);
     p->dct_rs = p->dct_ra + HW * p->nlev;
     p->dct_tl = p->dct_rs + HW * p->nlev;
+    p->dct_rl_plane = 2 * p->nlev + 1;
+    p->dct_gl = p->dct_ra + HW * (2 * p->nlev + 2);
     p->twDW = (float4*)(A + o_twDW);
     p->wdH = (float2*)(A + o_wdH);
     p->j_dct_x = (ColJob*)(A + o_jd1);
     p->j_dct_ana = (RowJob*)(A + o_jd2);
     p->j_dct_sum = (ColJob*)(A + o_jd3);
     p->j_dct_syn = (RowJob*)(A + o_jd4);
+    p->j_dct_low = (RowJob*)(A + o_jd5);
+    p->j_dct_lowc = (ColJob*)(A + o_jd6);
     std::vector<float> tab;
     dct_pyramid_tables(p->pf, p->nlev, H, W, &tab);
     auto tw = dct_row_twiddles(W);
     auto wh = dct_col_twiddles(H);
     auto f2 = [&](const void* ptr) { return (size_t)((const char*)ptr - A) / sizeof(float2); };
-    std::vector<ColJob> jx, js;
-    std::vector<RowJob> ja, jy;
+    std::vector<ColJob> jx, js, jlc;
+    std::vector<RowJob> ja, jy, jl;
     for (int i = 0; i < B; i++) {
       const size_t p0 = f2(p->pyr + i * p->s_pyr), p1 = f2(p->pyr + i * p->s_pyr + HW);
       const size_t lev = f2(p->lev + i * p->s_lev), sum = f2(p->sum + i * p->s_sum);
+      const size_t t0 = f2(p->tmp + i * p->s_tmp);
       jx.push_back(ColJob{p1, p0, 0, 0, 0, i});
       jy.push_back(RowJob{sum, p1, 0, i});
+      jl.push_back(RowJob{p0, t0, p->dct_rl_plane, i});
+      jlc.push_back(ColJob{t0, t0, 0, 0, 0, i});
       for (int l = 0; l < p->nlev; l++) {
         ja.push_back(RowJob{p0, lev + (size_t)l * HWh, l, i});
         js.push_back(ColJob{sum + (size_t)l * HWh, sum + (size_t)l * HWh, 0, 0, 0, i});
@@ -557,6 +570,8 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_ana, ja.data(), ja.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_sum, js.data(), js.size() * sizeof(ColJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_syn, jy.data(), jy.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_low, jl.data(), jl.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_lowc, jlc.data(), jlc.size() * sizeof(ColJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = prepare_dct_kernels(H, p->WH);
     if (ce != cudaSuccess) return destroy(cuda_fail(ce, "DCT pyramid tables"));
     p->dct_on = true;
@@ -839,10 +854,10 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
 }
 
 // Whether a fused pipeline call can take the DCT-domain pyramid: symmetric
-// filters, an unthresholded lowpass (it never leaves the DCT domain), no saved
-// forward state (the adjoint reads the spatial pyramid), 16-byte aligned images.
-bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* out, bool lowpass_th, bool keep) {
-  if (!p->dct_on || lowpass_th || keep) return false;
+// filters, no saved forward state (the adjoint reads the spatial pyramid),
+// 16-byte aligned images.
+bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* out, bool keep) {
+  if (!p->dct_on || keep) return false;
   for (int i = 0; i < n; i++)
     if (!aligned16(x[i]) || !aligned16(out[i])) return false;
   return true;
@@ -850,9 +865,11 @@ bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* ou
 
 // The fused pipeline with the pyramid in the DCT-II domain (k_dct.cu): the
 // pyramid's analysis merges with the level FFTs, its synthesis with the
-// inverse level FFTs; the directional stage is the same.
+// inverse level FFTs; the directional stage is the same.  The lowpass band
+// stays in the DCT domain unless it is thresholded (lowpass_th): then it is
+// transformed back, thresholded and transformed again (three passes).
 nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, float* const* out, int mode,
-                                const float* TH, cudaStream_t st) {
+                                bool lowpass_th, const float* TH, cudaStream_t st) {
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
@@ -869,8 +886,20 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   timer_mark(p, "dct_rows_image", st);
   NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_x, B, n, H, W, A, A, p->twH, p->wdH, st));
   timer_mark(p, "dct_cols_image", st);
+  if (lowpass_th) {  // lowpass band y0 = IDCT2(X .* R_low) -> threshold -> DCT2, in tmp plane 0
+    NSST_CUDA(launch_dct_rows_ana(p->j_dct_low, B, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW, true,
+                                  st));
+    NSST_CUDA(launch_dct_cols(kDctThresh, p->j_dct_lowc, B, n, H, W, A, A, p->twH, p->wdH, st, TH, p->nbands, mode));
+    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+      const int cn = std::min(kMaxAtrousJobs, n - c0);
+      DctIo io{};
+      for (int t = 0; t < cn; t++) io.src[t] = io.dst[t] = p->tmp + (size_t)(c0 + t) * p->s_tmp;
+      NSST_CUDA(launch_dct_rows_fwd(io, cn, H, W, p->twWh, p->twDW, st));
+    }
+    timer_mark(p, "dct_lowpass_threshold", st);
+  }
   NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, B * p->nlev, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW,
-                                st));
+                                false, st));
   timer_mark(p, "dct_rows_levels", st);
   NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
   timer_mark(p, "dct_cols_levels", st);
@@ -884,8 +913,9 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   timer_mark(p, "band_synthesis_cols", st);
   NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
   timer_mark(p, "dct_cols_sums", st);
-  NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A, p->pyr, p->s_pyr,
-                                p->dct_rs, HW, p->dct_tl, p->twWh, p->twW, p->twDW, st));
+  NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A,
+                                lowpass_th ? p->tmp : p->pyr, lowpass_th ? p->s_tmp : p->s_pyr, p->dct_rs, HW,
+                                lowpass_th ? p->dct_gl : p->dct_tl, p->twWh, p->twW, p->twDW, st));
   timer_mark(p, "dct_rows_synthesis", st);
   for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
     const int cn = std::min(kMaxAtrousJobs, n - c0);
@@ -911,7 +941,7 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
   const size_t HW = (size_t)H * W;
-  if (dct_path(p, n, x, out, lowpass_th, keep)) return enqueue_denoise_dct(p, n, x, out, mode, TH, st);
+  if (dct_path(p, n, x, out, keep)) return enqueue_denoise_dct(p, n, x, out, mode, lowpass_th, TH, st);
   std::vector<float*> ys(n);
   for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
   NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));

@@ -2,6 +2,7 @@
 // FFT kernels (k_directional.cu, k_dct.cu).
 #pragma once
 #include "fft_core.cuh"
+#include "internal.h"
 
 namespace nsst {
 
@@ -28,6 +29,14 @@ struct ColCfg {  // N = H points per column
   static constexpr int MINB = 1024 / T;  // in-place column passes: 4 CTAs of 256 threads per SM
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
+
+// The threshold rule of nsst_HT.m:34-46 (hard: |v| > th keeps v) and
+// soft thresholding (sign(v) max(|v| - th, 0)).
+__device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
+  if (mode == THRESH_HARD) return fabsf(v) > th ? v : 0.0f;
+  float a = fabsf(v) - th;  // soft: sign(v) * max(|v| - th, 0)
+  return a > 0.0f ? copysignf(a, v) : 0.0f;
+}
 
 // FFT hooks (see block_fft_hook).
 template <int NSEQ>

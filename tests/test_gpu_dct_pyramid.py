@@ -113,17 +113,32 @@ def test_spectral_batch_equals_single_and_graphs(built_lib, cuda):
         batch.use_graphs(False)
 
 
+@pytest.mark.parametrize('HW', [(256, 256), (256, 384)])
+def test_spectral_thresholded_lowpass(built_lib, cuda, HW):
+    # the lowpass band leaves the DCT domain once: IDCT2, threshold, DCT2
+    import shearcuda_gb300 as sc
+    H, W = HW
+    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL), _plan(H, W, sc.PYRAMID_DIRECT)
+    x = _img(H, W, 7, cuda)
+    K = [0.9] + list(K_DEMO[1:])  # lowpass threshold 0.9 * 20 * 0.5: a part of the lowpass is cut
+    assert 'dct_lowpass_threshold' in _stages(ps, x, K)
+    for mode, tol in [(sc.THRESH_SOFT, 1e-5), (sc.THRESH_HARD, 1e-3)]:
+        a = sc.nsst_denoise(x, ps, 20.0, K, None, mode=mode).cpu().numpy()
+        b = sc.nsst_denoise(x, pd, 20.0, K, None, mode=mode).cpu().numpy()
+        assert rel_l2(a, b) <= tol, (mode, rel_l2(a, b))
+    # a lowpass threshold above every lowpass value removes the lowpass on both paths
+    K = [1e6] + list(K_DEMO[1:])
+    a = sc.nsst_denoise(x, ps, 20.0, K, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    b = sc.nsst_denoise(x, pd, 20.0, K, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    assert rel_l2(a, b) <= 1e-4
+
+
 def test_direct_fallbacks(built_lib, cuda):
     import shearcuda_gb300 as sc
     H, W = 256, 256
-    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL), _plan(H, W, sc.PYRAMID_DIRECT)
+    ps = _plan(H, W, sc.PYRAMID_SPECTRAL)
     x = _img(H, W, 5, cuda)
-    # a thresholded lowpass band takes the direct pyramid: the same bits as a direct plan
-    K = [1.0] + list(K_DEMO[1:])
-    assert 'dct_rows_levels' not in _stages(ps, x, K)
-    np.testing.assert_array_equal(sc.nsst_denoise(x, ps, 20.0, K, None).cpu().numpy(),
-                                  sc.nsst_denoise(x, pd, 20.0, K, None).cpu().numpy())
-    # an image 4 bytes off a 16-byte boundary takes it too
+    # an image 4 bytes off a 16-byte boundary takes the direct pyramid
     buf = torch.zeros(H * W + 1, device=cuda)
     buf[1:] = x.reshape(-1)
     xm = buf[1:].view(H, W)
