@@ -56,9 +56,9 @@ typedef struct nsst_config {
                                    filters symmetric in both axes, as all of
                                    atrousfilters.m's sets are, else the plan is
                                    rejected); _AUTO: spectral where the filters
-                                   allow it.  Calls that threshold the lowpass band
-                                   or pass images not 16-byte aligned, and every
-                                   other entry point, use the direct pyramid. */
+                                   allow it.  Calls that pass images not 16-byte
+                                   aligned, the differentiable forward and every
+                                   other entry point use the direct pyramid. */
 } nsst_config;
 
 typedef struct nsst_plan nsst_plan;
