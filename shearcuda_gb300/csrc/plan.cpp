@@ -863,6 +863,87 @@ bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* ou
   return true;
 }
 
+// DCT-II of planes given by pointer (rows of the caller's images or arena
+// planes; src may equal dst): rows into rows_dst[i], then down the columns
+// with the static job list cols (in place on rows_dst or into its target).
+nsst_status enqueue_dct_rows_io(nsst_plan* p, int n, const float* const* src, float* const* dst, cudaStream_t st) {
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    DctIo io{};
+    for (int t = 0; t < cn; t++) {
+      io.src[t] = src[c0 + t];
+      io.dst[t] = dst[c0 + t];
+    }
+    NSST_CUDA(launch_dct_rows_fwd(io, cn, p->H, p->W, p->twWh, p->twDW, st));
+  }
+  return NSST_OK;
+}
+
+// DCT-III down the columns of arena planes src[i] into the caller's dst[i]
+nsst_status enqueue_dct_cols_out(nsst_plan* p, int n, const float* const* src, float* const* dst, cudaStream_t st) {
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    DctIo io{};
+    for (int t = 0; t < cn; t++) {
+      io.src[t] = src[c0 + t];
+      io.dst[t] = dst[c0 + t];
+    }
+    NSST_CUDA(launch_dct_cols_out(io, cn, p->H, p->W, p->twH, p->wdH, st));
+  }
+  return NSST_OK;
+}
+
+// Spectral analysis front of n items: X = DCT2(x) in pyr plane 0 (through
+// plane 1), then every level's spectrum (p->lev) from X .* R_l.
+nsst_status enqueue_dct_analysis(nsst_plan* p, int n, const float* const* x, cudaStream_t st) {
+  char* A = p->arena;
+  const int B = p->B, H = p->H, W = p->W;
+  const size_t HW = (size_t)H * W;
+  std::vector<float*> p1(n);
+  for (int i = 0; i < n; i++) p1[i] = p->pyr + (size_t)i * p->s_pyr + HW;
+  NSST_TRY(enqueue_dct_rows_io(p, n, x, p1.data(), st));
+  timer_mark(p, "dct_rows_image", st);
+  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_x, B, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_image", st);
+  NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, B * p->nlev, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW,
+                                false, st));
+  timer_mark(p, "dct_rows_levels", st);
+  NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_levels", st);
+  return NSST_OK;
+}
+
+// The lowpass band y0 = IDCT2(X .* R_low) of n items as rows DCT-III'd into
+// tmp plane 0 (its columns still in the DCT domain).
+nsst_status enqueue_dct_lowpass_rows(nsst_plan* p, int n, cudaStream_t st) {
+  char* A = p->arena;
+  NSST_CUDA(launch_dct_rows_ana(p->j_dct_low, p->B, n, p->H, p->W, A, A, p->dct_ra, (size_t)p->H * p->W, p->twWh,
+                                p->twW, p->twDW, true, st));
+  return NSST_OK;
+}
+
+// Spectral synthesis back end of n items: the band sums (p->sum, from the
+// band synthesis) DCT-II'd down the columns, then per row C2R -> DCT-II ->
+// .* Q_l summed over the levels with low .* lowtab (low: a DCT-domain plane
+// per item at lowbase + i * lowstride), DCT-III (pyr plane 1), and DCT-III down
+// the columns into out[i].
+nsst_status enqueue_dct_synthesis(nsst_plan* p, int n, const float* lowbase, size_t lowstride, const float* lowtab,
+                                  float* const* out, cudaStream_t st) {
+  char* A = p->arena;
+  const int B = p->B, H = p->H, W = p->W;
+  const size_t HW = (size_t)H * W;
+  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+  timer_mark(p, "dct_cols_sums", st);
+  NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A, lowbase, lowstride,
+                                p->dct_rs, HW, lowtab, p->twWh, p->twW, p->twDW, st));
+  timer_mark(p, "dct_rows_synthesis", st);
+  std::vector<const float*> p1(n);
+  for (int i = 0; i < n; i++) p1[i] = p->pyr + (size_t)i * p->s_pyr + HW;
+  NSST_TRY(enqueue_dct_cols_out(p, n, p1.data(), out, st));
+  timer_mark(p, "dct_cols_image_out", st);
+  return NSST_OK;
+}
+
 // The fused pipeline with the pyramid in the DCT-II domain (k_dct.cu): the
 // pyramid's analysis merges with the level FFTs, its synthesis with the
 // inverse level FFTs; the directional stage is the same.  The lowpass band
@@ -873,36 +954,16 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
-  const size_t HW = (size_t)H * W;
-  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
-    const int cn = std::min(kMaxAtrousJobs, n - c0);
-    DctIo io{};
-    for (int t = 0; t < cn; t++) {
-      io.src[t] = x[c0 + t];
-      io.dst[t] = p->pyr + (size_t)(c0 + t) * p->s_pyr + HW;
-    }
-    NSST_CUDA(launch_dct_rows_fwd(io, cn, H, W, p->twWh, p->twDW, st));
-  }
-  timer_mark(p, "dct_rows_image", st);
-  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_x, B, n, H, W, A, A, p->twH, p->wdH, st));
-  timer_mark(p, "dct_cols_image", st);
-  if (lowpass_th) {  // lowpass band y0 = IDCT2(X .* R_low) -> threshold -> DCT2, in tmp plane 0
-    NSST_CUDA(launch_dct_rows_ana(p->j_dct_low, B, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW, true,
-                                  st));
+  NSST_TRY(enqueue_dct_analysis(p, n, x, st));
+  if (lowpass_th) {  // lowpass band -> threshold -> DCT2, in tmp plane 0
+    NSST_TRY(enqueue_dct_lowpass_rows(p, n, st));
     NSST_CUDA(launch_dct_cols(kDctThresh, p->j_dct_lowc, B, n, H, W, A, A, p->twH, p->wdH, st, TH, p->nbands, mode));
-    for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
-      const int cn = std::min(kMaxAtrousJobs, n - c0);
-      DctIo io{};
-      for (int t = 0; t < cn; t++) io.src[t] = io.dst[t] = p->tmp + (size_t)(c0 + t) * p->s_tmp;
-      NSST_CUDA(launch_dct_rows_fwd(io, cn, H, W, p->twWh, p->twDW, st));
-    }
+    std::vector<float*> t0(n);
+    for (int i = 0; i < n; i++) t0[i] = p->tmp + (size_t)i * p->s_tmp;
+    std::vector<const float*> t0c(t0.begin(), t0.end());
+    NSST_TRY(enqueue_dct_rows_io(p, n, t0c.data(), t0.data(), st));
     timer_mark(p, "dct_lowpass_threshold", st);
   }
-  NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, B * p->nlev, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW,
-                                false, st));
-  timer_mark(p, "dct_rows_levels", st);
-  NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
-  timer_mark(p, "dct_cols_levels", st);
   NSST_TRY(enqueue_band_analysis(p, n, false, st));
   timer_mark(p, "band_analysis_cols", st);
   NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH, mode,
@@ -911,23 +972,8 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
                         p->twH, st));
   timer_mark(p, "band_synthesis_cols", st);
-  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
-  timer_mark(p, "dct_cols_sums", st);
-  NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A,
-                                lowpass_th ? p->tmp : p->pyr, lowpass_th ? p->s_tmp : p->s_pyr, p->dct_rs, HW,
-                                lowpass_th ? p->dct_gl : p->dct_tl, p->twWh, p->twW, p->twDW, st));
-  timer_mark(p, "dct_rows_synthesis", st);
-  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {
-    const int cn = std::min(kMaxAtrousJobs, n - c0);
-    DctIo io{};
-    for (int t = 0; t < cn; t++) {
-      io.src[t] = p->pyr + (size_t)(c0 + t) * p->s_pyr + HW;
-      io.dst[t] = out[c0 + t];
-    }
-    NSST_CUDA(launch_dct_cols_out(io, cn, H, W, p->twH, p->wdH, st));
-  }
-  timer_mark(p, "dct_cols_image_out", st);
-  return NSST_OK;
+  return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st)
+                    : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st);
 }
 
 // The fused batched pipeline (no host work, no allocation): capturable.
@@ -1013,11 +1059,21 @@ nsst_status enqueue_shear_trans(nsst_plan* p, const float* x, float* coeffs, cud
   char* A = p->arena;
   float2* A2 = (float2*)A;
   float* yb = p->pyr;
-  // the lowpass goes straight to coefficient plane 0
-  NSST_TRY(run_atrousdec(p, 1, &x, &yb, coeffs, st));
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
-                        st));
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
+  if (p->dct_on && aligned16(x)) {
+    // spectral pyramid: the level spectra from X = DCT2(x); the lowpass
+    // IDCT2(X .* R_low) straight to coefficient plane 0
+    NSST_TRY(enqueue_dct_analysis(p, 1, &x, st));
+    NSST_TRY(enqueue_dct_lowpass_rows(p, 1, st));
+    const float* t0 = p->tmp;
+    NSST_TRY(enqueue_dct_cols_out(p, 1, &t0, &coeffs, st));
+    timer_mark(p, "dct_lowpass", st);
+  } else {
+    // the lowpass goes straight to coefficient plane 0
+    NSST_TRY(run_atrousdec(p, 1, &x, &yb, coeffs, st));
+    NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
+                          st));
+    NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, p->nlev, 1, p->H, p->W, A2, A2, nullptr, 0, p->twH, st));
+  }
   // the job list covers every item; n_active = 1 skips the others
   NSST_CUDA(launch_cols(ColOp::Analysis, p->j_analysis, p->B * p->ndir_total, 1, p->H, p->W, A2, A2, p->spec, 0,
                         p->twH, st));
@@ -1184,6 +1240,15 @@ nsst_status nsst_inverse_shear(nsst_plan* p, const float* coeffs, float* x, void
   NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, 1, p->H, p->W, A2, A2, p->spec,
                         (size_t)p->H * p->WH, p->twH, st));
   timer_mark(p, "band_synthesis_cols", st);
+  if (p->dct_on && aligned16(x)) {
+    // spectral pyramid: the lowpass coefficients DCT2'd into tmp plane 0,
+    // then the band sums and that plane through the synthesis back end
+    float* t0 = p->tmp;
+    NSST_TRY(enqueue_dct_rows_io(p, 1, &coeffs, &t0, st));
+    NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_lowc, p->B, 1, p->H, p->W, A, A, p->twH, p->wdH, st));
+    timer_mark(p, "dct_lowpass", st);
+    return enqueue_dct_synthesis(p, 1, p->tmp, p->s_tmp, p->dct_gl, &x, st);
+  }
   NSST_CUDA(launch_rows(RowOp::Inv, p->j_rows_lev_inv, p->nlev, 1, p->H, p->W, A, A, p->twWh, p->twW, nullptr, 0,
                         st));
   timer_mark(p, "fft_rows_inv", st);

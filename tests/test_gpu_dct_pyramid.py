@@ -155,3 +155,37 @@ def test_pyramid_modes(built_lib, cuda):
     p = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256)
     p.set_scalars(np.ones(p.nbands))
     assert 'dct_rows_levels' in _stages(p, _img(256, 256, 6, cuda), K_DEMO)
+
+
+@pytest.mark.parametrize('HW', [(256, 384), (512, 512)])
+def test_spectral_shear_trans_and_inverse(built_lib, cuda, HW):
+    # nsst_shear_trans / nsst_inverse_shear (shear_trans_cuda / inverse_shear_cuda) on the
+    # spectral pyramid: coefficients and reconstructions within FP32 rounding of the direct ones
+    import shearcuda_gb300 as sc
+    H, W = HW
+    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL), _plan(H, W, sc.PYRAMID_DIRECT)
+    x = _img(H, W, 8, cuda)
+    ps.enable_timers(True)
+    try:
+        cs = sc.shear_trans_cuda(x, 'maxflat', ps)
+        assert 'dct_lowpass' in [n for n, _ in ps.read_timers(40)]
+    finally:
+        ps.enable_timers(False)
+    cd = sc.shear_trans_cuda(x, 'maxflat', pd)
+    assert rel_l2(cs.cpu().numpy(), cd.cpu().numpy()) <= 1e-5
+    assert rel_l2(cs[0].cpu().numpy(), cd[0].cpu().numpy()) <= 1e-5  # the lowpass plane alone
+    rs = sc.inverse_shear_cuda(cs, 'maxflat', ps)
+    rd = sc.inverse_shear_cuda(cs, 'maxflat', pd)
+    assert rel_l2(rs.cpu().numpy(), rd.cpu().numpy()) <= 1e-5
+    assert rel_l2(rs.cpu().numpy(), x.cpu().numpy()) <= 1e-5
+    # an output 4 bytes off a 16-byte boundary takes the direct pyramid
+    buf = torch.zeros(H * W + 1, device=cuda)
+    ps.enable_timers(True)
+    try:
+        from shearcuda_gb300 import _lib
+        _lib.check(_lib.lib().nsst_inverse_shear(ps.handle, cs.data_ptr(), buf.data_ptr() + 4, None))
+        assert 'dct_lowpass' not in [n for n, _ in ps.read_timers(40)]
+    finally:
+        ps.enable_timers(False)
+    torch.cuda.synchronize()
+    assert rel_l2(buf[1:].view(H, W).cpu().numpy(), rd.cpu().numpy()) <= 1e-5
