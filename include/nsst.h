@@ -56,11 +56,12 @@ typedef struct nsst_config {
                                    filters symmetric in both axes, as all of
                                    atrousfilters.m's sets are, else the plan is
                                    rejected); _AUTO: spectral where the filters
-                                   allow it.  nsst_shear_trans and
-                                   nsst_inverse_shear follow the same mode; calls
-                                   that pass images not 16-byte aligned, the
-                                   differentiable path and nsst_atrousdec /
-                                   nsst_atrousrec use the direct pyramid. */
+                                   allow it.  nsst_shear_trans,
+                                   nsst_inverse_shear and the differentiable
+                                   denoise (forward and backward) follow the same
+                                   mode; calls that pass images not 16-byte
+                                   aligned, nsst_atrousdec / nsst_atrousrec and
+                                   the operator adjoints use the direct pyramid. */
 } nsst_config;
 
 typedef struct nsst_plan nsst_plan;

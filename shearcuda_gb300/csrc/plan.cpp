@@ -156,6 +156,14 @@ struct nsst_plan {
   RowJob* gj_rows_lev_inv = nullptr;   // sum2 -> gy[1..]
   RowJob* gj_coeff_fwd = nullptr;      // caller coeffs -> band2 (item 0)
   RowJob* gj_band_to_coeff = nullptr;  // band2 -> caller coeffs (item 0)
+  // the backward on the spectral pyramid (when dct_ok)
+  bool saved_dct = false;              // the saved forward ran the spectral pyramid
+  ColJob* gj_dct_x = nullptr;          // gtmp plane 0 -> gtmp plane 1 (B)
+  RowJob* gj_dct_ana = nullptr;        // gtmp plane 1 -> lev2, Q tables (B*nlev)
+  RowJob* gj_dct_low = nullptr;        // gtmp plane 1 -> gtmp plane 0, lowpass synthesis table (B)
+  ColJob* gj_dct_gy0 = nullptr;        // gy plane 0 in place (B)
+  ColJob* gj_dct_sum = nullptr;        // sum2 in place (B*nlev)
+  RowJob* gj_dct_syn = nullptr;        // sum2 -> gy plane 1 (B)
 
   // stage timers
   bool timing = false;
@@ -854,10 +862,9 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
 }
 
 // Whether a fused pipeline call can take the DCT-domain pyramid: symmetric
-// filters, no saved forward state (the adjoint reads the spatial pyramid),
-// 16-byte aligned images.
-bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* out, bool keep) {
-  if (!p->dct_on || keep) return false;
+// filters, 16-byte aligned images.
+bool dct_path(const nsst_plan* p, int n, const float* const* x, float* const* out) {
+  if (!p->dct_on) return false;
   for (int i = 0; i < n; i++)
     if (!aligned16(x[i]) || !aligned16(out[i])) return false;
   return true;
@@ -950,7 +957,7 @@ nsst_status enqueue_dct_synthesis(nsst_plan* p, int n, const float* lowbase, siz
 // stays in the DCT domain unless it is thresholded (lowpass_th): then it is
 // transformed back, thresholded and transformed again (three passes).
 nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, float* const* out, int mode,
-                                bool lowpass_th, const float* TH, cudaStream_t st) {
+                                bool lowpass_th, const float* TH, cudaStream_t st, bool keep = false) {
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
@@ -966,11 +973,19 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   }
   NSST_TRY(enqueue_band_analysis(p, n, false, st));
   timer_mark(p, "band_analysis_cols", st);
-  NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH, mode,
-                        st));
-  timer_mark(p, "band_rows_threshold", st);
-  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
-                        p->twH, st));
+  if (keep) {  // the thresholded bands to bandT: band keeps the pre-threshold spectra for the backward
+    NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW, TH,
+                          mode, st));
+    timer_mark(p, "band_rows_threshold", st);
+    NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
+                          (size_t)H * p->WH, p->twH, st));
+  } else {
+    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH,
+                          mode, st));
+    timer_mark(p, "band_rows_threshold", st);
+    NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec,
+                          (size_t)H * p->WH, p->twH, st));
+  }
   timer_mark(p, "band_synthesis_cols", st);
   return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st)
                     : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st);
@@ -987,7 +1002,8 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
   const size_t HW = (size_t)H * W;
-  if (dct_path(p, n, x, out, keep)) return enqueue_denoise_dct(p, n, x, out, mode, lowpass_th, TH, st);
+  if (keep) p->saved_dct = dct_path(p, n, x, out);
+  if (dct_path(p, n, x, out)) return enqueue_denoise_dct(p, n, x, out, mode, lowpass_th, TH, st, keep);
   std::vector<float*> ys(n);
   for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
   NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
@@ -1538,6 +1554,11 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   size_t o_bandT = take(sizeof(float2) * NB * p->ndir_total * HWh);
   size_t o_jT = take(sizeof(RowJob) * nD), o_jS = take(sizeof(ColJob) * nL);
   size_t o_jA = take(sizeof(ColJob) * nL);
+  size_t o_gd1 = 0, o_gd2 = 0, o_gd3 = 0, o_gd4 = 0, o_gd5 = 0, o_gd6 = 0;
+  if (p->dct_ok) {
+    o_gd1 = take(sizeof(ColJob) * NB), o_gd2 = take(sizeof(RowJob) * nL), o_gd3 = take(sizeof(RowJob) * NB);
+    o_gd4 = take(sizeof(ColJob) * NB), o_gd5 = take(sizeof(ColJob) * nL), o_gd6 = take(sizeof(RowJob) * NB);
+  }
   cudaError_t ce = dev_alloc((void**)&p->garena, off);
   if (ce != cudaSuccess) {
     p->garena = nullptr;
@@ -1636,6 +1657,36 @@ nsst_status nsst_plan_enable_grad(nsst_plan* p) {
   if (ce == cudaSuccess) ce = up(p->gj_rows_T, jT.data(), jT.size() * sizeof(RowJob));
   if (ce == cudaSuccess) ce = up(p->gj_synth_T, jS.data(), jS.size() * sizeof(ColJob));
   if (ce != cudaSuccess) return cuda_fail(ce, "upload gradient job lists");
+  if (p->dct_ok) {
+    p->gj_dct_x = (ColJob*)(G + o_gd1);
+    p->gj_dct_ana = (RowJob*)(G + o_gd2);
+    p->gj_dct_low = (RowJob*)(G + o_gd3);
+    p->gj_dct_gy0 = (ColJob*)(G + o_gd4);
+    p->gj_dct_sum = (ColJob*)(G + o_gd5);
+    p->gj_dct_syn = (RowJob*)(G + o_gd6);
+    std::vector<ColJob> gx, gg, gs;
+    std::vector<RowJob> ga, gl, gy1;
+    for (int i = 0; i < B; i++) {
+      const size_t t0 = g2(p->gtmp + i * 2 * HW), t1 = g2(p->gtmp + i * 2 * HW + HW);
+      const size_t gy0 = g2(p->gy + i * (p->nlev + 1) * HW), gyl = g2(p->gy + i * (p->nlev + 1) * HW + HW);
+      const size_t lev = g2(p->lev2 + i * p->s_lev), sum = g2(p->sum2 + i * p->s_sum);
+      gx.push_back(ColJob{t0, t1, 0, 0, 0, i});
+      gl.push_back(RowJob{t1, t0, 2 * p->nlev + 2, i});  // the lowpass synthesis plane from dct_ra
+      gg.push_back(ColJob{gy0, gy0, 0, 0, 0, i});
+      gy1.push_back(RowJob{sum, gyl, 0, i});
+      for (int l = 0; l < p->nlev; l++) {
+        ga.push_back(RowJob{t1, lev + (size_t)l * HWh, l, i});
+        gs.push_back(ColJob{sum + (size_t)l * HWh, sum + (size_t)l * HWh, 0, 0, 0, i});
+      }
+    }
+    ce = up(p->gj_dct_x, gx.data(), gx.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->gj_dct_ana, ga.data(), ga.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->gj_dct_low, gl.data(), gl.size() * sizeof(RowJob));
+    if (ce == cudaSuccess) ce = up(p->gj_dct_gy0, gg.data(), gg.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->gj_dct_sum, gs.data(), gs.size() * sizeof(ColJob));
+    if (ce == cudaSuccess) ce = up(p->gj_dct_syn, gy1.data(), gy1.size() * sizeof(RowJob));
+    if (ce != cudaSuccess) return cuda_fail(ce, "upload spectral gradient job lists");
+  }
   for (int F : {p->pf.F[0], p->pf.F[1], p->pf.F[2], p->pf.F[3]}) {
     ce = prepare_atrous_kernels(F, 0, Mmax);
     if (ce != cudaSuccess) return cuda_fail(ce, "adjoint kernel set-up");
@@ -1719,9 +1770,94 @@ namespace {
 // The backward of nsst_denoise_tau_batch; x == NULL: the band spectra and the
 // pyramid's lowpass of the last differentiable forward are still in the
 // arena (saved_n == n), so step 1 is skipped.  Called with the plan locked.
+// tau_backward on the spectral pyramid.  Each pyramid operator is symmetric
+// (IDCT2 diag(r) DCT2 with the DCT-III the DCT-II's transpose times
+// diag(1, 2, 2, ...), and diagonals commute), so the adjoint of the synthesis
+// is the analysis front with the synthesis tables and the adjoint of the
+// analysis the synthesis back end with the analysis tables.  Images not
+// 16-byte aligned pass through gyp plane 1 (unused here).
+nsst_status tau_backward_dct(nsst_plan* p, const float* const* x, const float* const* grad_out, float* const* grad_x,
+                             int n, const float* tau, float* grad_tau, int accumulate_tau, int mode, cudaStream_t st) {
+  char* G = p->garena;
+  const int H = p->H, W = p->W, B = p->B, L = p->nlev;
+  const size_t HW = (size_t)H * W;
+  std::vector<const float*> gout(n), t0c(n), gt0c(n), gy0c(n);
+  std::vector<float*> ys(n), gt0(n), gyp0(n), gy0(n), gy1(n), gxo(n), gyp1(n);
+  for (int i = 0; i < n; i++) {
+    gyp1[i] = p->gyp + (size_t)i * (L + 1) * HW + HW;
+    gout[i] = aligned16(grad_out[i]) ? grad_out[i] : gyp1[i];
+    if (gout[i] != grad_out[i])
+      NSST_CUDA(cudaMemcpyAsync(gyp1[i], grad_out[i], HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    gxo[i] = aligned16(grad_x[i]) ? grad_x[i] : gyp1[i];
+    t0c[i] = p->tmp + (size_t)i * p->s_tmp;
+    ys[i] = p->pyr + (size_t)i * p->s_pyr + HW;
+    gt0[i] = p->gtmp + (size_t)i * 2 * HW;
+    gt0c[i] = gt0[i];
+    gyp0[i] = p->gyp + (size_t)i * (L + 1) * HW;
+    gy0[i] = p->gy + (size_t)i * (L + 1) * HW;
+    gy0c[i] = gy0[i];
+    gy1[i] = gy0[i] + HW;
+  }
+  // 1. the coefficient spectra of x (recomputed unless saved) and the
+  //    pre-threshold lowpass band, spatial, in pyr plane 1
+  if (x) {
+    NSST_TRY(enqueue_dct_analysis(p, n, x, st));
+    NSST_TRY(enqueue_band_analysis(p, n, false, st));
+    timer_mark(p, "recompute_coefficients", st);
+  }
+  NSST_TRY(enqueue_dct_lowpass_rows(p, n, st));
+  NSST_TRY(enqueue_dct_cols_out(p, n, t0c.data(), ys.data(), st));
+  // 2. d loss / d coefficients: level spectra of IDCT2(Q_l .* DCT2(grad_out)),
+  //    lowpass IDCT2(G_low .* DCT2(grad_out)) in gyp plane 0
+  NSST_TRY(enqueue_dct_rows_io(p, n, gout.data(), gt0.data(), st));
+  NSST_CUDA(launch_dct_cols(kDct2, p->gj_dct_x, B, n, H, W, G, G, p->twH, p->wdH, st));
+  NSST_CUDA(launch_dct_rows_ana(p->gj_dct_ana, B * L, n, H, W, G, G, p->dct_rs, HW, p->twWh, p->twW, p->twDW, false,
+                                st));
+  NSST_CUDA(launch_dct_cols(kDctAna, p->gj_cols_lev, B * L, n, H, W, G, G, p->twH, p->wdH, st));
+  NSST_CUDA(launch_dct_rows_ana(p->gj_dct_low, B, n, H, W, G, G, p->dct_ra, HW, p->twWh, p->twW, p->twDW, true, st));
+  NSST_TRY(enqueue_dct_cols_out(p, n, gt0c.data(), gyp0.data(), st));
+  NSST_TRY(enqueue_band_analysis(p, n, true, st));
+  timer_mark(p, "gradient_analysis", st);
+  // 3. threshold subgradient per band (+ tau partials), then D^T
+  const size_t pstride = (size_t)B * p->ntiles;
+  NSST_CUDA(launch_rows_backward(p->gj_rows_backward, B * p->ndir_total, n, H, W, p->arena, G, p->twWh, p->twW, tau,
+                                 mode, p->partials, pstride, st));
+  timer_mark(p, "band_rows_backward", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synthesis, B * L, n, H, W, (float2*)G, (float2*)G, p->spec,
+                        (size_t)H * p->WH, p->twH, st));
+  timer_mark(p, "gradient_synthesis", st);
+  for (int c0 = 0; c0 < n; c0 += kMaxAtrousJobs) {  // lowpass band mask -> gy plane 0
+    const int cn = std::min(kMaxAtrousJobs, n - c0);
+    FoldJobs jl{};
+    for (int t = 0; t < cn; t++) jl.j[t] = FoldJob{ys[c0 + t], gyp0[c0 + t], gy0[c0 + t]};
+    NSST_CUDA(launch_lowpass_backward(jl, cn, HW, tau, mode, p->partials, c0 * p->ntiles, p->ntiles, st));
+  }
+  // 4. d loss / d x = IDCT2(sum_l R_l .* DCT2(g_l) + R_low .* DCT2(g_0))
+  NSST_TRY(enqueue_dct_rows_io(p, n, gy0c.data(), gy0.data(), st));
+  NSST_CUDA(launch_dct_cols(kDct2, p->gj_dct_gy0, B, n, H, W, G, G, p->twH, p->wdH, st));
+  NSST_CUDA(launch_dct_cols(kDct2, p->gj_dct_sum, B * L, n, H, W, G, G, p->twH, p->wdH, st));
+  NSST_CUDA(launch_dct_rows_syn(p->gj_dct_syn, B, n, L, (size_t)H * p->WH, H, W, G, G, p->gy, (size_t)(L + 1) * HW,
+                                p->dct_ra, HW, p->dct_ra + (size_t)(2 * L + 1) * HW, p->twWh, p->twW, p->twDW, st));
+  std::vector<const float*> gy1c(gy1.begin(), gy1.end());
+  NSST_TRY(enqueue_dct_cols_out(p, n, gy1c.data(), gxo.data(), st));
+  for (int i = 0; i < n; i++)
+    if (gxo[i] != grad_x[i])
+      NSST_CUDA(cudaMemcpyAsync(grad_x[i], gxo[i], HW * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  timer_mark(p, "gradient_pyramid", st);
+  NSST_CUDA(launch_reduce_tau(p->partials, n * p->ntiles, pstride, p->nbands, grad_tau, accumulate_tau != 0, st));
+  timer_mark(p, "reduce_tau", st);
+  return NSST_OK;
+}
+
 nsst_status tau_backward(nsst_plan* p, const float* const* x, const float* const* grad_out, float* const* grad_x,
                          int n, const float* tau, float* grad_tau, int accumulate_tau, int mode, cudaStream_t st) {
   timer_begin(p, st);
+  bool spectral = p->saved_dct;
+  if (x) {
+    spectral = p->dct_on;
+    for (int i = 0; i < n; i++) spectral = spectral && aligned16(x[i]);
+  }
+  if (spectral) return tau_backward_dct(p, x, grad_out, grad_x, n, tau, grad_tau, accumulate_tau, mode, st);
   char* A = p->arena;
   float2* A2 = (float2*)A;
   char* G = p->garena;

@@ -189,3 +189,32 @@ def test_spectral_shear_trans_and_inverse(built_lib, cuda, HW):
         ps.enable_timers(False)
     torch.cuda.synchronize()
     assert rel_l2(buf[1:].view(H, W).cpu().numpy(), rd.cpu().numpy()) <= 1e-5
+
+
+@pytest.mark.parametrize('mode', [0, 1])
+def test_spectral_gradients_match_direct(built_lib, cuda, mode):
+    # the differentiable forward and its backward on the spectral pyramid
+    # (the pyramid operators are symmetric, so the adjoint swaps the analysis
+    # and synthesis tables) against the direct pyramid's
+    import shearcuda_gb300 as sc
+    H, W = 256, 256
+    grads = []
+    for pyr in (sc.PYRAMID_SPECTRAL, sc.PYRAMID_DIRECT):
+        p = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, pyramid=pyr, batch=2)
+        sc.autograd.enable_grad(p)
+        x = torch.stack([_img(H, W, 30, cuda), _img(H, W, 31, cuda)]).requires_grad_(True)
+        tau = torch.tensor(np.linspace(20.0, 60.0, p.nbands), dtype=torch.float32, device=cuda,
+                           requires_grad=True)
+        p.enable_timers(True)
+        out = sc.nsst_denoise_diff(x, tau, p, mode)
+        gy = torch.sin(torch.arange(out.numel(), device=cuda, dtype=torch.float32)).view_as(out)
+        out.backward(gy)
+        names = [n for n, _ in p.read_timers(40)]
+        p.enable_timers(False)
+        assert ('gradient_pyramid' in names) == (pyr == sc.PYRAMID_SPECTRAL)
+        grads.append((out.detach().cpu().numpy(), x.grad.cpu().numpy(), tau.grad.cpu().numpy()))
+    (o1, gx1, gt1), (o2, gx2, gt2) = grads
+    assert rel_l2(o1, o2) <= 1e-3
+    assert rel_l2(gx1, gx2) <= 1e-3, rel_l2(gx1, gx2)
+    if mode == 1:
+        assert rel_l2(gt1, gt2) <= 1e-3, rel_l2(gt1, gt2)
