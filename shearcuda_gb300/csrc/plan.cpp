@@ -1060,9 +1060,24 @@ nsst_status enqueue_band_maxima(nsst_plan* p, int n, const float* const* x, unsi
   std::vector<float*> ys(n);
   for (int i = 0; i < n; i++) ys[i] = p->pyr + i * p->s_pyr;
   NSST_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * n * p->nbands, st));
-  NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
-  NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
-  NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+  bool spectral = p->dct_on;
+  for (int i = 0; i < n; i++) spectral = spectral && aligned16(x[i]);
+  if (spectral) {
+    // level spectra from X = DCT2(x); the spatial lowpass into pyr plane 1
+    NSST_TRY(enqueue_dct_analysis(p, n, x, st));
+    NSST_TRY(enqueue_dct_lowpass_rows(p, n, st));
+    std::vector<const float*> t0(n);
+    for (int i = 0; i < n; i++) {
+      t0[i] = p->tmp + (size_t)i * p->s_tmp;
+      ys[i] += HW;
+    }
+    NSST_TRY(enqueue_dct_cols_out(p, n, t0.data(), ys.data(), st));
+  } else {
+    NSST_TRY(run_atrousdec(p, n, x, ys.data(), nullptr, st));
+    NSST_CUDA(launch_rows(RowOp::Fwd, p->j_rows_lev_fwd, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0,
+                          st));
+    NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
+  }
   NSST_TRY(enqueue_band_analysis(p, n, false, st));
   NSST_CUDA(launch_rows_max(p->j_rows_bands, B * p->ndir_total, n, H, W, A, p->twWh, p->twW, bits, st));
   for (int i = 0; i < n; i++)
@@ -1111,6 +1126,28 @@ nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream)
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
   float* yb = y;
+  if (p->dct_on && aligned16(x) && aligned16(y)) {
+    // spectral pyramid: X = DCT2(x); band l = IDCT2(X .* R_l) (rows into the
+    // level planes, then down the columns into y plane l + 1); the lowpass
+    const int L = p->nlev;
+    const size_t HW = (size_t)p->H * p->W;
+    std::vector<float*> p1{p->pyr + HW};
+    NSST_TRY(enqueue_dct_rows_io(p, 1, &x, p1.data(), st));
+    char* A = p->arena;
+    NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_x, p->B, 1, p->H, p->W, A, A, p->twH, p->wdH, st));
+    NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, p->B * L, 1, p->H, p->W, A, A, p->dct_ra, HW, p->twWh, p->twW,
+                                  p->twDW, true, st));
+    NSST_TRY(enqueue_dct_lowpass_rows(p, 1, st));
+    std::vector<const float*> src(L + 1);
+    std::vector<float*> dst(L + 1);
+    src[0] = p->tmp;
+    dst[0] = y;
+    for (int l = 0; l < L; l++) {
+      src[l + 1] = reinterpret_cast<const float*>(p->lev + (size_t)l * p->H * p->WH);
+      dst[l + 1] = y + (size_t)(l + 1) * HW;
+    }
+    return enqueue_dct_cols_out(p, L + 1, src.data(), dst.data(), st);
+  }
   return run_atrousdec(p, 1, &x, &yb, nullptr, st);
 }
 
