@@ -1,4 +1,5 @@
-// The à trous pyramid of the fused denoise pipeline in the DCT-II domain.
+// The à trous pyramid in the DCT-II domain (the spectral pyramid of the fused
+// denoise pipeline, its backward, shear_trans / inverse_shear and atrousdec).
 //
 // Every pyramid step of the reference (atrousc.cpp:43-73 on symext.m's
 // extension, atrousdec.m:33-44, atrousrec.m:33-40) filters with a filter that
@@ -20,8 +21,10 @@
 //     rows    : C2R -> DCT-II -> .* Q_l, summed over the levels, + X .* T,
 //               then DCT-III                            (k_dct_rows_syn)
 //     columns : DCT-III -> the output image             (k_dct_cols_out)
-// Five full-plane passes replace the pyramid's eight FFMA-bound convolution
-// launches per level pair.
+// A thresholded lowpass leaves the DCT domain once (k_dct_rows_ana<·, true>,
+// k_dct_cols<H, kDctThresh>, k_dct_rows_fwd).  Seven launches replace the
+// direct pyramid's two FFMA-bound convolution launches per level and step
+// (sixteen at four levels) and the three level-FFT launches.
 //
 // DCTs of length N through one N-point FFT (J. Makhoul, "A fast cosine
 // transform in one and two dimensions", IEEE Trans. ASSP 28(1), 1980), all
