@@ -23,8 +23,9 @@
 //     columns : DCT-III -> the output image             (k_dct_cols_out)
 // A thresholded lowpass leaves the DCT domain once (k_dct_rows_ana<·, true>,
 // k_dct_cols<H, kDctThresh>, k_dct_rows_fwd).  Seven launches replace the
-// direct pyramid's two FFMA-bound convolution launches per level and step
-// (sixteen at four levels) and the three level-FFT launches.
+// direct pyramid's FFMA-bound convolutions (two launches per analysis level,
+// one per synthesis level: twelve at four levels) and the three level-FFT
+// launches.
 //
 // DCTs of length N through one N-point FFT (J. Makhoul, "A fast cosine
 // transform in one and two dimensions", IEEE Trans. ASSP 28(1), 1980), all
