@@ -57,12 +57,12 @@ typedef struct nsst_config {
                                    atrousfilters.m's sets are, else the plan is
                                    rejected); _AUTO: spectral where the filters
                                    allow it.  nsst_shear_trans,
-                                   nsst_inverse_shear, nsst_atrousdec, the
-                                   differentiable denoise (forward and backward)
-                                   and the separation follow the same mode; calls
-                                   that pass images not 16-byte aligned,
-                                   nsst_atrousrec, nsst_re_weight_band and the
-                                   operator adjoints use the direct pyramid. */
+                                   nsst_inverse_shear, nsst_atrousdec,
+                                   nsst_atrousrec, the differentiable denoise
+                                   (forward and backward) and the separation
+                                   follow the same mode; calls that pass images
+                                   not 16-byte aligned, nsst_re_weight_band and
+                                   the operator adjoints use the direct pyramid. */
 } nsst_config;
 
 typedef struct nsst_plan nsst_plan;

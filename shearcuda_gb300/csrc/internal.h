@@ -124,7 +124,7 @@ cudaError_t launch_dct_rows_ana(const RowJob* jobs, int njobs, int n_active, int
 cudaError_t launch_dct_rows_syn(const RowJob* jobs, int njobs, int n_active, int nlev, size_t lev_stride, int H,
                                 int W, const void* src_base, void* dst_base, const float* xbase, size_t xstride,
                                 const float* resp, size_t resp_stride, const float* tlow, const float2* twWh,
-                                const float2* twW, const float4* twD, cudaStream_t st);
+                                const float2* twW, const float4* twD, cudaStream_t st, bool real_in = false);
 cudaError_t launch_dct_cols(int mode, const ColJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                             void* dst_base, const float2* twH, const float2* wdH, cudaStream_t st,
                             const float* thr = nullptr, int th_stride = 0, int th_mode = 0);

@@ -225,10 +225,11 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
 
 // synthesis rows of one item: for every level l the band sum's packed half
 // spectrum rows (DCT-II down the columns already) -> C2R -> DCT-II -> .* Q_l,
-// accumulated with X .* T in shared memory, then DCT-III -> real rows.
+// accumulated with X .* T in shared memory, then DCT-III -> real rows.  With
+// REAL the level planes already hold the bands' DCT-II coefficients (real).
 // job.src: level 0 of the band sums (level l at + l * lev_stride), job.dst:
 // the output plane; X plane of the item at xbase + item * xstride.
-template <int WH>
+template <int WH, bool REAL>
 __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
     k_dct_rows_syn(const RowJob* __restrict__ jobs, int n_active, int nlev, size_t lev_stride,
                    const float2* src_base, float2* dst_base, const float* __restrict__ xbase, size_t xstride,
@@ -254,7 +255,19 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
   }
   // (a prefetch of the next level into a third buffer measured no faster:
   // fewer CTAs per SM)
-  for (int l = 0; l < nlev; l++) {
+  for (int l = 0; l < nlev && REAL; l++) {
+    const float4* Y = reinterpret_cast<const float4*>(src_base + job.src + (size_t)l * lev_stride + off);
+    const float4* Q = reinterpret_cast<const float4*>(resp + (size_t)l * resp_stride + 2 * off);
+    for (int e = threadIdx.x; e < C::RS * CH; e += C::T) {
+      const int s = e / CH, c = e - s * CH;
+      const float4 y = Y[(size_t)s * CH + c], q = __ldg(&Q[(size_t)s * CH + c]);
+      float4* a = reinterpret_cast<float4*>(S + s * (WH + 2) + 2 * c);
+      const float4 v = *a;
+      *a = make_float4(v.x + y.x * q.x, v.y + y.y * q.y, v.z + y.z * q.z, v.w + y.w * q.w);
+    }
+  }
+  if (REAL) __syncthreads();
+  for (int l = 0; l < nlev && !REAL; l++) {
     fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + (size_t)l * lev_stride + off);
     cp_async_wait_all();
     __syncthreads();
@@ -410,7 +423,8 @@ cudaError_t prepare_dct_kernels(int H, int WH) {
     e = dct_opt_in(k_dct_rows_fwd<n>, RowCfg<n>::smem_rm());                     \
     if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_ana<n, false>, RowCfg<n>::smem_rm()); \
     if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_ana<n, true>, RowCfg<n>::smem_rm()); \
-    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_syn<n>, 2 * RowCfg<n>::smem_rm()); \
+    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_syn<n, false>, 2 * RowCfg<n>::smem_rm()); \
+    if (e == cudaSuccess) e = dct_opt_in(k_dct_rows_syn<n, true>, 2 * RowCfg<n>::smem_rm()); \
     break;
     NSST_DCT_ROW_SIZES(CASE)
 #undef CASE
@@ -481,17 +495,24 @@ cudaError_t launch_dct_rows_ana(const RowJob* jobs, int njobs, int n_active, int
 cudaError_t launch_dct_rows_syn(const RowJob* jobs, int njobs, int n_active, int nlev, size_t lev_stride, int H,
                                 int W, const void* src_base, void* dst_base, const float* xbase, size_t xstride,
                                 const float* resp, size_t resp_stride, const float* tlow, const float2* twWh,
-                                const float2* twW, const float4* twD, cudaStream_t st) {
+                                const float2* twW, const float4* twD, cudaStream_t st, bool real_in) {
   if (njobs == 0) return cudaSuccess;
   count_launch();
   const float2* sb = static_cast<const float2*>(src_base);
   float2* db = static_cast<float2*>(dst_base);
   switch (W / 2) {
 #define CASE(n_)                                                                                              \
-  case n_:                                                                                                    \
-    k_dct_rows_syn<n_><<<dim3(H / RowCfg<n_>::RS, njobs), RowCfg<n_>::T, 2 * RowCfg<n_>::smem_rm(), st>>>(    \
-        jobs, n_active, nlev, lev_stride, sb, db, xbase, xstride, resp, resp_stride, tlow, twWh, twW, twD);   \
-    return cudaGetLastError();
+  case n_: {                                                                                                  \
+    const dim3 grid(H / RowCfg<n_>::RS, njobs);                                                               \
+    constexpr size_t sm = 2 * RowCfg<n_>::smem_rm();                                                          \
+    if (real_in)                                                                                              \
+      k_dct_rows_syn<n_, true><<<grid, RowCfg<n_>::T, sm, st>>>(jobs, n_active, nlev, lev_stride, sb, db, xbase, \
+                                                               xstride, resp, resp_stride, tlow, twWh, twW, twD); \
+    else                                                                                                      \
+      k_dct_rows_syn<n_, false><<<grid, RowCfg<n_>::T, sm, st>>>(jobs, n_active, nlev, lev_stride, sb, db, xbase, \
+                                                                xstride, resp, resp_stride, tlow, twWh, twW, twD); \
+    return cudaGetLastError();                                                                                \
+  }
     NSST_DCT_ROW_SIZES(CASE)
 #undef CASE
     default:

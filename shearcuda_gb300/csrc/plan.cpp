@@ -105,6 +105,7 @@ struct nsst_plan {
   RowJob* j_dct_syn = nullptr; // sum (all levels) -> pyr plane 1      (B)
   RowJob* j_dct_low = nullptr; // pyr plane 0 -> tmp plane 0: the lowpass band (B)
   ColJob* j_dct_lowc = nullptr; // tmp plane 0 in place                 (B)
+  RowJob* j_dct_rec = nullptr;  // lev (bands' DCT-II planes) -> pyr plane 1 (B)
 
   std::vector<double> scalars;
   bool has_scalars = false;
@@ -379,7 +380,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->dct_ok = filters_symmetric(p->pf) && cfg->pyramid != NSST_PYRAMID_DIRECT;
   if (cfg->pyramid == NSST_PYRAMID_SPECTRAL && !p->dct_ok)
     return destroy(fail(NSST_ERR_INVALID_ARG, "the spectral pyramid needs pyramid filters symmetric in both axes"));
-  size_t o_dct = 0, o_twDW = 0, o_wdH = 0, o_jd1 = 0, o_jd2 = 0, o_jd3 = 0, o_jd4 = 0, o_jd5 = 0, o_jd6 = 0;
+  size_t o_dct = 0, o_twDW = 0, o_wdH = 0, o_jd1 = 0, o_jd2 = 0, o_jd3 = 0, o_jd4 = 0, o_jd5 = 0, o_jd6 = 0, o_jd7 = 0;
   if (p->dct_ok) {
     o_dct = take(sizeof(float) * HW * (2 * p->nlev + 3));
     o_twDW = take(sizeof(float4) * (p->WH + 1));
@@ -390,6 +391,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     o_jd4 = take(sizeof(RowJob) * NB);
     o_jd5 = take(sizeof(RowJob) * NB);
     o_jd6 = take(sizeof(ColJob) * NB);
+    o_jd7 = take(sizeof(RowJob) * NB);
   }
   p->arena_bytes = off;
   ce = dev_alloc((void**)&p->arena, p->arena_bytes);
@@ -551,13 +553,14 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     p->j_dct_syn = (RowJob*)(A + o_jd4);
     p->j_dct_low = (RowJob*)(A + o_jd5);
     p->j_dct_lowc = (ColJob*)(A + o_jd6);
+    p->j_dct_rec = (RowJob*)(A + o_jd7);
     std::vector<float> tab;
     dct_pyramid_tables(p->pf, p->nlev, H, W, &tab);
     auto tw = dct_row_twiddles(W);
     auto wh = dct_col_twiddles(H);
     auto f2 = [&](const void* ptr) { return (size_t)((const char*)ptr - A) / sizeof(float2); };
     std::vector<ColJob> jx, js, jlc;
-    std::vector<RowJob> ja, jy, jl;
+    std::vector<RowJob> ja, jy, jl, jr;
     for (int i = 0; i < B; i++) {
       const size_t p0 = f2(p->pyr + i * p->s_pyr), p1 = f2(p->pyr + i * p->s_pyr + HW);
       const size_t lev = f2(p->lev + i * p->s_lev), sum = f2(p->sum + i * p->s_sum);
@@ -566,6 +569,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
       jy.push_back(RowJob{sum, p1, 0, i});
       jl.push_back(RowJob{p0, t0, p->dct_rl_plane, i});
       jlc.push_back(ColJob{t0, t0, 0, 0, 0, i});
+      jr.push_back(RowJob{lev, p1, 0, i});
       for (int l = 0; l < p->nlev; l++) {
         ja.push_back(RowJob{p0, lev + (size_t)l * HWh, l, i});
         js.push_back(ColJob{sum + (size_t)l * HWh, sum + (size_t)l * HWh, 0, 0, 0, i});
@@ -580,6 +584,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_syn, jy.data(), jy.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_low, jl.data(), jl.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_lowc, jlc.data(), jlc.size() * sizeof(ColJob), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->j_dct_rec, jr.data(), jr.size() * sizeof(RowJob), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = prepare_dct_kernels(H, p->WH);
     if (ce != cudaSuccess) return destroy(cuda_fail(ce, "DCT pyramid tables"));
     p->dct_on = true;
@@ -1157,6 +1162,28 @@ nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream)
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
+  if (p->dct_on && aligned16(x) && aligned16(y)) {
+    // spectral pyramid: the DCT-II of every band (into the level planes) and
+    // of the lowpass (tmp plane 0), then IDCT2(sum_l Q_l .* Y_l + G_low .* Y_0)
+    const int L = p->nlev;
+    const size_t HW = (size_t)p->H * p->W, HWh = (size_t)p->H * p->WH;
+    char* A = p->arena;
+    std::vector<const float*> src(L + 1);
+    std::vector<float*> dst(L + 1);
+    src[0] = y;
+    dst[0] = p->tmp;
+    for (int l = 0; l < L; l++) {
+      src[l + 1] = y + (size_t)(l + 1) * HW;
+      dst[l + 1] = reinterpret_cast<float*>(p->lev + (size_t)l * HWh);
+    }
+    NSST_TRY(enqueue_dct_rows_io(p, L + 1, src.data(), dst.data(), st));
+    NSST_CUDA(launch_dct_cols(kDct2, p->j_cols_lev, p->B * L, 1, p->H, p->W, A, A, p->twH, p->wdH, st));
+    NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_lowc, p->B, 1, p->H, p->W, A, A, p->twH, p->wdH, st));
+    NSST_CUDA(launch_dct_rows_syn(p->j_dct_rec, p->B, 1, L, HWh, p->H, p->W, A, A, p->tmp, p->s_tmp, p->dct_rs, HW,
+                                  p->dct_gl, p->twWh, p->twW, p->twDW, st, true));
+    const float* p1 = p->pyr + HW;
+    return enqueue_dct_cols_out(p, 1, &p1, &x, st);
+  }
   return run_atrousrec(p, 1, &y, nullptr, &x, st);
 }
 

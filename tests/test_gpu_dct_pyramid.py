@@ -218,3 +218,20 @@ def test_spectral_gradients_match_direct(built_lib, cuda, mode):
     assert rel_l2(gx1, gx2) <= 1e-3, rel_l2(gx1, gx2)
     if mode == 1:
         assert rel_l2(gt1, gt2) <= 1e-3, rel_l2(gt1, gt2)
+
+
+def test_spectral_atrousdec_atrousrec(built_lib, cuda):
+    # nsst_atrousdec / nsst_atrousrec (the reference's atrousdec / atrousrec) on
+    # the spectral pyramid: every plane within FP32 rounding of the direct one
+    import shearcuda_gb300 as sc
+    H, W = 384, 512
+    ps, pd = _plan(H, W, sc.PYRAMID_SPECTRAL), _plan(H, W, sc.PYRAMID_DIRECT)
+    x = _img(H, W, 12, cuda)
+    ys, yd = sc.atrousdec(x, ps), sc.atrousdec(x, pd)
+    for k in range(ys.shape[0]):
+        assert rel_l2(ys[k].cpu().numpy(), yd[k].cpu().numpy()) <= 1e-5, k
+    ys2 = ys.clone()
+    ys2[1:] *= 0.5  # a synthesis input that is not an analysis output
+    rs, rd = sc.atrousrec(ys2, ps), sc.atrousrec(ys2, pd)
+    assert rel_l2(rs.cpu().numpy(), rd.cpu().numpy()) <= 1e-5
+    assert rel_l2(sc.atrousrec(ys, ps).cpu().numpy(), x.cpu().numpy()) <= 1e-5
