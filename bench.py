@@ -453,7 +453,8 @@ def run_gpu(args):
                                    % BATCH,
                        'H': H, 'W': W, 'batch_per_gpu': BATCH, 'dcomp': DCOMP, 'dsize': DSIZE, 'lpfilt': 'maxflat',
                        'K': K, 'sigma': SIGMA, 'parallelism': 'replicas' if world > 1 else 'single',
-                       'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True},
+                       'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True,
+                       'pyramid': 'spectral (2-D DCT-II domain, NSST_PYRAMID_AUTO)'},
             'gpu_launches': kernels_per_step * args.steps, 'kernels_per_step': kernels_per_step,
             'clocks': clocks, 'roofline': roofline}
 
