@@ -101,3 +101,9 @@ def test_status_codes_without_gpu(built_lib):
     assert e.value.status in (1, 4)  # invalid name (4 only if no device at all)
     with pytest.raises(NsstError):
         sc.level_spectra(31, 3, 256, 256)
+    # pyramid modes: AUTO (0), DIRECT (1) and SPECTRAL (2) exist, others are
+    # rejected by the configuration check before any device call
+    with pytest.raises(NsstError) as e:
+        sc.ShearPlan([3, 3], [32, 32], 256, 256, pyramid=3)
+    assert e.value.status == 1 and 'pyramid mode' in str(e.value)
+    assert (sc.PYRAMID_AUTO, sc.PYRAMID_DIRECT, sc.PYRAMID_SPECTRAL) == (0, 1, 2)
