@@ -118,6 +118,86 @@ int nsst_plan_batch_capacity(const nsst_plan* plan);
  * per-call upload).  enable = 0 launches kernels one by one. */
 nsst_status nsst_plan_use_graphs(nsst_plan* plan, int enable);
 
+/* How nsst_denoise(_batch) runs the directional stage (analysis W_k .* Y and
+ * column IFFT, row C2R -> threshold -> R2C, synthesis column FFT and
+ * conj(W_k) sum; nsst_dec2.m:58, nsst_HT.m:34-46, nsst_rec2.m:27-33):
+ *   _SPLIT: three kernels, every band plane through device memory, as the
+ *           reference's shear_trans_cuda.cpp:228-233 / inverse_shear_cuda.cpp:222-286
+ *           materialise them;
+ *   _FUSED: one thread-block cluster per (image, level) keeps the bands on
+ *           chip (distributed shared memory); sizes 256x256, 384x512, 512x512;
+ *   _AUTO:  the autotuner's choice for the call's batch size
+ *           (nsst_plan_autotune), fused where untuned and available.
+ * The results agree to FP32 rounding.  Setting a mode drops the captured
+ * graphs.  NSST_ERR_UNSUPPORTED_SIZE if _FUSED has no configuration here. */
+enum { NSST_DIRECTIONAL_AUTO = 0, NSST_DIRECTIONAL_SPLIT = 1, NSST_DIRECTIONAL_FUSED = 2 };
+nsst_status nsst_plan_set_directional(nsst_plan* plan, int mode);
+
+/* The implementation (NSST_DIRECTIONAL_SPLIT or _FUSED) a call of n items
+ * runs; -1 for a NULL plan or n < 1. */
+int nsst_plan_directional(const nsst_plan* plan, int n);
+
+/* Autotuner.  Times every implementation of the directional stage this plan
+ * can run on n synthetic images (median of 7 passes after 2 warm-ups, CUDA
+ * events): the split kernels with each analysis variant (one CTA per band and
+ * column group, or per level streaming all its bands) and each row tile, and
+ * the fused cluster kernel where the size has one; the fastest becomes the
+ * choice of NSST_DIRECTIONAL_AUTO for batches in n's bucket (2^b <= n <
+ * 2^(b+1)) and the captured graphs are dropped.  It also evaluates direct
+ * (spatial) directional convolution, the alternative the reference offers
+ * nowhere on the GPU: the effective spatial filter of a band is
+ * ifft2(W_k / d) (nsst_dec2.m:47-57), which the normalisation by d spreads
+ * beyond the shearing filter's dsize support, so per level it finds the
+ * smallest square window around that support that keeps every band's
+ * truncation error <= 1e-5 relative L2 (0: none smaller than the image), and
+ * the lower bound of a direct convolution with it (support^2 FMAs per pixel
+ * and band, each way, at the FP32 FMA peak).  direct_wins is the verdict of
+ * the rule "every level has a window and the bound beats the fastest measured
+ * candidate"; no direct directional kernel is built, so the FFT candidates
+ * run whatever it says (at 256^2 .. 512^2 with dsize [32 32 16 16] the
+ * windows are 110-204 px and the bound is ~200x the FFT path's time).
+ * Synchronous; allocates 2 n images for the run. */
+enum { NSST_TUNE_MAX_CANDIDATES = 8 };
+typedef struct nsst_tune_result {
+  int n;                                     /* batch size timed */
+  int ncand;                                 /* candidates timed */
+  int chosen;                                /* index of the fastest */
+  char name[NSST_TUNE_MAX_CANDIDATES][48];   /* e.g. "split/level-analysis/rows8", "fused/cluster16" */
+  float ms[NSST_TUNE_MAX_CANDIDATES];        /* median ms of one directional-stage pass over n images */
+  int direct_support[NSST_MAX_LEVELS];       /* per level, px (0: no window below the image size) */
+  double direct_err[NSST_MAX_LEVELS];        /* per level: the worst band's truncation error at that window */
+  float direct_bound_ms;                     /* lower bound of the direct path (-1: some level has no window) */
+  int direct_wins;                           /* 1 if the rule above would pick direct convolution */
+} nsst_tune_result;
+nsst_status nsst_plan_autotune(nsst_plan* plan, int n, nsst_tune_result* out);
+
+/* The directional-stage candidates of a plan, in the autotuner's order, as
+ * newline-separated names into `names` (NUL-terminated, truncated to len);
+ * returns their count (-1 for a NULL plan). */
+int nsst_plan_directional_candidates(const nsst_plan* plan, char* names, size_t len);
+
+/* Make candidate `index` the automatic choice for batches in n's bucket, as if
+ * the autotuner had picked it; index -1 returns the bucket to the untuned
+ * default.  Drops the captured graphs. */
+nsst_status nsst_plan_select_directional(nsst_plan* plan, int n, int index);
+
+/* The autotuner's direct-convolution evaluation alone, on the host (no GPU):
+ * per level of cfg at H x W the smallest square window (px) around the
+ * shearing filter's support keeping every band's truncation error <= tol
+ * relative L2 (0: none below the image size), and the worst band's error
+ * there; support and err hold cfg->nlevels entries each. */
+nsst_status nsst_direct_support(const nsst_config* cfg, int H, int W, double tol, int* support, double* err);
+
+/* Co-resident clusters of the fused directional kernel (0: not available). */
+int nsst_plan_fused_clusters(const nsst_plan* plan);
+
+/* Synchronises the device and reads the plan's device error word:
+ * NSST_ERR_TIMEOUT if a bounded device-side wait (the fused kernel's TMA
+ * completion wait) ran out since the last check (the word is then cleared and
+ * the outputs of those calls are invalid), else NSST_OK.  No counterpart in
+ * the reference, whose kernels have no device-side waits. */
+nsst_status nsst_plan_check_device(nsst_plan* plan);
+
 /* Release a plan and all its device memory.
  * Replaces clear_shearing_filters_cuda (clear_shearing_filters_cuda.cpp:51-96). */
 nsst_status nsst_plan_destroy(nsst_plan* plan);

@@ -15,6 +15,7 @@ STATUS_NAMES = {0: 'NSST_OK', 1: 'NSST_ERR_INVALID_ARG', 2: 'NSST_ERR_UNSUPPORTE
                 3: 'NSST_ERR_OUT_OF_MEMORY', 4: 'NSST_ERR_CUDA', 5: 'NSST_ERR_TIMEOUT', 6: 'NSST_ERR_NUMERIC'}
 THRESH_HARD, THRESH_SOFT = 0, 1
 PYRAMID_AUTO, PYRAMID_DIRECT, PYRAMID_SPECTRAL = 0, 1, 2
+DIRECTIONAL_AUTO, DIRECTIONAL_SPLIT, DIRECTIONAL_FUSED = 0, 1, 2
 MAX_LEVELS = 8
 
 
@@ -35,6 +36,16 @@ class Nsst3Config(ctypes.Structure):
 class NsstSeparateInfo(ctypes.Structure):
     _fields_ = [('sigma', ctypes.c_double), ('stop', ctypes.c_double), ('buff_shear', ctypes.c_double),
                 ('buff_wavelet', ctypes.c_double), ('deltamax', ctypes.c_double), ('lam', ctypes.c_double)]
+
+
+TUNE_MAX_CANDIDATES = 8
+
+
+class NsstTuneResult(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_int), ('ncand', ctypes.c_int), ('chosen', ctypes.c_int),
+                ('name', (ctypes.c_char * 48) * TUNE_MAX_CANDIDATES), ('ms', ctypes.c_float * TUNE_MAX_CANDIDATES),
+                ('direct_support', ctypes.c_int * MAX_LEVELS), ('direct_err', ctypes.c_double * MAX_LEVELS),
+                ('direct_bound_ms', ctypes.c_float), ('direct_wins', ctypes.c_int)]
 
 
 class NsstError(RuntimeError):
@@ -58,6 +69,14 @@ SIGNATURES = [
     ('nsst_filters_load', _ci, [ctypes.c_char_p, _ip, _ip, _ip, _ip, _dp, _dp, _ip]),
     ('nsst_plan_create_from_file', _ci, [ctypes.c_char_p, _ci, _ci, _ci, ctypes.POINTER(_vp)]),
     ('nsst_plan_use_graphs', _ci, [_vp, _ci]),
+    ('nsst_plan_set_directional', _ci, [_vp, _ci]),
+    ('nsst_plan_directional', _ci, [_vp, _ci]),
+    ('nsst_plan_fused_clusters', _ci, [_vp]),
+    ('nsst_plan_check_device', _ci, [_vp]),
+    ('nsst_plan_autotune', _ci, [_vp, _ci, ctypes.POINTER(NsstTuneResult)]),
+    ('nsst_plan_select_directional', _ci, [_vp, _ci, _ci]),
+    ('nsst_plan_directional_candidates', _ci, [_vp, ctypes.c_char_p, _sz]),
+    ('nsst_direct_support', _ci, [ctypes.POINTER(NsstConfig), _ci, _ci, _cd, _ip, _dp]),
     ('nsst_plan_destroy', _ci, [_vp]),
     ('nsst_plan_num_bands', _ci, [_vp]),
     ('nsst_plan_band_levels', _ci, [_vp, _ip]),

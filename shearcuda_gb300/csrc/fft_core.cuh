@@ -651,6 +651,13 @@ __device__ __forceinline__ void block_fft_hook_ip(E* buf, const float2* __restri
   fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, after_first_read, typename FftPlan<N>::type{});
 }
 
+// block_fft_hook_ip with an explicit radix plan (a RadixList whose product is N)
+template <int N, int NSEQ, int T, int DIR, class Plan, class E, class Ld, class St, class Hook = NoHook>
+__device__ __forceinline__ void block_fft_hook_ip_plan(E* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                       const St& st, const Hook& after_first_read = Hook{}) {
+  fft_hook_ip_passes<N, NSEQ, T, DIR, 1, 0>(buf, tw, ld, st, after_first_read, Plan{});
+}
+
 // 16-byte asynchronous global -> shared copies (cp.async, sm_80+)
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);

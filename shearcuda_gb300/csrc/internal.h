@@ -35,6 +35,17 @@ struct ColJob {
   int item;      // batch item; jobs with item >= n_active are skipped
 };
 
+// One (item, level) of the fused directional stage (k_dir_fused.cu).
+struct FusedJob {
+  size_t dst;     // offset (float2) of the level's band-sum plane (column-IFFT'd, as k_band_synthesis leaves it)
+  size_t spec;    // offset (float2) of the level's first band spectrum
+  size_t m0;      // offset (float2) of the level's first column-0 side array
+  int ymap_row;   // first row of the level spectrum in the tensor map over the level spectra
+  int nbands;     // bands of the level
+  int th0;        // threshold index of the level's first band
+  int item;       // batch item; jobs with item >= n_active are skipped
+};
+
 struct AtrousJob {
   const float* xa;
   const float* xb;  // optional second input (synthesis)
@@ -109,9 +120,29 @@ cudaError_t prepare_atrous_kernels(int FA, int FB, int Mmax);
 cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                         void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
                         cudaStream_t st);
+// The band row pass (RowOp::Thresh) with tile_mult (1 or 2) times the rows of
+// RowCfg's tile per CTA.
+cudaError_t launch_rows_thresh(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                               void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
+                               int tile_mult, cudaStream_t st);
 cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, int H, int W, const float2* src_base,
                         float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                         cudaStream_t st);
+// Fused directional stage (k_dir_fused.cu): W_k .* Y -> column IFFT -> row
+// C2R -> threshold -> R2C -> column FFT -> sum conj(W_k) .* X -> column IFFT,
+// one thread-block cluster per (item, level) job, bands on chip.
+bool dir_fused_supported(int H, int WH);
+int dir_fused_cluster(int H, int WH);
+// kernel attributes (shared memory, cluster size) and the largest number of
+// co-resident clusters (0: the device cannot run them)
+cudaError_t prepare_dir_fused(int H, int WH, int* max_clusters);
+// tensor map (a 128-byte CUtensorMap at `out`, 64-byte aligned) over `rows`
+// rows of WH float2 starting at lev
+cudaError_t make_level_tmap(void* out, const float2* lev, int H, int WH, size_t rows);
+cudaError_t launch_dir_fused(const void* ymap, const FusedJob* jobs, int njobs, int n_active, int nclusters, int H,
+                             int W, float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
+                             const float2* twWh, const float2* twW, const float* thr, int mode, int* err,
+                             cudaStream_t st);
 cudaError_t launch_atrous(const AtrousJobs& jobs, int njobs, int maxH, int maxW, int M, int FA, const float* ha,
                           int FB, const float* hb, cudaStream_t st);
 // The DCT-domain pyramid of the fused pipeline (k_dct.cu).

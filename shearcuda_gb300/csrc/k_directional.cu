@@ -56,17 +56,6 @@ struct AnaCfg : ColCfg<N> {
 // packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM (tiles.cuh):
 // Z[k] = E + iO with E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k;
 // k = 0 unpacks the two real bins.
-template <int NSEQ>
-struct ThreshSt {
-  float2* p;
-  float th;
-  int mode;
-  __device__ __forceinline__ void operator()(int i, int s, float2 v) const {
-    v.x = apply_thresh(v.x, th, mode);
-    v.y = apply_thresh(v.y, th, mode);
-    p[i * NSEQ + s] = v;
-  }
-};
 // ---------------------------------------------------------------------------
 // Row kernels.  grid = (H / RS, njobs).
 // ---------------------------------------------------------------------------
@@ -111,34 +100,41 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_inv(co
   store_rows_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A);
 }
 
-// packed rows -> C2R -> threshold -> R2C -> packed rows (the fused band round trip)
-template <int WH>
-__global__ void __launch_bounds__(RowCfg<WH>::T, RowCfg<WH>::MINB) k_rows_thresh(const RowJob* __restrict__ jobs, int n_active,
-                                                                const float2* src_base, float2* dst_base,
-                                                                const float2* __restrict__ twWh,
-                                                                const float2* __restrict__ twW,
-                                                                const float* __restrict__ thr, int mode) {
-  using C = RowCfg<WH>;
+// packed rows -> C2R -> threshold -> R2C -> packed rows (the band round trip
+// of the split directional stage).  RS rows per CTA: RowCfg's tile, or a
+// multiple of it (the autotuner's row-tile candidates) with the threads per
+// row unchanged.
+template <int WH, int RS>
+struct RowTile {
+  static constexpr int T = RowCfg<WH>::T / RowCfg<WH>::RS * RS;
+  static constexpr int MINB = 1024 / T > 0 ? 1024 / T : 1;
+  static constexpr size_t smem() { return (size_t)RS * (WH + 2) * sizeof(float2); }
+};
+template <int WH, int RS = RowCfg<WH>::RS>
+__global__ void __launch_bounds__(RowTile<WH, RS>::T, RowTile<WH, RS>::MINB)
+    k_rows_thresh(const RowJob* __restrict__ jobs, int n_active, const float2* src_base, float2* dst_base,
+                  const float2* __restrict__ twWh, const float2* __restrict__ twW, const float* __restrict__ thr,
+                  int mode) {
+  constexpr int T = RowTile<WH, RS>::T;
   extern __shared__ float2 smem[];
-  float2 *A = smem, *B = smem + (size_t)WH * C::LD;
+  float2* A = smem;
   const RowJob job = jobs[blockIdx.y];
   if (job.item >= n_active) return;
   const float th = thr[job.th_index];
-  const size_t off = (size_t)blockIdx.x * C::RS * WH;
+  const size_t off = (size_t)blockIdx.x * RS * WH;
   // the tile arrives row-major (padded); the first pass reads it from there
   // and leaves the dense [index][row] layout in the same buffer
-  fetch_rows_rm<WH, C::RS, C::T>(A, src_base + job.src + off);
+  fetch_rows_rm<WH, RS, T>(A, src_base + job.src + off);
   cp_async_wait_all();
   __syncthreads();
   // C2R (pre-processing in the first pass) with the threshold in the last pass
   // (both transforms in place on one buffer: every pass reads all of its
   // inputs, the pre-processing's mirrored ones included, before a barrier)
-  (void)B;
-  block_fft_hook_ip<WH, C::RS, C::T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshSt<C::RS>{A, th, mode});
+  block_fft_hook_ip<WH, RS, T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshSt<RS>{A, th, mode});
   // R2C of the thresholded rows, its last pass back to the padded row-major
   // layout; post-processing fused with a store along the rows
-  block_fft_hook_ip<WH, C::RS, C::T, -1>(A, twWh, SmemLd<C::RS>{A}, SmemStRM<WH>{A});
-  r2c_post_store_rm<WH, C::RS, C::T>(dst_base + job.dst + off, A, twW);
+  block_fft_hook_ip<WH, RS, T, -1>(A, twWh, SmemLd<RS>{A}, SmemStRM<WH>{A});
+  r2c_post_store_rm<WH, RS, T>(dst_base + job.dst + off, A, twW);
 }
 
 // Band maxima (thresh.m's opt == 1 maximum with a zero threshold): C2R of the
@@ -447,6 +443,7 @@ cudaError_t prepare_row_kernels(int wh) {
     cudaError_t e = opt_in(k_rows_fwd<n>, sm);                                \
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
+    if (e == cudaSuccess) e = opt_in(k_rows_thresh<n, 2 * RowCfg<n>::RS>, RowTile<n, 2 * RowCfg<n>::RS>::smem()); \
     if (e == cudaSuccess) e = opt_in(k_rows_max<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * RowCfg<n>::smem_rm()); \
     return e;                                                                 \
@@ -500,6 +497,34 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
     else                                                                               \
       k_rows_thresh<n><<<grid, RowCfg<n>::T, smr, st>>>(jobs, n_active, sb, db, twWh, twW, thr, mode); \
     return cudaGetLastError();                                                         \
+  }
+    NSST_ROW_SIZES(CASE)
+#undef CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_rows_thresh(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
+                               void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
+                               int tile_mult, cudaStream_t st) {
+  if (tile_mult == 1)
+    return launch_rows(RowOp::Thresh, jobs, njobs, n_active, H, W, src_base, dst_base, twWh, twW, thr, mode, st);
+  if (tile_mult != 2) return cudaErrorInvalidValue;
+  const int WH = W / 2;
+  if (njobs == 0) return cudaSuccess;
+  count_launch();
+  const float2* sb = static_cast<const float2*>(src_base);
+  float2* db = static_cast<float2*>(dst_base);
+  switch (WH) {
+#define CASE(n)                                                                                         \
+  case n: {                                                                                             \
+    constexpr int RS2 = 2 * RowCfg<n>::RS;                                                              \
+    using Tl = RowTile<n, RS2>;                                                                         \
+    if (H % RS2 != 0) return cudaErrorInvalidValue;                                                     \
+    k_rows_thresh<n, RS2><<<dim3(H / RS2, njobs), Tl::T, Tl::smem(), st>>>(jobs, n_active, sb, db, twWh, twW, \
+                                                                         thr, mode);                    \
+    return cudaGetLastError();                                                                          \
   }
     NSST_ROW_SIZES(CASE)
 #undef CASE

@@ -20,6 +20,24 @@
 
 namespace nsst {
 
+// One implementation of the directional stage: the fused cluster kernel, or
+// the split kernels with an analysis variant (one CTA per band and column
+// group, or per level streaming all its bands) and a row tile (1 or 2 times
+// RowCfg's rows per CTA).
+struct DirChoice {
+  bool fused = false;
+  int ana = 0;       // 0: by grid size, 1: per level, 2: per band
+  int row_tile = 1;
+};
+
+// autotuner buckets of the batch size n: bucket b holds 2^b <= n < 2^(b+1)
+constexpr int kTuneBuckets = 13;
+inline int tune_bucket(int n) {
+  int b = 0;
+  while (b + 1 < kTuneBuckets && (2 << b) <= n) b++;
+  return b;
+}
+
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -106,6 +124,21 @@ struct nsst_plan {
   RowJob* j_dct_low = nullptr; // pyr plane 0 -> tmp plane 0: the lowpass band (B)
   ColJob* j_dct_lowc = nullptr; // tmp plane 0 in place                 (B)
   RowJob* j_dct_rec = nullptr;  // lev (bands' DCT-II planes) -> pyr plane 1 (B)
+
+  // fused directional stage (k_dir_fused.cu): one thread-block cluster per
+  // (item, level), the bands kept on chip
+  bool fused_ok = false;        // the size has a fused configuration and the device runs its clusters
+  int dir_mode = NSST_DIRECTIONAL_AUTO;
+  int fused_clusters = 0;       // co-resident clusters of the fused kernel
+  alignas(64) unsigned char fused_tmap[128] = {};  // TMA tensor map over the level spectra
+  FusedJob* j_fused = nullptr;  // (B*nlev) levels with more bands first, then items
+  int* dev_err = nullptr;       // error word of the bounded device waits
+  // autotuner record (nsst_plan_autotune): per batch-size bucket the fastest
+  // directional-stage candidate, and the candidate under test while tuning
+  bool tuned[kTuneBuckets] = {};
+  DirChoice tuned_choice[kTuneBuckets];
+  bool forcing = false;
+  DirChoice forced;
 
   std::vector<double> scalars;
   bool has_scalars = false;
@@ -255,6 +288,26 @@ void timer_mark(nsst_plan* p, const char* name, cudaStream_t st) {
 
 bool aligned16(const void* ptr) { return ((uintptr_t)ptr & 15) == 0; }
 
+// The directional-stage implementation of a denoise call of n items: the
+// candidate under test while tuning; else the plan's mode (split or fused),
+// with the tuned split settings where the autotuner chose a split candidate;
+// else (auto) the tuned choice of n's bucket; else the untuned default, the
+// fused kernel where it has been measured faster and its clusters fill the
+// GPU (256 x 256, one cluster per image and level), the split kernels otherwise.
+DirChoice dir_choice(const nsst_plan* p, int n) {
+  if (p->forcing) return p->forced;
+  const int b = tune_bucket(n);
+  DirChoice c;
+  if (p->tuned[b]) c = p->tuned_choice[b];
+  else c.fused = p->fused_ok && p->H == 256 && p->W == 256 && n * p->nlev >= p->fused_clusters;
+  if (p->dir_mode == NSST_DIRECTIONAL_SPLIT && c.fused) c = DirChoice{};
+  if (p->dir_mode == NSST_DIRECTIONAL_FUSED) c.fused = true;
+  if (!p->fused_ok) c.fused = false;
+  return c;
+}
+bool use_fused(const nsst_plan* p, int n) { return dir_choice(p, n).fused; }
+
+
 }  // namespace
 
 // ===================================================================== API
@@ -377,6 +430,8 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_j5 = take(sizeof(ColJob) * nL), o_j6 = take(sizeof(RowJob) * nL);
   size_t o_j7 = take(sizeof(RowJob) * p->ndir_total), o_j8 = take(sizeof(RowJob) * p->ndir_total);
   size_t o_j9 = take(sizeof(ColJob) * nL);
+  size_t o_jf = take(sizeof(FusedJob) * nL);
+  size_t o_err = take(sizeof(int) * 4);
   p->dct_ok = filters_symmetric(p->pf) && cfg->pyramid != NSST_PYRAMID_DIRECT;
   if (cfg->pyramid == NSST_PYRAMID_SPECTRAL && !p->dct_ok)
     return destroy(fail(NSST_ERR_INVALID_ARG, "the spectral pyramid needs pyramid filters symmetric in both axes"));
@@ -435,6 +490,10 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->j_rows_lev_inv = (RowJob*)(A + o_j6);
   p->j_coeff_fwd = (RowJob*)(A + o_j7);
   p->j_band_to_coeff = (RowJob*)(A + o_j8);
+  p->j_fused = (FusedJob*)(A + o_jf);
+  p->dev_err = (int*)(A + o_err);
+  ce = cudaMemset(p->dev_err, 0, sizeof(int) * 4);
+  if (ce != cudaSuccess) return destroy(cuda_fail(ce, "clear the device error word"));
 
   // ---- filter spectra (FP64 host) -> packed FP32 layout, scaled by 1/(H W)
   {
@@ -595,6 +654,33 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[1], 0, Mmax);
   if (ce == cudaSuccess) ce = prepare_atrous_kernels(p->pf.F[2], p->pf.F[3], Mmax);
   if (ce != cudaSuccess) return destroy(cuda_fail(ce, "kernel attribute setup"));
+  // fused directional stage: where the size has a configuration and the
+  // device can hold its clusters (else the split kernels run)
+  if (dir_fused_supported(H, p->WH)) {
+    int ncl = 0;
+    ce = prepare_dir_fused(H, p->WH, &ncl);
+    if (ce == cudaSuccess && ncl > 0)
+      ce = make_level_tmap(p->fused_tmap, p->lev, H, p->WH, (size_t)B * p->nlev * H);
+    if (ce == cudaSuccess && ncl > 0) {
+      auto f2 = [&](const void* ptr) { return (size_t)((const char*)ptr - A) / sizeof(float2); };
+      std::vector<int> order(p->nlev);
+      for (int l = 0; l < p->nlev; l++) order[l] = l;
+      // levels with more bands first: the long jobs start early
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return p->ndir[a] > p->ndir[b]; });
+      std::vector<FusedJob> jf;
+      for (int l : order)
+        for (int i = 0; i < B; i++)
+          jf.push_back(FusedJob{f2(p->sum + i * p->s_sum + (size_t)l * HWh), (size_t)p->first_band[l] * HWh,
+                                p->m0_off + (size_t)p->first_band[l] * H, (i * p->nlev + l) * H, p->ndir[l],
+                                i * p->nbands + 1 + p->first_band[l], i});
+      ce = cudaMemcpy(p->j_fused, jf.data(), jf.size() * sizeof(FusedJob), cudaMemcpyHostToDevice);
+      if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload fused job list"));
+      p->fused_ok = true;
+      p->fused_clusters = ncl;
+    } else {
+      (void)cudaGetLastError();  // the split kernels stay; clear a refused attribute or occupancy query
+    }
+  }
   *out = p;
   return NSST_OK;
 }
@@ -747,6 +833,48 @@ nsst_status nsst_plan_use_graphs(nsst_plan* p, int enable) {
   return NSST_OK;
 }
 
+nsst_status nsst_plan_set_directional(nsst_plan* p, int mode) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  if (mode != NSST_DIRECTIONAL_AUTO && mode != NSST_DIRECTIONAL_SPLIT && mode != NSST_DIRECTIONAL_FUSED)
+    return fail(NSST_ERR_INVALID_ARG, "unknown directional mode");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (mode == NSST_DIRECTIONAL_FUSED && !p->fused_ok)
+    return fail(NSST_ERR_UNSUPPORTED_SIZE,
+                "no fused directional configuration for this image size on this device (sizes 256x256, 384x512, "
+                "512x512)");
+  if (mode != p->dir_mode) {  // captured graphs hold the other kernels
+    for (auto& g : p->graphs)
+      if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key.clear();
+      }
+  }
+  p->dir_mode = mode;
+  return NSST_OK;
+}
+
+int nsst_plan_directional(const nsst_plan* p, int n) {
+  if (!p || n < 1) return -1;
+  return use_fused(p, n) ? NSST_DIRECTIONAL_FUSED : NSST_DIRECTIONAL_SPLIT;
+}
+
+int nsst_plan_fused_clusters(const nsst_plan* p) { return p && p->fused_ok ? p->fused_clusters : 0; }
+
+nsst_status nsst_plan_check_device(nsst_plan* p) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  int host[4] = {};
+  NSST_CUDA(cudaDeviceSynchronize());
+  NSST_CUDA(cudaMemcpy(host, p->dev_err, sizeof(host), cudaMemcpyDeviceToHost));
+  if (host[0] != 0) {
+    NSST_CUDA(cudaMemset(p->dev_err, 0, sizeof(host)));
+    return fail(NSST_ERR_TIMEOUT, "a bounded device-side wait (TMA completion) ran out; the outputs of the calls "
+                                  "since the last check are invalid");
+  }
+  return NSST_OK;
+}
+
 }  // extern "C"
 
 // ============================================================ stage helpers
@@ -853,16 +981,40 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 // group streams all bands of the level when that grid fills the GPU once (two
 // CTAs per SM); smaller batches (a single image) keep one CTA per (band,
 // item) column group, which has ndir times more CTAs.
-nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st) {
+nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0) {
   float2* base = (float2*)(grad ? p->garena : p->arena);
   const size_t ctas = (size_t)n * p->nlev * (p->WH / 8);
-  if (ctas >= (size_t)2 * p->sm_count) {
+  if (ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count)) {
     NSST_CUDA(launch_cols(ColOp::AnalysisLevel, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
                           p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, p->twH, st));
   } else {
     NSST_CUDA(launch_cols(ColOp::Analysis, grad ? p->gj_analysis : p->j_analysis, p->B * p->ndir_total, n, p->H,
                           p->W, base, base, p->spec, 0, p->twH, st));
   }
+  return NSST_OK;
+}
+
+// The directional stage of the fused denoise (level spectra in p->lev, band
+// sums out in p->sum): one cluster kernel, or the split analysis / row /
+// synthesis kernels with the bands in p->band.
+nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, cudaStream_t st) {
+  const DirChoice c = dir_choice(p, n);
+  if (c.fused) {
+    const int ncl = std::min(p->fused_clusters, n * p->nlev);
+    NSST_CUDA(launch_dir_fused(p->fused_tmap, p->j_fused, p->B * p->nlev, n, ncl, p->H, p->W, (float2*)p->arena,
+                               p->spec, (size_t)p->H * p->WH, p->twH, p->twWh, p->twW, TH, mode, p->dev_err, st));
+    timer_mark(p, "band_fused", st);
+    return NSST_OK;
+  }
+  char* A = p->arena;
+  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana));
+  timer_mark(p, "band_analysis_cols", st);
+  NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
+                               c.row_tile, st));
+  timer_mark(p, "band_rows_threshold", st);
+  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A,
+                        p->spec, (size_t)p->H * p->WH, p->twH, st));
+  timer_mark(p, "band_synthesis_cols", st);
   return NSST_OK;
 }
 
@@ -976,22 +1128,18 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
     NSST_TRY(enqueue_dct_rows_io(p, n, t0c.data(), t0.data(), st));
     timer_mark(p, "dct_lowpass_threshold", st);
   }
-  NSST_TRY(enqueue_band_analysis(p, n, false, st));
-  timer_mark(p, "band_analysis_cols", st);
   if (keep) {  // the thresholded bands to bandT: band keeps the pre-threshold spectra for the backward
+    NSST_TRY(enqueue_band_analysis(p, n, false, st));
+    timer_mark(p, "band_analysis_cols", st);
     NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW, TH,
                           mode, st));
     timer_mark(p, "band_rows_threshold", st);
     NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
                           (size_t)H * p->WH, p->twH, st));
+    timer_mark(p, "band_synthesis_cols", st);
   } else {
-    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH,
-                          mode, st));
-    timer_mark(p, "band_rows_threshold", st);
-    NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec,
-                          (size_t)H * p->WH, p->twH, st));
+    NSST_TRY(enqueue_directional(p, n, mode, TH, st));
   }
-  timer_mark(p, "band_synthesis_cols", st);
   return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st)
                     : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st);
 }
@@ -1016,22 +1164,18 @@ nsst_status enqueue_denoise(nsst_plan* p, int n, const float* const* x, float* c
   timer_mark(p, "fft_rows_fwd", st);
   NSST_CUDA(launch_cols(ColOp::Fwd, p->j_cols_lev, B * p->nlev, n, H, W, A2, A2, nullptr, 0, p->twH, st));
   timer_mark(p, "fft_cols_fwd", st);
-  NSST_TRY(enqueue_band_analysis(p, n, false, st));
-  timer_mark(p, "band_analysis_cols", st);
   if (keep) {
+    NSST_TRY(enqueue_band_analysis(p, n, false, st));
+    timer_mark(p, "band_analysis_cols", st);
     NSST_CUDA(launch_rows(RowOp::Thresh, p->gj_rows_T, B * p->ndir_total, n, H, W, A, p->garena, p->twWh, p->twW,
                           TH, mode, st));
     timer_mark(p, "band_rows_threshold", st);
     NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
                           (size_t)H * p->WH, p->twH, st));
+    timer_mark(p, "band_synthesis_cols", st);
   } else {
-    NSST_CUDA(launch_rows(RowOp::Thresh, p->j_rows_bands, B * p->ndir_total, n, H, W, A, A, p->twWh, p->twW, TH,
-                          mode, st));
-    timer_mark(p, "band_rows_threshold", st);
-    NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, B * p->nlev, n, H, W, A2, A2, p->spec, (size_t)H * p->WH,
-                          p->twH, st));
+    NSST_TRY(enqueue_directional(p, n, mode, TH, st));
   }
-  timer_mark(p, "band_synthesis_cols", st);
   NSST_CUDA(launch_rows(RowOp::Inv, p->j_rows_lev_inv, B * p->nlev, n, H, W, A, A, p->twWh, p->twW, nullptr, 0, st));
   timer_mark(p, "fft_rows_inv", st);
   std::vector<const float*> yr(n), low(n, nullptr);
@@ -1393,6 +1537,296 @@ nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const
   hit->used = ++p->graph_clock;
   count_launch(0);
   NSST_CUDA(cudaGraphLaunch(hit->exec, st));
+  return NSST_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The directional-stage candidates of a plan: the split kernels with each
+// analysis variant and row tile, and the fused cluster kernel where the plan
+// has it.
+std::vector<std::pair<DirChoice, std::string>> dir_candidates(const nsst_plan* p) {
+  std::vector<std::pair<DirChoice, std::string>> c;
+  const int rs = row_tile(p->WH);
+  for (int ana : {1, 2})
+    for (int rt : {1, 2}) {
+      DirChoice d;
+      d.ana = ana;
+      d.row_tile = rt;
+      if (p->H % (rs * rt) != 0) continue;
+      c.push_back({d, std::string("split/") + (ana == 1 ? "level" : "band") + "-analysis/rows" +
+                          std::to_string(rs * rt)});
+    }
+  if (p->fused_ok) {
+    DirChoice d;
+    d.fused = true;
+    c.push_back({d, "fused/cluster" + std::to_string(dir_fused_cluster(p->H, p->WH))});
+  }
+  return c;
+}
+
+// Direct (spatial) directional convolution instead of the FFT path: the
+// effective filter of band k is e_k = ifft2(W_k / d), d = sqrt(sum_j |W_j|^2)
+// (nsst_dec2.m:47-57), which the normalisation spreads over the whole image.
+// For each level the smallest square window around the shearing filter's own
+// support [0, dsize)^2 (circularly, with the same margin m on every side) that
+// keeps every band's truncation error ||e_k - window(e_k)|| / ||e_k|| <= tol;
+// 0 if no window smaller than the image does.  err: the worst band's error
+// at the largest window tried.
+void direct_support(int nlev, const int* dsize, const int* ndir, const std::vector<double>* shear_w, int H, int W,
+                    double tol, int* support, double* err) {
+  const int WC = W / 2 + 1;
+  for (int l = 0; l < nlev; l++) {
+    const int nd = ndir[l], ds = dsize[l];
+    std::vector<cd> S;
+    support[l] = 0;
+    err[l] = 1.0;
+    if (!level_spectra(shear_w[l], nd, ds, H, W, &S, host_threads())) continue;
+    const int mmax = (std::min(H, W) - ds) / 2 - 1;
+    std::vector<int> need(nd, -1);
+    std::vector<double> worst(nd, 0.0);
+    auto work = [&](int k) {
+      // full Hermitian spectrum -> 2-D inverse FFT (rows, then columns) -> e_k
+      std::vector<cd> F((size_t)H * W);
+      const cd* s = S.data() + (size_t)k * H * WC;
+      for (int u = 0; u < H; u++)
+        for (int v = 0; v < W; v++)
+          F[(size_t)u * W + v] = v < WC ? s[(size_t)u * WC + v] : std::conj(s[(size_t)((H - u) % H) * WC + (W - v)]);
+      for (int u = 0; u < H; u++) fft_inplace(F.data() + (size_t)u * W, W, +1);
+      std::vector<cd> col(H);
+      for (int v = 0; v < W; v++) {
+        for (int u = 0; u < H; u++) col[u] = F[(size_t)u * W + v];
+        fft_inplace(col.data(), H, +1);
+        for (int u = 0; u < H; u++) F[(size_t)u * W + v] = col[u];
+      }
+      // energy per circular "ring" distance from the filter's support
+      double total = 0.0;
+      std::vector<double> ring(std::max(H, W), 0.0);
+      for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+          const double e = std::norm(F[(size_t)i * W + j].real());
+          total += e;
+          auto dist = [&](int a, int n) {  // circular distance of a from [0, ds)
+            if (a < ds) return 0;
+            return std::min(a - ds + 1, n - a);
+          };
+          ring[std::max(dist(i, H), dist(j, W))] += e;
+        }
+      double inside = 0.0;
+      for (int m = 0; m <= mmax; m++) {
+        inside += ring[m];
+        const double rel = std::sqrt(std::max(total - inside, 0.0) / total);
+        if (m == mmax) worst[k] = rel;
+        if (rel <= tol) {
+          need[k] = m;
+          worst[k] = rel;
+          break;
+        }
+      }
+    };
+    std::vector<std::thread> th;
+    const int nt = std::min(host_threads(), nd);
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, t]() {
+        for (int k = t; k < nd; k += nt) work(k);
+      });
+    for (auto& t : th) t.join();
+    int m = 0;
+    double w = 0.0;
+    bool ok = true;
+    for (int k = 0; k < nd; k++) {
+      if (need[k] < 0) ok = false;
+      m = std::max(m, need[k]);
+      w = std::max(w, worst[k]);
+    }
+    support[l] = ok ? ds + 2 * m : 0;
+    err[l] = w;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+nsst_status nsst_plan_select_directional(nsst_plan* p, int n, int index) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const auto cands = dir_candidates(p);
+  const int b = tune_bucket(n);
+  if (index < 0) {
+    p->tuned[b] = false;
+  } else {
+    if (index >= (int)cands.size()) return fail(NSST_ERR_INVALID_ARG, "candidate index out of range");
+    p->tuned[b] = true;
+    p->tuned_choice[b] = cands[index].first;
+  }
+  for (auto& g : p->graphs)
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      g.key.clear();
+    }
+  return NSST_OK;
+}
+
+int nsst_plan_directional_candidates(const nsst_plan* p, char* names, size_t len) {
+  if (!p) return -1;
+  const auto cands = dir_candidates(p);
+  std::string all;
+  for (const auto& c : cands) all += c.second + "\n";
+  if (names && len) {
+    const size_t m = std::min(all.size(), len - 1);
+    std::memcpy(names, all.data(), m);
+    names[m] = 0;
+  }
+  return (int)cands.size();
+}
+
+nsst_status nsst_direct_support(const nsst_config* cfg, int H, int W, double tol, int* support, double* err) {
+  if (!cfg || !support || !err) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(validate_config(cfg, H, W));
+  if (!(tol > 0.0)) return fail(NSST_ERR_INVALID_ARG, "tol must be positive");
+  std::vector<std::vector<double>> w(cfg->nlevels);
+  std::vector<int> nd(cfg->nlevels);
+  for (int l = 0; l < cfg->nlevels; l++) {
+    w[l] = shearing_filters_myer(cfg->dsize[l], cfg->dcomp[l]);
+    nd[l] = 1 << cfg->dcomp[l];
+  }
+  direct_support(cfg->nlevels, cfg->dsize, nd.data(), w.data(), H, W, tol, support, err);
+  return NSST_OK;
+}
+
+nsst_status nsst_plan_autotune(nsst_plan* p, int n, nsst_tune_result* res) {
+  if (!p) return fail(NSST_ERR_INVALID_ARG, "NULL plan");
+  if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "item count outside [1, batch capacity]");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t HW = (size_t)p->H * p->W;
+  float* buf = nullptr;
+  cudaError_t ce = dev_alloc((void**)&buf, sizeof(float) * HW * 2 * (size_t)n);
+  if (ce != cudaSuccess) return cuda_fail(ce, "autotune image buffers");
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool was_timing = p->timing;
+  auto cleanup = [&]() {
+    p->forcing = false;
+    p->timing = was_timing;
+    if (st) cudaStreamSynchronize(st);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    cudaFree(buf);
+  };
+  auto bail = [&](nsst_status s) {
+    cleanup();
+    return s;
+  };
+  // a noisy test image (N(128, 40^2)), the same for every item
+  {
+    std::vector<float> h(HW);
+    std::mt19937_64 gen(20261204);
+    std::normal_distribution<double> nd(128.0, 40.0);
+    for (auto& v : h) v = (float)nd(gen);
+    for (int i = 0; i < n; i++) {
+      ce = cudaMemcpy(buf + (size_t)i * HW, h.data(), HW * sizeof(float), cudaMemcpyHostToDevice);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "autotune input upload"));
+    }
+  }
+  ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) return bail(cuda_fail(ce, "autotune stream / events"));
+  std::vector<const float*> xs(n);
+  std::vector<float*> outs(n);
+  for (int i = 0; i < n; i++) {
+    xs[i] = buf + (size_t)i * HW;
+    outs[i] = buf + (size_t)(n + i) * HW;
+  }
+  std::vector<double> sig(n, 20.0), K(p->nlev + 1, 3.0);
+  K[0] = 0.0;
+  K[p->nlev] = 4.0;
+  std::vector<double> sc = p->has_scalars ? p->scalars : std::vector<double>(p->nbands, 1.0);
+  p->timing = false;
+  p->forcing = false;
+  float lmax = 0.f;
+  nsst_status s = upload_thresholds(p, n, sig.data(), K.data(), sc.data(), st, &lmax);
+  // one full pass leaves the level spectra that every candidate reads
+  if (s == NSST_OK) s = enqueue_denoise(p, n, xs.data(), outs.data(), NSST_THRESH_HARD, false, st);
+  if (s != NSST_OK) return bail(s);
+  auto cands = dir_candidates(p);
+  std::vector<float> med(cands.size());
+  for (size_t c = 0; c < cands.size(); c++) {
+    p->forcing = true;
+    p->forced = cands[c].first;
+    std::vector<float> t;
+    for (int r = 0; r < 9; r++) {
+      ce = cudaEventRecord(e0, st);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaEventRecord"));
+      s = enqueue_directional(p, n, NSST_THRESH_HARD, p->th, st);
+      if (s != NSST_OK) return bail(s);
+      ce = cudaEventRecord(e1, st);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      if (ce != cudaSuccess) return bail(cuda_fail(ce, "autotune timing"));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r >= 2) t.push_back(ms);  // two warm-up passes
+    }
+    std::sort(t.begin(), t.end());
+    med[c] = t[t.size() / 2];
+  }
+  p->forcing = false;
+  {
+    int host_err[4] = {};
+    ce = cudaMemcpy(host_err, p->dev_err, sizeof(host_err), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "read the device error word"));
+    if (host_err[0] != 0) {
+      cudaMemset(p->dev_err, 0, sizeof(host_err));
+      return bail(fail(NSST_ERR_TIMEOUT, "a bounded device-side wait ran out while tuning"));
+    }
+  }
+  const size_t best = (size_t)(std::min_element(med.begin(), med.end()) - med.begin());
+  const int b = tune_bucket(n);
+  p->tuned[b] = true;
+  p->tuned_choice[b] = cands[best].first;
+  for (auto& g : p->graphs)  // captured graphs hold the previous choice
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      g.key.clear();
+    }
+  if (res) {
+    std::memset(res, 0, sizeof(*res));
+    res->n = n;
+    res->ncand = (int)std::min<size_t>(cands.size(), NSST_TUNE_MAX_CANDIDATES);
+    res->chosen = (int)best;
+    for (int c = 0; c < res->ncand; c++) {
+      std::snprintf(res->name[c], sizeof(res->name[c]), "%s", cands[c].second.c_str());
+      res->ms[c] = med[c];
+    }
+    direct_support(p->nlev, p->cfg.dsize, p->ndir.data(), p->shear_w.data(), p->H, p->W, 1e-5, res->direct_support,
+                   res->direct_err);
+    // A direct convolution with the truncated filters costs support^2 FMAs
+    // per pixel and band for the analysis and as many for the synthesis; its
+    // lower bound is that work at the FP32 FMA peak (SMs x 128 lanes x clock).
+    // It is chosen only if every level has a support (the truncation is
+    // proven within 1e-5) and the bound beats the fastest measured candidate.
+    int khz = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev);
+    const double fma_per_s = (double)p->sm_count * 128.0 * (khz > 0 ? khz * 1e3 : 2.07e9);
+    double fmas = 0.0;
+    bool all = true;
+    for (int l = 0; l < p->nlev; l++) {
+      const double s2 = (double)res->direct_support[l] * res->direct_support[l];
+      if (res->direct_support[l] == 0) all = false;
+      fmas += 2.0 * s2 * (double)HW * p->ndir[l] * n;
+    }
+    res->direct_bound_ms = all ? (float)(fmas / fma_per_s * 1e3) : -1.0f;
+    res->direct_wins = all && res->direct_bound_ms < med[best] ? 1 : 0;
+  }
+  cleanup();
   return NSST_OK;
 }
 

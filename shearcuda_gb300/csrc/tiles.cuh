@@ -38,6 +38,19 @@ __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {
   return a > 0.0f ? copysignf(a, v) : 0.0f;
 }
 
+// threshold of both real values of a packed element, stored dense [i][s]
+template <int NSEQ>
+struct ThreshSt {
+  float2* p;
+  float th;
+  int mode;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const {
+    v.x = apply_thresh(v.x, th, mode);
+    v.y = apply_thresh(v.y, th, mode);
+    p[i * NSEQ + s] = v;
+  }
+};
+
 // FFT hooks (see block_fft_hook).
 template <int NSEQ>
 struct SmemLd {

@@ -28,9 +28,10 @@ import ctypes
 import numpy as np
 import torch
 
-from ._lib import (NsstConfig, NsstError, NsstItem, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO, check, lib)
+from ._lib import (NsstConfig, NsstError, NsstItem, NsstTuneResult, THRESH_HARD, THRESH_SOFT, PYRAMID_AUTO,
+                   DIRECTIONAL_AUTO, DIRECTIONAL_SPLIT, DIRECTIONAL_FUSED, check, lib)
 
-__all__ = ['ShearPlan', 'prepare_shearing_filters_cuda', 'clear_shearing_filters_cuda', 'shear_trans_cuda',
+__all__ = ['ShearPlan', 'direct_support', 'prepare_shearing_filters_cuda', 'clear_shearing_filters_cuda', 'shear_trans_cuda',
            'thresh_cuda', 'softth_cuda', 'inverse_shear_cuda', 'atrousdec', 'atrousrec', 'atrousdec_noalloc',
            'nsst_scalars',
            'nsst_denoise', 'nsst_denoise_batch', 'MultiBatch', 'pyramid_filters', 'shearing_filters',
@@ -105,6 +106,46 @@ class ShearPlan:
 
     def use_graphs(self, on=True):
         check(lib().nsst_plan_use_graphs(self.handle, 1 if on else 0))
+
+    def set_directional(self, mode):
+        """'auto', 'split' or 'fused': the kernels of the directional stage of
+        nsst_denoise (see nsst_plan_set_directional)."""
+        m = {'auto': DIRECTIONAL_AUTO, 'split': DIRECTIONAL_SPLIT, 'fused': DIRECTIONAL_FUSED}[mode]
+        check(lib().nsst_plan_set_directional(self.handle, m))
+
+    def directional(self, n=1):
+        """The directional implementation a call of n images runs: 'split' or 'fused'."""
+        return {DIRECTIONAL_SPLIT: 'split', DIRECTIONAL_FUSED: 'fused'}[lib().nsst_plan_directional(self.handle, n)]
+
+    def fused_clusters(self):
+        return lib().nsst_plan_fused_clusters(self.handle)
+
+    def autotune(self, n=1):
+        """Time every directional-stage candidate on n images; the fastest
+        becomes the automatic choice for batches of n's size bucket.  Returns
+        {'n', 'candidates': [(name, ms)], 'chosen': name, 'direct_support',
+        'direct_err', 'direct_bound_ms', 'direct_wins'} (see nsst_plan_autotune)."""
+        r = NsstTuneResult()
+        check(lib().nsst_plan_autotune(self.handle, int(n), ctypes.byref(r)))
+        cands = [(bytes(r.name[i]).split(b'\0')[0].decode(), float(r.ms[i])) for i in range(r.ncand)]
+        return {'n': r.n, 'candidates': cands, 'chosen': cands[r.chosen][0],
+                'direct_support': list(r.direct_support)[:self.nlevels],
+                'direct_err': list(r.direct_err)[:self.nlevels], 'direct_bound_ms': float(r.direct_bound_ms),
+                'direct_wins': bool(r.direct_wins)}
+
+    def directional_candidates(self):
+        buf = ctypes.create_string_buffer(1024)
+        n = lib().nsst_plan_directional_candidates(self.handle, buf, 1024)
+        return buf.value.decode().split('\n')[:n]
+
+    def select_directional(self, n, index):
+        """Make candidate `index` (of directional_candidates()) the automatic
+        choice for batches of n's size bucket; -1 restores the default."""
+        check(lib().nsst_plan_select_directional(self.handle, int(n), int(index)))
+
+    def check_device(self):
+        """Raise NsstError(NSST_ERR_TIMEOUT) if a bounded device-side wait ran out."""
+        check(lib().nsst_plan_check_device(self.handle))
 
     @property
     def handle(self):
@@ -359,6 +400,22 @@ class MultiBatch:
             self.close()
         except Exception:
             pass
+
+
+def direct_support(dcomp, dsize, H, W, tol=1e-5):
+    """Per level: the smallest square window (px) of the effective spatial
+    directional filters keeping the truncation error <= tol (0: none below the
+    image size), and the worst band's error there (host only, no GPU)."""
+    cfg = NsstConfig()
+    cfg.nlevels = len(dcomp)
+    for i, (c, s) in enumerate(zip(dcomp, dsize)):
+        cfg.dcomp[i] = int(c)
+        cfg.dsize[i] = int(s)
+    cfg.lpfilt = b'maxflat'
+    sup = (ctypes.c_int * len(dcomp))()
+    err = (ctypes.c_double * len(dcomp))()
+    check(lib().nsst_direct_support(ctypes.byref(cfg), int(H), int(W), float(tol), sup, err))
+    return list(sup), list(err)
 
 
 def launch_count():

@@ -1,0 +1,133 @@
+"""The fused directional stage (one thread-block cluster per image and level,
+bands on chip) against the split kernels and against the FP64 oracle.
+
+Tolerances:
+  * fused vs split denoise on the same plan: the same mathematics in FP32,
+    with radix plans that may differ between the two, so relative L2 <= 1e-5
+    under the soft threshold, and under the hard threshold (a coefficient
+    within rounding of t flips) relative L2 <= 1e-4 and |dPSNR| <= 0.01 dB;
+    a batch and a single image on the fused kernel: bit-identical;
+  * vs the oracle: |PSNR_gpu - PSNR_oracle| <= 0.01 dB, and relative L2 <=
+    1e-5 under the soft threshold (1-Lipschitz, so FP32 rounding of the
+    coefficients cannot flip a decision by more than it moves them).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import DCOMP, DSIZE, K_DEMO, flat_scalars, rel_l2
+from oracle import nsst2d
+
+pytestmark = pytest.mark.gpu
+
+FUSED_SIZES = [(256, 256), (384, 512), (512, 512)]
+_cache = {}
+
+
+def _setup(H, W, seed=0):
+    key = (H, W, seed)
+    if key not in _cache:
+        import shearcuda_gb300 as sc
+        from shearcuda_gb300.synth import noisy_image
+        clean, noisy = noisy_image(H, W, 20.0, seed)
+        sf = nsst2d.shear_spectra(H, W, DCOMP, DSIZE)
+        scal = nsst2d.nsst_scalars(H, W, sf, seed=100, nthreads=8)
+        shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=3)
+        _cache[key] = (clean, noisy.astype(np.float32), sf, scal, shear)
+    return _cache[key]
+
+
+@pytest.mark.parametrize('HW', FUSED_SIZES)
+def test_fused_available(built_lib, cuda, HW):
+    clean, noisy32, sf, scal, shear = _setup(*HW)
+    assert shear.fused_clusters() > 0
+    shear.set_directional('fused')
+    assert shear.directional(1) == 'fused'
+    shear.set_directional('split')
+    assert shear.directional(3) == 'split'
+    shear.set_directional('auto')
+    # untuned default: the split kernels unless the fused kernel was measured
+    # faster for the size and its clusters fill the GPU (256 x 256, >= 9 images)
+    assert shear.directional(1) == 'split'
+
+
+def test_fused_default_for_large_256_batches(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256, batch=16)
+    assert shear.directional(16) == 'fused'
+    assert shear.directional(2) == 'split'
+
+
+@pytest.mark.parametrize('HW', FUSED_SIZES)
+@pytest.mark.parametrize('mode', [0, 1])
+def test_fused_equals_split(built_lib, cuda, HW, mode):
+    import shearcuda_gb300 as sc
+    clean, noisy32, sf, scal, shear = _setup(*HW)
+    from shearcuda_gb300.synth import noisy_image
+    xs = [torch.tensor(noisy32, device=cuda)]
+    for s in (1, 2):
+        xs.append(torch.tensor(noisy_image(HW[0], HW[1], 20.0, s)[1].astype(np.float32), device=cuda))
+    sig = [20.0, 12.0, 33.0]
+    flat = flat_scalars(scal)
+    shear.set_directional('split')
+    ref = [o.cpu().numpy() for o in sc.nsst_denoise_batch(xs, shear, sig, K_DEMO, flat, mode=mode)]
+    shear.set_directional('fused')
+    got = [o.cpu().numpy() for o in sc.nsst_denoise_batch(xs, shear, sig, K_DEMO, flat, mode=mode)]
+    shear.check_device()
+    for g, r, x in zip(got, ref, xs):
+        if mode == 1:
+            assert rel_l2(g, r) <= 1e-5, rel_l2(g, r)
+        else:
+            assert rel_l2(g, r) <= 1e-4, rel_l2(g, r)
+    d = abs(nsst2d.psnr(clean, got[0].astype(np.float64)) - nsst2d.psnr(clean, ref[0].astype(np.float64)))
+    assert d <= 0.01, d
+    # one image alone on the same plan (n < capacity): the same bits as in the batch
+    one = sc.nsst_denoise(xs[1], shear, sig[1], K_DEMO, flat, mode=mode).cpu().numpy()
+    np.testing.assert_array_equal(one, got[1])
+    shear.set_directional('auto')
+
+
+@pytest.mark.parametrize('HW', FUSED_SIZES)
+@pytest.mark.parametrize('mode', ['hard', 'soft'])
+def test_fused_matches_oracle(built_lib, cuda, HW, mode):
+    import shearcuda_gb300 as sc
+    clean, noisy32, sf, scal, shear = _setup(*HW)
+    shear.set_directional('fused')
+    x = torch.tensor(noisy32, device=cuda)
+    out = sc.nsst_denoise(x, shear, 20.0, K_DEMO, flat_scalars(scal), mode=0 if mode == 'hard' else 1)
+    out = out.cpu().numpy().astype(np.float64)
+    shear.check_device()
+    shear.set_directional('auto')
+    ref, _ = nsst2d.denoise(noisy32.astype(np.float64), 20.0, K_DEMO, scal, DCOMP, DSIZE, mode=mode, shear_f=sf,
+                            nthreads=8)
+    p_gpu, p_ref = nsst2d.psnr(clean, out), nsst2d.psnr(clean, ref)
+    assert abs(p_gpu - p_ref) <= 0.01, (p_gpu, p_ref)
+    if mode == 'soft':
+        assert rel_l2(out, ref) <= 1e-5, rel_l2(out, ref)
+    else:
+        assert rel_l2(out, ref) <= 1e-3
+
+
+def test_fused_graph_replay(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    clean, noisy32, sf, scal, shear = _setup(512, 512)
+    shear.set_directional('fused')
+    x = [torch.tensor(noisy32, device=cuda)]
+    flat = flat_scalars(scal)
+    eager = sc.nsst_denoise_batch(x, shear, [20.0], K_DEMO, flat)[0].cpu().numpy()
+    shear.use_graphs(True)
+    for _ in range(3):
+        rep = sc.nsst_denoise_batch(x, shear, [20.0], K_DEMO, flat)[0].cpu().numpy()
+        np.testing.assert_array_equal(rep, eager)
+    shear.use_graphs(False)
+    shear.check_device()
+    shear.set_directional('auto')
+
+
+def test_fused_rejected_where_unsupported(built_lib, cuda):
+    import shearcuda_gb300 as sc
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 1024, 1024)
+    assert shear.fused_clusters() == 0
+    assert shear.directional(1) == 'split'
+    with pytest.raises(sc.NsstError):
+        shear.set_directional('fused')

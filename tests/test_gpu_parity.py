@@ -120,6 +120,7 @@ def test_fused_denoise_equals_materialised_chain(built_lib, cuda):
     import shearcuda_gb300 as sc
     clean, noisy32, _, sf, scal = _setup(512, 512)
     shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 512, 512, pyramid=sc.PYRAMID_DIRECT)
+    shear.set_directional('split')  # test_gpu_fused.py covers the cluster kernel
     x = torch.tensor(noisy32, device=cuda)
     flat = flat_scalars(scal)
     fused = sc.nsst_denoise(x, shear, 20.0, K_DEMO, flat)
