@@ -16,9 +16,14 @@ are all 2^a 3^b, and the result is cropped back.  This convention is shared by
 the oracle and the GPU path.
 """
 import math
+import os
 
 import numpy as np
 from scipy import fft as sfft
+
+# FFT worker threads: the transforms split over independent 1-D sequences,
+# so the result does not depend on the count
+WORKERS = os.cpu_count() or 1
 
 PYR_MODES = {1: ([0.5, 0.25], [1 / 6, 1 / 12], [1.0, 2.0]),
              1.5: ([0.5, 3 / 8], [1 / 7, 1 / 9], [1.5, 2.0]),
@@ -130,13 +135,13 @@ def pyr_dec(x, L=3, mode=1.5):
     """PyrNDDec_mm.m:20-109 with OutD = 'S' (DoPyrDec.m): [HP fine ... coarse, LP]."""
     w, t, d = pyr_params(mode, L)
     N = x.ndim
-    X = ccsym(sfft.fftn(x), N - 1, 'c')
+    X = ccsym(sfft.fftn(x, workers=WORKERS), N - 1, 'c')
     subs = []
     for n in range(L):
         Lp, Hp = prysd_dec_onestep(X, w[n], t[n], d[n])
         X = Lp
-        subs.append(np.real(sfft.ifftn(ccsym(Hp, N - 1, 'e'))))
-    subs.append(np.real(sfft.ifftn(ccsym(X, N - 1, 'e'))))
+        subs.append(np.real(sfft.ifftn(ccsym(Hp, N - 1, 'e'), workers=WORKERS)))
+    subs.append(np.real(sfft.ifftn(ccsym(X, N - 1, 'e'), workers=WORKERS)))
     return subs
 
 
@@ -145,11 +150,11 @@ def pyr_rec(subs, mode=1.5):
     L = len(subs) - 1
     w, t, d = pyr_params(mode, L)
     N = subs[0].ndim
-    Lp = ccsym(sfft.fftn(subs[-1]), N - 1, 'c')
+    Lp = ccsym(sfft.fftn(subs[-1], workers=WORKERS), N - 1, 'c')
     for n in range(L - 1, -1, -1):
-        Hp = ccsym(sfft.fftn(subs[n]), N - 1, 'c')
+        Hp = ccsym(sfft.fftn(subs[n], workers=WORKERS), N - 1, 'c')
         Lp = prysd_rec_onestep(Lp, Hp, w[n], t[n], d[n])
-    return np.real(sfft.ifftn(ccsym(Lp, N - 1, 'e')))
+    return np.real(sfft.ifftn(ccsym(Lp, N - 1, 'e'), workers=WORKERS))
 
 
 # ----------------------------------------------------------------------------
@@ -289,12 +294,30 @@ def convnfft_same(A, B):
     for dim in range(A.ndim):
         m, n = A.shape[dim], B.shape[dim]
         lf = 2 ** math.ceil(math.log2(m + n - 1))
-        out = sfft.fft(out, lf, axis=dim)
-        Bs = sfft.fft(Bs, lf, axis=dim)
+        out = sfft.fft(out, lf, axis=dim, workers=WORKERS)
+        Bs = sfft.fft(Bs, lf, axis=dim, workers=WORKERS)
         s0 = math.ceil((n - 1) / 2)
         subs.append(slice(s0, s0 + m))
-    out = np.real(sfft.ifftn(out * Bs))
+    out = np.real(sfft.ifftn(out * Bs, workers=WORKERS))
     return out[tuple(subs)]
+
+
+def convnfft_same_level(BPl, filters):
+    """convnfft 'same' (convnfft.m:79-201) of one level's volume with each of
+    several filters, restated with real FFTs at the smallest fast length >=
+    m + n - 1 per axis and the volume's transform shared by the filters.  Any
+    length >= m + n - 1 gives the same linear convolution (convnfft.m's
+    power-of-two length included), so this equals convnfft_same up to FP64
+    rounding (test_oracle3d.py checks 1e-12); it is several times faster on
+    the large volumes."""
+    shp = [sfft.next_fast_len(m + n - 1, real=True) for m, n in zip(BPl.shape, filters[0].shape)]
+    A = sfft.rfftn(BPl, shp, workers=WORKERS)
+    out = []
+    for f in filters:
+        s0 = [math.ceil((n - 1) / 2) for n in f.shape]
+        full = sfft.irfftn(A * sfft.rfftn(f, shp, workers=WORKERS), shp, workers=WORKERS)
+        out.append(full[tuple(slice(a, a + m) for a, m in zip(s0, BPl.shape))])
+    return out
 
 
 def band_list(F):
@@ -326,14 +349,24 @@ def nsst_scalars3(shape, F, seed, L=3, mode=1.5):
     return mad(bp[L]), np.asarray(out)
 
 
-def denoise3(x, F, sigma, T, band_scalars, L=3, mode=1.5):
+def denoise3(x, F, sigma, T, band_scalars, L=3, mode=1.5, fast=False):
     """The 3-D denoise of DenoiseDemo/main.m:35-75: pyramid, per band
     convnfft 'same', hard threshold (ThresholdShCoeff.m: zero where
     |c| <= T(l) sigma bandEst), band + cone sums (ShRec.m, main.m:58-63),
-    lowpass untouched (main.m:67), pyramid reconstruction."""
+    lowpass untouched (main.m:67), pyramid reconstruction.  fast: the
+    convolutions through convnfft_same_level (same results to FP64 rounding)."""
     bp = pyr_dec(x, L, mode)
     rec = [np.zeros_like(b) for b in bp[:L]] + [bp[L]]
-    for b, (c, l, l2, l1, f) in enumerate(band_list(F)):
+    bands = band_list(F)
+    if fast:
+        coefs = {}
+        for l in range(L):
+            idx = [b for b, bd in enumerate(bands) if bd[1] == l]
+            for b, c in zip(idx, convnfft_same_level(bp[l], [bands[b][4] for b in idx])):
+                c[np.abs(c) <= T[l] * sigma * band_scalars[b]] = 0.0
+                rec[l] += c
+        return pyr_rec(rec, mode)
+    for b, (c, l, l2, l1, f) in enumerate(bands):
         coef = convnfft_same(bp[l], f)
         coef[np.abs(coef) <= T[l] * sigma * band_scalars[b]] = 0.0
         rec[l] += coef
@@ -373,8 +406,18 @@ def pad_size(n, L=3, mode=1.5):
     raise ValueError('volume dimension %d larger than 192' % n)
 
 
+def marshal_data(X, level=3):
+    """MarshalData.m:1-22 as the reference ships it: every dimension x gains
+    d - rem(x, d) planes, d = divFactor(level) = [3 6 12 24](level), by
+    replicating its last plane (so a multiple of d gains d planes: 128 -> 132,
+    192 -> 204, 96 -> 108 for three levels)."""
+    d = [3, 6, 12, 24][level - 1]
+    return np.pad(X, [(0, d - (s % d)) for s in X.shape], mode='edge')
+
+
 def pad_volume(x):
-    """Edge replication to pad_size in every dimension (as MarshalData.m:3-22)."""
+    """Edge replication to pad_size in every dimension (MarshalData.m's edge
+    replication, to the GPU path's 2^a 3^b grid instead of marshal_data's)."""
     pads = [(0, pad_size(s) - s) for s in x.shape]
     return np.pad(x, pads, mode='edge')
 
@@ -412,7 +455,7 @@ def corr_same(G, B):
     Z[tuple(sl)] = G
     Bp = np.zeros(L)
     Bp[tuple(slice(0, n) for n in B.shape)] = B
-    out = np.real(sfft.ifftn(sfft.fftn(Z) * np.conj(sfft.fftn(Bp))))
+    out = np.real(sfft.ifftn(sfft.fftn(Z, workers=WORKERS) * np.conj(sfft.fftn(Bp, workers=WORKERS)), workers=WORKERS))
     return out[tuple(slice(0, m) for m in G.shape)]
 
 

@@ -169,3 +169,27 @@ def test_denoise3_adjoint_dot_product_and_fd():
     # the denoise is linear where the masks hold: J x = denoise(x)
     full = nsst3d.denoise3(nsst3d.pad_volume_to(x, grid), F, 30.0, [3.0, 3.0], sc, L=2)[:40, :44, :36]
     assert np.abs(nsst3d.denoise3_jvp(x, masks, F, grid, L=2) - full).max() < 1e-9 * np.abs(full).max()
+
+
+def test_marshal_data_restates_the_reference_padding():
+    # MarshalData.m:3-22 with level 3 (divFactor 12): every dimension gains
+    # 12 - rem(x, 12) replicated planes, even when it is already a multiple
+    from oracle import nsst3d
+    x = np.arange(5 * 6 * 7, dtype=np.float64).reshape(5, 6, 7)
+    for level, d in ((1, 3), (2, 6), (3, 12), (4, 24)):
+        y = nsst3d.marshal_data(x, level)
+        assert y.shape == tuple(s + d - s % d for s in x.shape)
+        assert np.array_equal(y[:5, :6, :7], x)
+        assert np.array_equal(y[-1, :6, :7], x[-1])
+        assert np.array_equal(y[:5, :6, -1], x[:, :, -1])
+    assert nsst3d.marshal_data(np.zeros((128, 192, 96)), 3).shape == (132, 204, 108)
+
+
+def test_level_convolution_equals_convnfft_same():
+    from oracle import nsst3d
+    F = nsst3d.meyer_filters_3d([2, 2])
+    x = np.random.default_rng(2).standard_normal((24, 30, 36))
+    fs = [b[4] for b in nsst3d.band_list(F)[:4]]
+    for f, got in zip(fs, nsst3d.convnfft_same_level(x, fs)):
+        ref = nsst3d.convnfft_same(x, f)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
