@@ -48,6 +48,12 @@ def parse():
     ap.add_argument('--sep-batch', type=int, default=8, help='images per batched separation call')
     ap.add_argument('--v3-sizes', default='128,192', help='volume edge lengths of the v3 workload')
     ap.add_argument('--v3-batch', type=int, default=4, help='volumes per batched v3 pass')
+    ap.add_argument('--directional', default='auto', choices=['auto', 'split', 'fused'],
+                    help='directional-stage kernels of the batched pass: the autotuner\'s choice (auto, the plan is '
+                         'tuned for the batch first) or one forced implementation (for profiling it)')
+    ap.add_argument('--cpu-sweep', action='store_true',
+                    help='only the CPU baseline table: the FP64 oracle port at 512^2, 1024^2 and 2048^2, one thread '
+                         'and all host threads (median of 5 / 5 / 3 runs); no GPU work')
     return ap.parse_args()
 
 
@@ -79,7 +85,8 @@ def job_throughput(units_per_rank, world, seconds):
 def cpu_baseline(min_seconds=10.0, max_images=8):
     """The oracle (FP64 NumPy/SciPy + C atrous restatement) on the host cores,
     on a bounded sample of the same workload: whole 512x512 images of the
-    batch, one at a time, until min_seconds have passed."""
+    batch, one at a time, until min_seconds have passed; and one image on a
+    single thread."""
     from oracle import nsst2d
     from shearcuda_gb300.synth import noisy_image
     cores = os.cpu_count() or 1
@@ -94,8 +101,42 @@ def cpu_baseline(min_seconds=10.0, max_images=8):
         if time.perf_counter() - t0 >= min_seconds:
             break
     dt = time.perf_counter() - t0
+    _, noisy = noisy_image(H, W, SIGMA, 0)
+    t1 = time.perf_counter()
+    nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=1)
+    one = time.perf_counter() - t1
     return {'value': n / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': '%d of the 512x512 images, dec+thresh+rec, filter/scalar setup excluded, %.1f s' % (n, dt)}
+            'sample': '%d of the 512x512 images, dec+thresh+rec, filter/scalar setup excluded, %.1f s' % (n, dt),
+            'single_thread': {'value': 1.0 / one, 'unit': UNIT, 'cores': 1, 'sample': 'one 512x512 image, %.1f s' % one}}
+
+
+def cpu_sweep():
+    """The CPU baseline table: the oracle port's dec + hard threshold + rec
+    per image at 512^2, 1024^2 and 2048^2 (seeds 0, 1, 2, sigma 20), on one
+    thread and on every host thread (median of 5, 5 and 3 runs), filter and
+    scalar setup timed separately."""
+    from oracle import nsst2d
+    from shearcuda_gb300.synth import noisy_image
+    cores = os.cpu_count() or 1
+    rows = []
+    for (H_, W_), seed, reps in (((512, 512), 0, 5), ((1024, 1024), 1, 5), ((2048, 2048), 2, 3)):
+        t0 = time.perf_counter()
+        sf = nsst2d.shear_spectra(H_, W_, DCOMP, DSIZE)
+        scal = nsst2d.nsst_scalars(H_, W_, sf, seed=100, nthreads=cores)
+        setup = time.perf_counter() - t0
+        _, noisy = noisy_image(H_, W_, SIGMA, seed)
+        row = {'H': H_, 'W': W_, 'setup_s': setup}
+        for nt in (1, cores):
+            ts = []
+            for _ in range(reps):
+                t1 = time.perf_counter()
+                nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=nt)
+                ts.append(time.perf_counter() - t1)
+            row['threads_%d' % nt] = {'median_s': float(np.median(ts)), 'runs': reps,
+                                      'images_per_s': 1.0 / float(np.median(ts))}
+        rows.append(row)
+        print(json.dumps({'cpu_sweep_row': row}), flush=True)
+    print(json.dumps({'workload': 'cpu_sweep', 'cores': cores, 'kind': 'port', 'rows': rows}), flush=True)
 
 
 def run_reference(args):
@@ -196,9 +237,84 @@ def measured_peak():
         return 6800.0, 'fallback'
 
 
+# Stage groups of the library's per-stage timers, mapped to the terms of the
+# fused design's algorithmic traffic (per image of N pixels, FP32): pyramid
+# analysis 48N B (4 levels x read 1 + write 2 images), directional 32N B
+# (4 levels x read the band-pass level + write its band sum) plus the filter
+# spectra, 192N B, once per distinct size per launch, synthesis 48N B.
+STAGE_GROUPS = {
+    'pyramid_analysis': ('dct_rows_image', 'dct_cols_image', 'dct_rows_levels', 'dct_cols_levels',
+                         'dct_lowpass_threshold', 'fft_rows_fwd', 'fft_cols_fwd'),
+    'directional': ('band_analysis_cols', 'band_rows_threshold', 'band_synthesis_cols', 'band_fused'),
+    'synthesis': ('dct_cols_sums', 'dct_rows_synthesis', 'dct_cols_image_out', 'fft_rows_inv', 'lowpass_threshold'),
+}
+
+
+def s8d_bytes(nimg, H_, W_):
+    """Algorithmic HBM bytes of one pass over nimg images of one size, per
+    stage group (the spectra counted once per launch)."""
+    N = H_ * W_
+    return {'pyramid_analysis': 48 * N * nimg, 'directional': 32 * N * nimg + 192 * N, 'synthesis': 48 * N * nimg}
+
+
+def fft_flops(nimg, H_, W_, ntrans=104):
+    """FP32 flops of the pass's 2-D real FFTs: per image 4 level transforms,
+    48 band inverses, 48 band forwards and 4 level inverses, 2.5 N log2 N each."""
+    N = H_ * W_
+    return nimg * ntrans * 2.5 * N * np.log2(N)
+
+
+def fp32_peak_tflops(sm_count):
+    """Nominal FP32 FMA peak: SMs x 128 lanes x 2 flop x the maximum SM clock
+    (MEASURED_PEAKS.json's sm_max_mhz, else 2070 MHz)."""
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            mhz = float(json.load(f).get('sm_max_mhz', mhz))
+    except (OSError, ValueError):
+        pass
+    return sm_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def roofline_report(stage_ms, nimg, H_, W_, peak, peak_kind, ms_per_step, sm_count, traffic_db=None):
+    """The roofline object of the bench line: the directional stage (the
+    dominant one) against the HBM peak with the fused design's algorithmic
+    bytes, the same for the whole step and each stage group, and the FFT
+    arithmetic against the FP32 peak."""
+    alg = s8d_bytes(nimg, H_, W_)
+    groups = {}
+    for g, names in STAGE_GROUPS.items():
+        ms = sum(stage_ms.get(k, 0.0) for k in names)
+        if ms > 0:
+            a = alg[g] / (ms / 1000.0) / 1e9
+            groups[g] = {'ms': ms, 'algorithmic_bytes': alg[g], 'achieved_gbs': a, 'frac': a / peak}
+    d = groups.get('directional', {'ms': float('nan'), 'achieved_gbs': float('nan')})
+    step_bytes = sum(alg.values())
+    step_gbs = step_bytes / (ms_per_step / 1000.0) / 1e9
+    traffic, ratio = None, None
+    if traffic_db:
+        parts = [traffic_db[k] for k in STAGE_GROUPS['directional'] if k in stage_ms and k in traffic_db]
+        if parts and len(parts) == sum(1 for k in STAGE_GROUPS['directional'] if k in stage_ms):
+            traffic = float(sum(parts)) * nimg / traffic_db.get('_images', nimg)
+            ratio = traffic / alg['directional']
+    fl = fft_flops(nimg, H_, W_)
+    pk = fp32_peak_tflops(sm_count)
+    ach = fl / (ms_per_step / 1000.0) / 1e12
+    return {'bound': 'hbm', 'achieved': d['achieved_gbs'], 'peak': peak, 'unit': 'GB/s',
+            'frac': d['achieved_gbs'] / peak, 'traffic': traffic, 'traffic_ratio': ratio,
+            'kernel': 'directional stage (%s)' % ' + '.join(k for k in STAGE_GROUPS['directional'] if k in stage_ms),
+            'kernel_ms': d['ms'], 'algorithmic_bytes_per_launch': alg['directional'], 'peak_source': peak_kind,
+            'step': {'algorithmic_bytes': step_bytes, 'achieved_gbs': step_gbs, 'frac': step_gbs / peak},
+            'stage_groups': groups,
+            'compute': {'bound': 'fp32', 'fft_flops_per_step': fl, 'achieved_tflops': ach, 'peak_tflops': pk,
+                        'frac': ach / pk, 'peak_source': 'nominal (SMs x 128 FP32 lanes x 2 x max SM clock)'},
+            'stages_ms': stage_ms}
+
+
 def algorithmic_bytes(stage, nimg, H_, W_, nlev=4, nbands_dir=48):
-    """Algorithmic HBM bytes of one launch of a stage over nimg images of
-    H_ x W_ (FP32 real images: 4 B/px; packed spectra: 8 B per 2 px)."""
+    """Bytes one launch of a split-pipeline stage moves as designed (band
+    planes materialised: FP32 real images 4 B/px, packed spectra 8 B per 2 px);
+    reported beside the fused design's algorithmic bytes (s8d_bytes)."""
     N = H_ * W_
     per = {
         # band round trip: read the band's packed spectrum and write it back
@@ -371,6 +487,13 @@ def run_gpu(args):
 
     plan = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=BATCH)
     scal = sc.nsst_scalars(plan, seed=100)  # product's Monte-Carlo scalars (setup, untimed)
+    # the directional kernels: the autotuner's pick for this batch (setup,
+    # untimed), or the one forced on the command line
+    tune = None
+    if args.directional == 'auto':
+        tune = plan.autotune(BATCH)
+    else:
+        plan.set_directional(args.directional)
     plan.use_graphs(True)
     host = []
     for i in range(BATCH):
@@ -430,21 +553,22 @@ def run_gpu(args):
     plan.enable_timers(False)
     plan.use_graphs(True)
     stage_avg = {k: float(np.median(v)) for k, v in stage_ms.items()}
-    dom = max(stage_avg, key=stage_avg.get)
     peak, peak_kind = measured_peak()
-    alg = algorithmic_bytes(dom, BATCH, H, W)
-    achieved = alg / (stage_avg[dom] / 1000.0) / 1e9
-    traffic = None
+    traffic_db = None
     tpath = os.path.join(ROOT, 'profiles', 'ncu_traffic.json')
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get(dom)
+            traffic_db = json.load(open(tpath))
         except ValueError:
-            traffic = None
-    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-                'traffic': traffic, 'kernel': dom, 'peak_source': peak_kind,
-                'kernel_ms': stage_avg[dom], 'algorithmic_bytes_per_launch': alg,
-                'stages_ms': stage_avg}
+            traffic_db = None
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    roofline = roofline_report(stage_avg, BATCH, H, W, peak, peak_kind, ms_per_step, sms, traffic_db)
+    # the split kernels' own bytes (band planes materialised), for the dominant one
+    dom = max(stage_avg, key=stage_avg.get)
+    mat = algorithmic_bytes(dom, BATCH, H, W)
+    if mat:
+        roofline['dominant_launch'] = {'kernel': dom, 'ms': stage_avg[dom], 'bytes_as_designed': mat,
+                                       'achieved_gbs': mat / (stage_avg[dom] / 1000.0) / 1e9}
 
     line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
@@ -454,9 +578,15 @@ def run_gpu(args):
                        'H': H, 'W': W, 'batch_per_gpu': BATCH, 'dcomp': DCOMP, 'dsize': DSIZE, 'lpfilt': 'maxflat',
                        'K': K, 'sigma': SIGMA, 'parallelism': 'replicas' if world > 1 else 'single',
                        'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True,
-                       'pyramid': 'spectral (2-D DCT-II domain, NSST_PYRAMID_AUTO)'},
+                       'pyramid': 'spectral (2-D DCT-II domain, NSST_PYRAMID_AUTO)',
+                       'directional': tune['chosen'] if tune else args.directional},
             'gpu_launches': kernels_per_step * args.steps, 'kernels_per_step': kernels_per_step,
             'clocks': clocks, 'roofline': roofline}
+    if tune:
+        line['autotune'] = {'n': tune['n'], 'chosen': tune['chosen'],
+                            'candidates_ms': {c: m for c, m in tune['candidates']},
+                            'direct_support_px': tune['direct_support'], 'direct_err': tune['direct_err'],
+                            'direct_bound_ms': tune['direct_bound_ms'], 'direct_wins': tune['direct_wins']}
 
     if not args.no_extras:
         # ---- e2e through the public API with host buffers: every step copies its
@@ -532,11 +662,17 @@ def run_gpu(args):
         counts = {}
         for _, nz, _ in items:
             counts[nz.shape] = counts.get(nz.shape, 0) + 1
-        plans = []
+        plans, singles, uchoice = [], {}, {}
         for shp, cnt in counts.items():
             pp = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, shp[0], shp[1], batch=cnt)
-            sc.nsst_scalars(pp, seed=100)
+            us = sc.nsst_scalars(pp, seed=100)
+            uchoice['%dx%d' % shp] = pp.autotune(cnt)['chosen']
             plans.append(pp)
+            p1s = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, shp[0], shp[1])
+            p1s.set_scalars(us)
+            p1s.autotune(1)
+            p1s.use_graphs(True)
+            singles[shp] = p1s
         m = sc.MultiBatch(plans)
         uxs = [torch.tensor(nz.astype(np.float32), device=dev) for _, nz, _ in items]
         uouts = [torch.empty_like(x) for x in uxs]
@@ -554,10 +690,75 @@ def run_gpu(args):
             torch.cuda.synchronize()
             ut += e0.elapsed_time(e1)
         npx = sum(x.numel() for x in uxs)
-        line['uneven_b64'] = {'images_per_s': BATCH / (ut / nu / 1000.0), 'ms_per_batch': ut / nu,
-                              'megapixels': npx / 1e6, 'sizes': {'%dx%d' % k: v for k, v in counts.items()}}
+        # the plain path on the same 64 images: one call per image through a
+        # single-image plan of its size (graph replay, tuned for one image)
+        pouts = [torch.empty_like(x) for x in uxs]
+        for _ in range(2):
+            for x, o, sg in zip(uxs, pouts, usig):
+                sc.nsst_denoise(x, singles[tuple(x.shape)], sg, K, None, out=o)
+        torch.cuda.synchronize()
+        pt = 0.0
+        for _ in range(3):
+            flush.fill_(1.0)
+            e0.record(stream)
+            for x, o, sg in zip(uxs, pouts, usig):
+                sc.nsst_denoise(x, singles[tuple(x.shape)], sg, K, None, out=o)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            pt += e0.elapsed_time(e1)
+        pt /= 3
+        same = all(torch.equal(a, b) for a, b in zip(uouts, pouts))
+        ub = BATCH / (ut / nu / 1000.0)
+        up = BATCH / (pt / 1000.0)
+        line['uneven_b64'] = {'images_per_s': ub, 'ms_per_batch': ut / nu, 'megapixels': npx / 1e6,
+                              'gigapixels_per_s': npx / (ut / nu / 1000.0) / 1e9,
+                              'plain_images_per_s': up, 'plain_ms': pt, 'vs_plain': ub / up,
+                              'plain_equals_batched': same, 'directional': uchoice,
+                              'sizes': {'%dx%d' % k: v for k, v in counts.items()}}
         m.close()
-        del plans
+        del plans, singles
+
+        # ---- single images at 1024^2 and 2048^2 (the plain pipeline as a
+        # drop-in): images/s and per-stage times against the roofline
+        big = {}
+        for (Hb, Wb), seed in (((1024, 1024), 1), ((2048, 2048), 2)):
+            pb = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, Hb, Wb)
+            sc.nsst_scalars(pb, seed=100)
+            tb = pb.autotune(1)
+            xb = torch.tensor(noisy_image(Hb, Wb, SIGMA, seed)[1].astype(np.float32), device=dev)
+            ob = torch.empty_like(xb)
+            pb.use_graphs(True)
+            for _ in range(3):
+                sc.nsst_denoise(xb, pb, SIGMA, K, None, out=ob)
+            torch.cuda.synchronize()
+            reps = 10
+            bt = 0.0
+            for _ in range(reps):
+                flush.fill_(1.0)
+                e0.record(stream)
+                sc.nsst_denoise(xb, pb, SIGMA, K, None, out=ob)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                bt += e0.elapsed_time(e1)
+            bt /= reps
+            pb.use_graphs(False)
+            pb.enable_timers(True)
+            st_ms = {}
+            for _ in range(3):
+                flush.fill_(1.0)
+                sc.nsst_denoise(xb, pb, SIGMA, K, None, out=ob)
+                for name, ms in pb.read_timers():
+                    st_ms.setdefault(name, []).append(ms)
+            pb.enable_timers(False)
+            st_avg = {k: float(np.median(v)) for k, v in st_ms.items()}
+            rf = roofline_report(st_avg, 1, Hb, Wb, peak, peak_kind, bt, sms, None)
+            big['%dx%d' % (Hb, Wb)] = {'images_per_s': 1000.0 / bt, 'ms_per_image': bt,
+                                        'directional': tb['chosen'], 'stages_ms': st_avg,
+                                        'stage_groups': rf['stage_groups'], 'step': rf['step'],
+                                        'compute': rf['compute']}
+            del pb, xb, ob
+            torch.cuda.empty_cache()
+        line['single_image_p1k_p2k'] = big
 
         # ---- differentiable config: 16 x 512^2, forward vs forward + hand-written adjoint
         pd = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=16)
@@ -639,7 +840,9 @@ def main():
     args = parse()
     global BATCH
     BATCH = args.batch
-    if args.impl == 'reference':
+    if args.cpu_sweep:
+        cpu_sweep()
+    elif args.impl == 'reference':
         run_reference(args)
     elif args.workload == 'v3':
         run_v3(args)

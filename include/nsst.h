@@ -248,8 +248,8 @@ nsst_status nsst_atrousrec(nsst_plan* plan, const float* y, float* x, void* stre
  * plane 0 lowpass, then bandpass coarse -> fine), both device pointers, and
  * the one scratch image the lowpass chain needs lives in a static device array
  * of 2048*2048 floats (16 MiB) that every GPU loading the library holds until
- * exit.  H*W above 2048*2048 is rejected with NSST_ERR_UNSUPPORTED_SIZE.
- * The first call on a device does a one-time set-up for that device (the
+ * exit.  H*W above 2048*2048 is rejected with NSST_ERR_UNSUPPORTED_SIZE,
+ * an x that overlaps y with NSST_ERR_INVALID_ARG.  The first call on a device does a one-time set-up for that device (the
  * array's device address, kernel shared-memory limits); make that first call
  * before any stream capture.  All calls share the one array and it keeps the
  * last call's contents (nothing in it needs to start at zero): calls that

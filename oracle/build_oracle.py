@@ -11,7 +11,8 @@
 Both reference builds happen only when the reference checkout is present (it
 is not on machines that only run tests).
 
-Usage: python oracle/build_oracle.py [--reference DIR]
+Usage: python oracle/build_oracle.py [--reference DIR]  (default: $SHEARCUDA_REFERENCE, else
+``reference`` beside the repository)
 """
 import argparse
 import os
@@ -22,7 +23,18 @@ PORT_SO = os.path.join(HERE, 'libatrous_port.so')
 REF_DIR = os.path.join(HERE, '_ref')
 REF_SO = os.path.join(REF_DIR, 'libatrousc_ref.so')
 RWT_SO = os.path.join(REF_DIR, 'librwt_ref.so')
-DEFAULT_REFERENCE = '/root/reference'
+
+
+def default_reference():
+    """The reference checkout: $SHEARCUDA_REFERENCE, else a directory named
+    `reference` beside this repository's directory."""
+    env = os.environ.get('SHEARCUDA_REFERENCE')
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), 'reference')
+
+
+DEFAULT_REFERENCE = default_reference()
 
 
 def _newer(target, sources):

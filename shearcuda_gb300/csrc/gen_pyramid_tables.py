@@ -76,4 +76,7 @@ def main(path):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference/shearlet_toolbox_1/atrousfilters.m')
+    # the reference checkout: an argument, $SHEARCUDA_REFERENCE, else `reference` beside the repository
+    ref = os.environ.get('SHEARCUDA_REFERENCE') or os.path.join(
+        os.path.dirname(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))), 'reference')
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ref, 'shearlet_toolbox_1', 'atrousfilters.m'))

@@ -71,6 +71,16 @@ extern "C" nsst_status nsst_atrousdec_noalloc(const float* x, float* y, int H, i
               "use a plan (nsst_plan_create + nsst_atrousdec) for larger images");
     return NSST_ERR_UNSUPPORTED_SIZE;
   }
+  {
+    // the input must not overlap the (nlevels+1) output planes: level 0
+    // writes planes while its kernels still read x
+    const uintptr_t xb = (uintptr_t)x, xe = xb + (uintptr_t)H * (uintptr_t)W * sizeof(float);
+    const uintptr_t yb = (uintptr_t)y, ye = yb + (uintptr_t)(nlevels + 1) * H * W * sizeof(float);
+    if (xb < ye && yb < xe) {
+      set_error("nsst_atrousdec_noalloc: x overlaps the output planes y");
+      return NSST_ERR_INVALID_ARG;
+    }
+  }
   const PyrTable* tab = find_table(lpfilt && lpfilt[0] ? lpfilt : "maxflat");
   if (!tab) {
     set_error("nsst_atrousdec_noalloc: unknown pyramid filter name");

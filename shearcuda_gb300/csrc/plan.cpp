@@ -8,6 +8,7 @@
 // reference it also owns static job lists for each kernel stage, so one call
 // is a fixed sequence of launches on the caller's stream.
 #include <algorithm>
+#include <initializer_list>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -287,6 +288,24 @@ void timer_mark(nsst_plan* p, const char* name, cudaStream_t st) {
 }
 
 bool aligned16(const void* ptr) { return ((uintptr_t)ptr & 15) == 0; }
+
+// The spectral pyramid moves 16-byte elements of the caller's images.  Under
+// NSST_PYRAMID_AUTO a call with an image that is not 16-byte aligned runs on
+// the direct pyramid instead (the same results to FP32 rounding); under
+// NSST_PYRAMID_SPECTRAL such a call is an error rather than a silent switch.
+nsst_status check_spectral(const nsst_plan* p, std::initializer_list<const void*> ptrs) {
+  if (!p->dct_on || p->cfg.pyramid != NSST_PYRAMID_SPECTRAL) return NSST_OK;
+  for (const void* q : ptrs)
+    if (q && !aligned16(q))
+      return fail(NSST_ERR_INVALID_ARG,
+                  "NSST_PYRAMID_SPECTRAL needs 16-byte aligned images (NSST_PYRAMID_AUTO runs this call on the "
+                  "direct pyramid)");
+  return NSST_OK;
+}
+nsst_status check_spectral_n(const nsst_plan* p, int n, const float* const* a, const float* const* b) {
+  for (int i = 0; i < n; i++) NSST_TRY(check_spectral(p, {a ? a[i] : nullptr, b ? b[i] : nullptr}));
+  return NSST_OK;
+}
 
 // The directional-stage implementation of a denoise call of n items: the
 // candidate under test while tuning; else the plan's mode (split or fused),
@@ -1270,6 +1289,7 @@ extern "C" {
 
 nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_spectral(p, {x, y}));
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
@@ -1302,6 +1322,7 @@ nsst_status nsst_atrousdec(nsst_plan* p, const float* x, float* y, void* stream)
 
 nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream) {
   if (!p || !x || !y) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_spectral(p, {x, y}));
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
@@ -1333,6 +1354,7 @@ nsst_status nsst_atrousrec(nsst_plan* p, const float* y, float* x, void* stream)
 
 nsst_status nsst_shear_trans(nsst_plan* p, const float* x, float* coeffs, void* stream) {
   if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_spectral(p, {x}));
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
@@ -1451,6 +1473,7 @@ nsst_status nsst_band_norms(nsst_plan* p, double* E) {
 
 nsst_status nsst_inverse_shear(nsst_plan* p, const float* coeffs, float* x, void* stream) {
   if (!p || !x || !coeffs) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_spectral(p, {x}));
   if (!aligned16(coeffs)) return fail(NSST_ERR_INVALID_ARG, "coeffs must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
@@ -1487,6 +1510,7 @@ nsst_status nsst_denoise_batch(nsst_plan* p, const float* const* x, float* const
   if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
   for (int i = 0; i < n; i++)
     if (!x[i] || !out[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  NSST_TRY(check_spectral_n(p, n, x, out));
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // the arena no longer holds the last differentiable forward
   cudaStream_t st = (cudaStream_t)stream;
@@ -2248,6 +2272,7 @@ nsst_status nsst_denoise_tau_batch(nsst_plan* p, const float* const* x, float* c
   if (mode != NSST_THRESH_HARD && mode != NSST_THRESH_SOFT) return fail(NSST_ERR_INVALID_ARG, "bad mode");
   for (int i = 0; i < n; i++)
     if (!x[i] || !out[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  NSST_TRY(check_spectral_n(p, n, x, out));
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = (cudaStream_t)stream;
   timer_begin(p, st);
@@ -2429,6 +2454,7 @@ nsst_status nsst_denoise_tau_backward(nsst_plan* p, const float* const* x, const
   if (!x) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
   for (int i = 0; i < n; i++)
     if (!x[i]) return fail(NSST_ERR_INVALID_ARG, "NULL image pointer");
+  NSST_TRY(check_spectral_n(p, n, x, nullptr));
   std::lock_guard<std::mutex> lk(p->mu);
   p->saved_n = 0;  // step 1 rewrites the arena's band spectra
   return tau_backward(p, x, grad_out, grad_x, n, tau, grad_tau, accumulate_tau, mode, (cudaStream_t)stream);
@@ -2737,6 +2763,7 @@ nsst_status nsst_separate(nsst_plan* p, const float* img, int n, int level2, int
                           double gamma, const double* coeff, int ncoeff, float* C, float* P,
                           nsst_separate_info* info, void* stream) {
   if (!p || !img || !coeff || !C || !P) return fail(NSST_ERR_INVALID_ARG, "NULL argument");
+  NSST_TRY(check_spectral(p, {img}));
   if (n < 1 || n > p->B) return fail(NSST_ERR_INVALID_ARG, "image count outside [1, batch capacity]");
   if (itermax < 1) return fail(NSST_ERR_INVALID_ARG, "itermax must be >= 1");
   if (!std::isfinite(stop) || stop <= 0) return fail(NSST_ERR_INVALID_ARG, "stop must be finite and > 0");

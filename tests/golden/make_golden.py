@@ -2,7 +2,8 @@
 
 Run in the container that holds the read-only reference checkout:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference DIR]
+(default: $SHEARCUDA_REFERENCE, else ``reference`` beside the repository)
 
 It writes two kinds of fixtures, both small enough to commit:
 
@@ -174,7 +175,9 @@ def rwt_cases(seed=4321):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default='/root/reference')
+    sys.path.insert(0, ROOT)
+    from oracle.build_oracle import default_reference
+    ap.add_argument('--reference', default=default_reference())
     args = ap.parse_args()
     tables = filter_tables(args.reference)
     with open(os.path.join(HERE, 'pyramid_filter_tables.json'), 'w') as f:

@@ -136,15 +136,21 @@ def test_spectral_thresholded_lowpass(built_lib, cuda, HW):
 def test_direct_fallbacks(built_lib, cuda):
     import shearcuda_gb300 as sc
     H, W = 256, 256
-    ps = _plan(H, W, sc.PYRAMID_SPECTRAL)
+    pa = _plan(H, W, sc.PYRAMID_AUTO)
     x = _img(H, W, 5, cuda)
-    # an image 4 bytes off a 16-byte boundary takes the direct pyramid
+    # under NSST_PYRAMID_AUTO an image 4 bytes off a 16-byte boundary takes the direct pyramid
     buf = torch.zeros(H * W + 1, device=cuda)
     buf[1:] = x.reshape(-1)
     xm = buf[1:].view(H, W)
-    a = sc.nsst_denoise(xm, ps, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
-    b = sc.nsst_denoise(x, ps, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    a = sc.nsst_denoise(xm, pa, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
+    b = sc.nsst_denoise(x, pa, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT).cpu().numpy()
     assert rel_l2(a, b) <= 1e-5
+    # NSST_PYRAMID_SPECTRAL refuses it rather than switching silently
+    ps = _plan(H, W, sc.PYRAMID_SPECTRAL)
+    with pytest.raises(sc.NsstError):
+        sc.nsst_denoise(xm, ps, 20.0, K_DEMO, None, mode=sc.THRESH_SOFT)
+    with pytest.raises(sc.NsstError):
+        sc.shear_trans_cuda(xm, 'maxflat', ps)
 
 
 def test_pyramid_modes(built_lib, cuda):
@@ -178,15 +184,18 @@ def test_spectral_shear_trans_and_inverse(built_lib, cuda, HW):
     rd = sc.inverse_shear_cuda(cs, 'maxflat', pd)
     assert rel_l2(rs.cpu().numpy(), rd.cpu().numpy()) <= 1e-5
     assert rel_l2(rs.cpu().numpy(), x.cpu().numpy()) <= 1e-5
-    # an output 4 bytes off a 16-byte boundary takes the direct pyramid
+    # under NSST_PYRAMID_AUTO an output 4 bytes off a 16-byte boundary takes the
+    # direct pyramid; NSST_PYRAMID_SPECTRAL refuses it
+    from shearcuda_gb300 import _lib
     buf = torch.zeros(H * W + 1, device=cuda)
-    ps.enable_timers(True)
+    assert _lib.lib().nsst_inverse_shear(ps.handle, cs.data_ptr(), buf.data_ptr() + 4, None) == 1
+    pa = _plan(H, W, sc.PYRAMID_AUTO)
+    pa.enable_timers(True)
     try:
-        from shearcuda_gb300 import _lib
-        _lib.check(_lib.lib().nsst_inverse_shear(ps.handle, cs.data_ptr(), buf.data_ptr() + 4, None))
-        assert 'dct_lowpass' not in [n for n, _ in ps.read_timers(40)]
+        _lib.check(_lib.lib().nsst_inverse_shear(pa.handle, cs.data_ptr(), buf.data_ptr() + 4, None))
+        assert 'dct_lowpass' not in [n for n, _ in pa.read_timers(40)]
     finally:
-        ps.enable_timers(False)
+        pa.enable_timers(False)
     torch.cuda.synchronize()
     assert rel_l2(buf[1:].view(H, W).cpu().numpy(), rd.cpu().numpy()) <= 1e-5
 
@@ -235,3 +244,4 @@ def test_spectral_atrousdec_atrousrec(built_lib, cuda):
     rs, rd = sc.atrousrec(ys2, ps), sc.atrousrec(ys2, pd)
     assert rel_l2(rs.cpu().numpy(), rd.cpu().numpy()) <= 1e-5
     assert rel_l2(sc.atrousrec(ys, ps).cpu().numpy(), x.cpu().numpy()) <= 1e-5
+

@@ -107,3 +107,16 @@ def test_status_codes_without_gpu(built_lib):
         sc.ShearPlan([3, 3], [32, 32], 256, 256, pyramid=3)
     assert e.value.status == 1 and 'pyramid mode' in str(e.value)
     assert (sc.PYRAMID_AUTO, sc.PYRAMID_DIRECT, sc.PYRAMID_SPECTRAL) == (0, 1, 2)
+
+
+def test_noalloc_rejects_overlapping_buffers_before_any_device_call(built_lib):
+    # host-side argument checks: no GPU is touched (fake device addresses)
+    import ctypes
+    from shearcuda_gb300._lib import lib
+    H, W, L = 256, 256, 4
+    plane = H * W * 4
+    y = 1 << 32
+    for x in (y, y + plane, y + L * plane, y - plane + 4):  # inside y or straddling its start
+        st = lib().nsst_atrousdec_noalloc(ctypes.c_void_p(x), ctypes.c_void_p(y), H, W, L, b'maxflat', None)
+        assert st == 1, x
+        assert b'overlaps' in lib().nsst_last_error()

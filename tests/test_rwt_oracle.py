@@ -12,7 +12,9 @@ import pytest
 from oracle import rwt
 
 GOLD = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'rwt_ref_cases.npz'))
-REFERENCE = '/root/reference'
+from oracle.build_oracle import default_reference  # noqa: E402
+
+REFERENCE = default_reference()
 
 
 @pytest.mark.parametrize('i', range(int(GOLD['n'][0])))
