@@ -38,7 +38,7 @@ class NsstSeparateInfo(ctypes.Structure):
                 ('buff_wavelet', ctypes.c_double), ('deltamax', ctypes.c_double), ('lam', ctypes.c_double)]
 
 
-TUNE_MAX_CANDIDATES = 8
+TUNE_MAX_CANDIDATES = 16
 
 
 class NsstTuneResult(ctypes.Structure):

@@ -87,6 +87,77 @@ __device__ __forceinline__ float4 rot8_3(float4 o, float r) {
   return pk4(rot8_3<DIR>(lo2(o), r), rot8_3<DIR>(hi2(o), r));
 }
 
+// Two complex values of two sequences at one index in split form: the real
+// parts in one register pair, the imaginary parts in another.  Every complex
+// operation on the pair is then packed FP32x2 arithmetic (a twiddle multiply
+// of both values is two FMUL2 and two FFMA2 instead of eight scalar
+// instructions), and a thread's index arithmetic serves two sequences.  Each
+// packed lane rounds exactly like the scalar operation it replaces.
+struct cpx2 {
+  float2 re, im;
+};
+__device__ __forceinline__ float2 bcast(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ cpx2 cadd(cpx2 a, cpx2 b) { return {cadd(a.re, b.re), cadd(a.im, b.im)}; }
+__device__ __forceinline__ cpx2 csub(cpx2 a, cpx2 b) { return {csub(a.re, b.re), csub(a.im, b.im)}; }
+__device__ __forceinline__ cpx2 cconj(cpx2 a) { return {a.re, neg2(a.im)}; }
+__device__ __forceinline__ cpx2 cscale(cpx2 a, float s) { return {__fmul2_rn(a.re, bcast(s)), __fmul2_rn(a.im, bcast(s))}; }
+// a * t for a twiddle given as its broadcast pairs (t.x, t.x), (t.y, t.y)
+__device__ __forceinline__ cpx2 cmul_b(cpx2 a, float2 tx, float2 ty) {
+  return {__ffma2_rn(a.re, tx, neg2(__fmul2_rn(a.im, ty))), __ffma2_rn(a.im, tx, __fmul2_rn(a.re, ty))};
+}
+// a * conj(t)
+__device__ __forceinline__ cpx2 cmulc_b(cpx2 a, float2 tx, float2 ty) {
+  return {__ffma2_rn(a.re, tx, __fmul2_rn(a.im, ty)), __ffma2_rn(a.im, tx, neg2(__fmul2_rn(a.re, ty)))};
+}
+__device__ __forceinline__ cpx2 cmul(cpx2 a, float2 t) { return cmul_b(a, bcast(t.x), bcast(t.y)); }
+__device__ __forceinline__ cpx2 cmulc(cpx2 a, float2 t) { return cmulc_b(a, bcast(t.x), bcast(t.y)); }
+template <int DIR>
+__device__ __forceinline__ cpx2 mul_i(cpx2 a) {
+  return DIR < 0 ? cpx2{a.im, neg2(a.re)} : cpx2{neg2(a.im), a.re};
+}
+__device__ __forceinline__ cpx2 caxc(cpx2 a, float c, cpx2 t) {
+  return {__ffma2_rn(t.re, bcast(c), a.re), __ffma2_rn(t.im, bcast(c), a.im)};
+}
+// a (c + i sg sn)
+__device__ __forceinline__ cpx2 crot(cpx2 a, float c, float sg, float sn) {
+  const float2 s2 = bcast(sg * sn);
+  return {__ffma2_rn(a.re, bcast(c), neg2(__fmul2_rn(a.im, s2))), __ffma2_rn(a.im, bcast(c), __fmul2_rn(a.re, s2))};
+}
+template <int DIR>
+__device__ __forceinline__ cpx2 rot8_1(cpx2 o, float r) {
+  return DIR < 0 ? cpx2{__fmul2_rn(cadd(o.re, o.im), bcast(r)), __fmul2_rn(csub(o.im, o.re), bcast(r))}
+                 : cpx2{__fmul2_rn(csub(o.re, o.im), bcast(r)), __fmul2_rn(cadd(o.im, o.re), bcast(r))};
+}
+template <int DIR>
+__device__ __forceinline__ cpx2 rot8_3(cpx2 o, float r) {
+  return DIR < 0 ? cpx2{__fmul2_rn(csub(o.im, o.re), bcast(r)), neg2(__fmul2_rn(cadd(o.im, o.re), bcast(r)))}
+                 : cpx2{neg2(__fmul2_rn(cadd(o.re, o.im), bcast(r))), __fmul2_rn(csub(o.re, o.im), bcast(r))};
+}
+// the two values of a pair as ordinary complex numbers, and back
+__device__ __forceinline__ float2 lane0(cpx2 a) { return make_float2(a.re.x, a.im.x); }
+__device__ __forceinline__ float2 lane1(cpx2 a) { return make_float2(a.re.y, a.im.y); }
+__device__ __forceinline__ cpx2 pair(float2 a, float2 b) { return {make_float2(a.x, b.x), make_float2(a.y, b.y)}; }
+
+// Twiddle multiply inside a pass: for cpx2 elements the table holds each
+// twiddle as its broadcast pairs (t.x, t.x, t.y, t.y) in one 16-byte entry.
+template <int DIR>
+__device__ __forceinline__ float2 tw_mul(float2 v, const float2* __restrict__ tw, int idx) {
+  const float2 t = __ldg(&tw[idx]);
+  return DIR < 0 ? cmul(v, t) : cmulc(v, t);
+}
+template <int DIR>
+__device__ __forceinline__ float4 tw_mul(float4 v, const float2* __restrict__ tw, int idx) {
+  const float2 t = __ldg(&tw[idx]);
+  return DIR < 0 ? cmul(v, t) : cmulc(v, t);
+}
+template <int DIR>
+__device__ __forceinline__ cpx2 tw_mul(cpx2 v, const float2* __restrict__ tw, int idx) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(tw) + idx);
+  return DIR < 0 ? cmul_b(v, make_float2(t.x, t.y), make_float2(t.z, t.w))
+                 : cmulc_b(v, make_float2(t.x, t.y), make_float2(t.z, t.w));
+}
+
 // ---------------------------------------------------------------------------
 // R-point DFTs in registers.  DIR = -1 forward (exp(-2 pi i ...)), +1 inverse.
 // ---------------------------------------------------------------------------
@@ -589,10 +660,7 @@ __device__ __forceinline__ void stockham_ip(const Rd& rd, const Wr& wr, const fl
       const int k = j % NS;
       if (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; r++) {
-          const float2 t = __ldg(&tw[r * k * STEP]);
-          v[it][r] = DIR < 0 ? cmul(v[it][r], t) : cmulc(v[it][r], t);
-        }
+        for (int r = 1; r < R; r++) v[it][r] = tw_mul<DIR>(v[it][r], tw, r * k * STEP);
       }
       Dft<R, DIR>::run(v[it]);
     }

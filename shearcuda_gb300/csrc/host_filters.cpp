@@ -297,6 +297,12 @@ std::vector<float2> twiddle_table(int n) {
   return t;
 }
 
+std::vector<float4> broadcast_table(const std::vector<float2>& tab) {
+  std::vector<float4> t(tab.size());
+  for (size_t i = 0; i < tab.size(); i++) t[i] = make_float4(tab[i].x, tab[i].x, tab[i].y, tab[i].y);
+  return t;
+}
+
 std::vector<float2> half_twiddle_table(int n) {
   std::vector<float2> t(n / 2);
   for (int i = 0; i < n / 2; i++) {

@@ -121,10 +121,14 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
                         void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
                         cudaStream_t st);
 // The band row pass (RowOp::Thresh) with tile_mult (1 or 2) times the rows of
-// RowCfg's tile per CTA.
+// RowCfg's tile per CTA; packed: on split-complex row pairs, with the row
+// twiddle tables twWh4 / twW4 (W/2 entries each) in broadcast form.
 cudaError_t launch_rows_thresh(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                                void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
-                               int tile_mult, cudaStream_t st);
+                               int tile_mult, cudaStream_t st, bool packed = false, const float4* twWh4 = nullptr,
+                               const float4* twW4 = nullptr);
+// twiddle table in broadcast form: entry t = (c.x, c.x, c.y, c.y) of tab[t]
+std::vector<float4> broadcast_table(const std::vector<float2>& tab);
 cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, int H, int W, const float2* src_base,
                         float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                         cudaStream_t st);

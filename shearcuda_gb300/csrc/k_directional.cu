@@ -137,6 +137,97 @@ __global__ void __launch_bounds__(RowTile<WH, RS>::T, RowTile<WH, RS>::MINB)
   r2c_post_store_rm<WH, RS, T>(dst_base + job.dst + off, A, twW);
 }
 
+// The band row pass on split-complex pairs (cpx2): rows 2p and 2p + 1 of the
+// tile share a thread's registers, so the twiddle multiplies, the packed-real
+// pre- and post-processing and the index arithmetic serve two rows at once as
+// FP32x2 instructions.  Same operations per value as k_rows_thresh.  twWh4 /
+// twW4: the row twiddle tables with each entry as its broadcast pairs.
+// Radix plans of the paired row transforms: FftPlan's, up to 128 registers
+// (sixteen pairs in a radix-16 pass).  A 256-point 8 x 8 x 4 plan at 64
+// registers (32 warps per SM) measured slower than radix 16 x 16 at 128
+// (4.71 against 4.44 ms for the directional stage of 64 x 512^2).
+template <int WH>
+struct RowPlanP {
+  using type = typename FftPlan<WH>::type;
+  static constexpr int R0 = 16;  // largest radix: butterflies per pass = WH / R0 per sequence
+  static constexpr int MAXREG = 128;
+};
+template <int WH, int RS>
+struct RowTileP {
+  static constexpr int NP = RS / 2;  // row pairs
+  static constexpr int T0 = WH / RowPlanP<WH>::R0 * NP;
+  static constexpr int T = T0 < 64 ? 64 : T0;
+  static constexpr int MINB = 65536 / RowPlanP<WH>::MAXREG / T > 0 ? 65536 / RowPlanP<WH>::MAXREG / T : 1;
+  static constexpr size_t smem() { return (size_t)RS * (WH + 2) * sizeof(float2); }
+  static_assert(RS % 2 == 0 && T % 32 == 0, "row pairs, whole warps");
+};
+template <int WH, int RS>
+__global__ void __launch_bounds__(RowTileP<WH, RS>::T, RowTileP<WH, RS>::MINB)
+    k_rows_thresh_p(const RowJob* __restrict__ jobs, int n_active, const float2* src_base, float2* dst_base,
+                    const float2* __restrict__ twWh4, const float4* __restrict__ twW4, const float* __restrict__ thr,
+                    int mode) {
+  constexpr int NP = RowTileP<WH, RS>::NP, T = RowTileP<WH, RS>::T, RP = WH + 2;
+  extern __shared__ float2 smem[];
+  float2* A = smem;                         // row-major rows, pitch WH + 2
+  cpx2* D = reinterpret_cast<cpx2*>(smem);  // dense [index][pair] between passes
+  const RowJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const float th = thr[job.th_index];
+  const size_t off = (size_t)blockIdx.x * RS * WH;
+  fetch_rows_rm<WH, RS, T>(A, src_base + job.src + off);
+  cp_async_wait_all();
+  __syncthreads();
+  // C2R, pre-processing (see c2r_pre) in the first pass's loads:
+  // Z[k] = E + iO, E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k
+  auto ld = [&](int k, int p) -> cpx2 {
+    const float2* r0 = A + 2 * p * RP;
+    const cpx2 xk = pair(r0[k], r0[RP + k]);
+    if (k == 0) return {cadd(xk.re, xk.im), csub(xk.re, xk.im)};
+    const cpx2 xmc = cconj(pair(r0[WH - k], r0[RP + WH - k]));
+    const cpx2 E = cadd(xk, xmc);
+    const float4 t = __ldg(&twW4[k]);
+    const cpx2 O = cmulc_b(csub(xk, xmc), make_float2(t.x, t.y), make_float2(t.z, t.w));
+    return {csub(E.re, O.im), cadd(E.im, O.re)};
+  };
+  auto thr_st = [&](int i, int p, cpx2 v) {
+    v.re.x = apply_thresh(v.re.x, th, mode);
+    v.re.y = apply_thresh(v.re.y, th, mode);
+    v.im.x = apply_thresh(v.im.x, th, mode);
+    v.im.y = apply_thresh(v.im.y, th, mode);
+    D[i * NP + p] = v;
+  };
+  using Plan = typename RowPlanP<WH>::type;
+  block_fft_hook_ip_plan<WH, NP, T, +1, Plan>(D, twWh4, ld, thr_st);
+  // R2C of the thresholded rows, the last pass back to the row-major layout
+  auto ldd = [&](int i, int p) -> cpx2 { return D[i * NP + p]; };
+  auto st_rm = [&](int i, int p, cpx2 v) {
+    A[2 * p * RP + i] = lane0(v);
+    A[(2 * p + 1) * RP + i] = lane1(v);
+  };
+  block_fft_hook_ip_plan<WH, NP, T, -1, Plan>(D, twWh4, ldd, st_rm);
+  // post-processing (see r2c_post) fused with the store along the rows:
+  // X[k] = E + w^k O, E = (Z[k] + conj(Z[WH-k]))/2, O = (Z[k] - conj(Z[WH-k]))/(2i)
+  float2* dst = dst_base + job.dst + off;
+#pragma unroll 2
+  for (int e = threadIdx.x; e < WH * NP; e += T) {
+    const int k = e % WH, p = e / WH;
+    const float2* r0 = A + 2 * p * RP;
+    const cpx2 zk = pair(r0[k], r0[RP + k]);
+    cpx2 out;
+    if (k == 0) {
+      out = {cadd(zk.re, zk.im), csub(zk.re, zk.im)};
+    } else {
+      const cpx2 zmc = cconj(pair(r0[WH - k], r0[RP + WH - k]));
+      const cpx2 E = cscale(cadd(zk, zmc), 0.5f);
+      const cpx2 d = cscale(csub(zk, zmc), 0.5f);
+      const float4 t = __ldg(&twW4[k]);
+      out = cadd(E, cmul_b(cpx2{d.im, neg2(d.re)}, make_float2(t.x, t.y), make_float2(t.z, t.w)));
+    }
+    dst[(size_t)(2 * p) * WH + k] = lane0(out);
+    dst[(size_t)(2 * p + 1) * WH + k] = lane1(out);
+  }
+}
+
 // Band maxima (thresh.m's opt == 1 maximum with a zero threshold): C2R of the
 // CTA's rows of one band, then max |c| over them into bits[job.th_index] as
 // the bit pattern of a non-negative float (atomicMax; bits zeroed first).
@@ -444,6 +535,8 @@ cudaError_t prepare_row_kernels(int wh) {
     if (e == cudaSuccess) e = opt_in(k_rows_inv<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n>, sm);                   \
     if (e == cudaSuccess) e = opt_in(k_rows_thresh<n, 2 * RowCfg<n>::RS>, RowTile<n, 2 * RowCfg<n>::RS>::smem()); \
+    if (e == cudaSuccess) e = opt_in(k_rows_thresh_p<n, RowCfg<n>::RS>, RowTileP<n, RowCfg<n>::RS>::smem()); \
+    if (e == cudaSuccess) e = opt_in(k_rows_thresh_p<n, 2 * RowCfg<n>::RS>, RowTileP<n, 2 * RowCfg<n>::RS>::smem()); \
     if (e == cudaSuccess) e = opt_in(k_rows_max<n>, sm);                      \
     if (e == cudaSuccess) e = opt_in(k_rows_backward<n>, 3 * RowCfg<n>::smem_rm()); \
     return e;                                                                 \
@@ -507,15 +600,42 @@ cudaError_t launch_rows(RowOp op, const RowJob* jobs, int njobs, int n_active, i
 
 cudaError_t launch_rows_thresh(const RowJob* jobs, int njobs, int n_active, int H, int W, const void* src_base,
                                void* dst_base, const float2* twWh, const float2* twW, const float* thr, int mode,
-                               int tile_mult, cudaStream_t st) {
-  if (tile_mult == 1)
+                               int tile_mult, cudaStream_t st, bool packed, const float4* twWh4,
+                               const float4* twW4) {
+  if (tile_mult == 1 && !packed)
     return launch_rows(RowOp::Thresh, jobs, njobs, n_active, H, W, src_base, dst_base, twWh, twW, thr, mode, st);
-  if (tile_mult != 2) return cudaErrorInvalidValue;
+  if (tile_mult != 1 && tile_mult != 2) return cudaErrorInvalidValue;
   const int WH = W / 2;
   if (njobs == 0) return cudaSuccess;
-  count_launch();
   const float2* sb = static_cast<const float2*>(src_base);
   float2* db = static_cast<float2*>(dst_base);
+  if (packed) {
+    if (!twWh4 || !twW4) return cudaErrorInvalidValue;
+    switch (WH) {
+#define CASE(n)                                                                                            \
+  case n: {                                                                                                \
+    constexpr int R1 = RowCfg<n>::RS, R2 = 2 * RowCfg<n>::RS;                                              \
+    if (tile_mult == 1) {                                                                                  \
+      using Tl = RowTileP<n, R1>;                                                                          \
+      count_launch();                                                                                      \
+      k_rows_thresh_p<n, R1><<<dim3(H / R1, njobs), Tl::T, Tl::smem(), st>>>(                              \
+          jobs, n_active, sb, db, reinterpret_cast<const float2*>(twWh4), twW4, thr, mode);                \
+    } else {                                                                                               \
+      if (H % R2 != 0) return cudaErrorInvalidValue;                                                       \
+      using Tl = RowTileP<n, R2>;                                                                          \
+      count_launch();                                                                                      \
+      k_rows_thresh_p<n, R2><<<dim3(H / R2, njobs), Tl::T, Tl::smem(), st>>>(                              \
+          jobs, n_active, sb, db, reinterpret_cast<const float2*>(twWh4), twW4, thr, mode);                \
+    }                                                                                                      \
+    return cudaGetLastError();                                                                             \
+  }
+      NSST_ROW_SIZES(CASE)
+#undef CASE
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+  count_launch();
   switch (WH) {
 #define CASE(n)                                                                                         \
   case n: {                                                                                             \

@@ -29,6 +29,7 @@ struct DirChoice {
   bool fused = false;
   int ana = 0;       // 0: by grid size, 1: per level, 2: per band
   int row_tile = 1;
+  bool packed = false;  // row pass on split-complex row pairs (FP32x2 arithmetic)
 };
 
 // autotuner buckets of the batch size n: bucket b holds 2^b <= n < 2^(b+1)
@@ -80,6 +81,7 @@ struct nsst_plan {
   float2* spec = nullptr;  // [ndir_total][H][WH] then the column-0 side arrays [ndir_total][H]
   size_t m0_off = 0;       // offset (float2) of the side arrays from spec
   float2 *twH = nullptr, *twWh = nullptr, *twW = nullptr;
+  float4 *twWh4 = nullptr, *twW4 = nullptr;  // twWh / twW with each entry as broadcast pairs
   // per-item work buffers (item i at base + i * stride)
   float* pyr = nullptr;    // (nlev+1) x H x W   analysis pyramid
   float* tmp = nullptr;    // 2 x H x W          lowpass ping-pong
@@ -435,6 +437,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_spec = take(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
   size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH),
          o_twW = take(sizeof(float2) * p->WH);
+  size_t o_twWh4 = take(sizeof(float4) * p->WH), o_twW4 = take(sizeof(float4) * p->WH);
   size_t o_pyr = take(sizeof(float) * p->s_pyr * NB);
   size_t o_tmp = take(sizeof(float) * p->s_tmp * NB);
   size_t o_lev = take(sizeof(float2) * p->s_lev * NB);
@@ -492,6 +495,8 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->twH = (float2*)(A + o_twH);
   p->twWh = (float2*)(A + o_twWh);
   p->twW = (float2*)(A + o_twW);
+  p->twWh4 = (float4*)(A + o_twWh4);
+  p->twW4 = (float4*)(A + o_twW4);
   p->pyr = (float*)(A + o_pyr);
   p->tmp = (float*)(A + o_tmp);
   p->lev = (float2*)(A + o_lev);
@@ -548,6 +553,10 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     ce = cudaMemcpy(p->twH, tH.data(), tH.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->twWh, tWh.data(), tWh.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->twW, tW.data(), tW.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    const auto bWh = broadcast_table(tWh), bW = broadcast_table(tW);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(p->twWh4, bWh.data(), bWh.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->twW4, bW.data(), bW.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) return destroy(cuda_fail(ce, "upload twiddles"));
   }
   // ---- static job lists (offsets in float2 units from the launch bases)
@@ -1029,7 +1038,7 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana));
   timer_mark(p, "band_analysis_cols", st);
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
-                               c.row_tile, st));
+                               c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
   NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A,
                         p->spec, (size_t)p->H * p->WH, p->twH, st));
@@ -1575,14 +1584,16 @@ std::vector<std::pair<DirChoice, std::string>> dir_candidates(const nsst_plan* p
   std::vector<std::pair<DirChoice, std::string>> c;
   const int rs = row_tile(p->WH);
   for (int ana : {1, 2})
-    for (int rt : {1, 2}) {
-      DirChoice d;
-      d.ana = ana;
-      d.row_tile = rt;
-      if (p->H % (rs * rt) != 0) continue;
-      c.push_back({d, std::string("split/") + (ana == 1 ? "level" : "band") + "-analysis/rows" +
-                          std::to_string(rs * rt)});
-    }
+    for (bool packed : {false, true})
+      for (int rt : {1, 2}) {
+        DirChoice d;
+        d.ana = ana;
+        d.row_tile = rt;
+        d.packed = packed;
+        if (p->H % (rs * rt) != 0) continue;
+        c.push_back({d, std::string("split/") + (ana == 1 ? "level" : "band") + "-analysis/rows" +
+                            std::to_string(rs * rt) + (packed ? "-pairs" : "")});
+      }
   if (p->fused_ok) {
     DirChoice d;
     d.fused = true;
