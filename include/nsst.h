@@ -140,9 +140,9 @@ int nsst_plan_directional(const nsst_plan* plan, int n);
 /* Autotuner.  Times every implementation of the directional stage this plan
  * can run on n synthetic images (median of 7 passes after 2 warm-ups, CUDA
  * events): the split kernels with each analysis variant (one CTA per band and
- * column group, or per level streaming all its bands), each row tile and each
- * row element form (one complex value per thread, or a split-complex pair of
- * rows whose arithmetic runs as FP32x2 instructions: "-pairs"), and
+ * column group, or per level streaming all its bands), row tiles, and one
+ * complex value per thread or split-complex pairs of rows or columns whose
+ * arithmetic runs as FP32x2 instructions ("-pairs"), and
  * the fused cluster kernel where the size has one; the fastest becomes the
  * choice of NSST_DIRECTIONAL_AUTO for batches in n's bucket (2^b <= n <
  * 2^(b+1)) and the captured graphs are dropped.  It also evaluates direct
@@ -164,8 +164,9 @@ typedef struct nsst_tune_result {
   int n;                                     /* batch size timed */
   int ncand;                                 /* candidates timed */
   int chosen;                                /* index of the fastest */
-  char name[NSST_TUNE_MAX_CANDIDATES][48];   /* e.g. "split/level-analysis/rows8", "split/level-analysis/rows16-pairs",
-                                                "fused/cluster16" */
+  char name[NSST_TUNE_MAX_CANDIDATES][48];   /* "split/<analysis>/<rows>/<synthesis>" (analysis: level, level-pairs
+                                                or band; rows: rows8, rows8-pairs, rows16-pairs; synthesis:
+                                                synthesis or synthesis-pairs) or "fused/cluster<C>" */
   float ms[NSST_TUNE_MAX_CANDIDATES];        /* median ms of one directional-stage pass over n images */
   int direct_support[NSST_MAX_LEVELS];       /* per level, px (0: no window below the image size) */
   double direct_err[NSST_MAX_LEVELS];        /* per level: the worst band's truncation error at that window */

@@ -107,7 +107,9 @@ inline void fill_taps(AtrousTaps<F>& t, const float* hflip) {
 inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
 
 enum class RowOp { Fwd, Inv, Thresh, Backward };
-enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis };  // AnalysisLevel: one job per level (all its bands)
+// AnalysisLevel: one job per level (all its bands); *Pairs: the same kernels on
+// split-complex column pairs, with twH pointing to the broadcast twiddle table
+enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis, AnalysisLevelPairs, SynthesisPairs };
 
 bool row_len_supported(int wh);
 bool col_len_supported(int h);

@@ -488,6 +488,140 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
 }
 
 // ---------------------------------------------------------------------------
+// The two column kernels above on split-complex column pairs (cpx2): columns
+// 2p and 2p + 1 of the CTA's group share a thread's registers, so the
+// spectrum products, twiddle multiplies and index arithmetic run as FP32x2
+// instructions for two columns, a thread holds half the butterflies of the
+// one-column form (the same registers), and global stores move 16 bytes.
+// The staging buffers keep the [row][column] float2 layout of global memory;
+// the transform buffers hold [row][pair] cpx2.  twH4: the column twiddle
+// table with each entry as its broadcast pairs.
+// ---------------------------------------------------------------------------
+// a * b and a * conj(b) for two independent products
+__device__ __forceinline__ cpx2 cmul_pp(cpx2 a, cpx2 b) {
+  return {__ffma2_rn(a.re, b.re, neg2(__fmul2_rn(a.im, b.im))), __ffma2_rn(a.re, b.im, __fmul2_rn(a.im, b.re))};
+}
+__device__ __forceinline__ cpx2 cmulc_pp(cpx2 a, cpx2 b) {
+  return {__ffma2_rn(a.re, b.re, __fmul2_rn(a.im, b.im)), __ffma2_rn(a.im, b.re, neg2(__fmul2_rn(a.re, b.im)))};
+}
+__device__ __forceinline__ cpx2 ld_pair(const float2* p) {  // two adjacent float2 (16-byte aligned)
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  return pair(make_float2(q.x, q.y), make_float2(q.z, q.w));
+}
+__device__ __forceinline__ void st_pair(float2* p, cpx2 v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.re.x, v.im.x, v.re.y, v.im.y);
+}
+
+template <int H>
+__global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
+    k_band_analysis_ml_p(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base,
+                         float2* dst_base, const float2* __restrict__ spec_base, size_t band_stride,
+                         const float2* __restrict__ twH4) {
+  using C = AnaCfg<H>;
+  constexpr int CS = C::CS, CH = CS / 2, NP = CS / 2;
+  extern __shared__ float2 smem[];
+  cpx2* A = reinterpret_cast<cpx2*>(smem);  // transform [row][pair], in place
+  float2* Y = smem + H * CS;                // level spectrum column group [row][column]
+  float2* Wb = Y + H * CS;                  // staged filter spectrum of the current band
+  const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const int col0 = blockIdx.x * CS;
+  const bool dc = col0 == 0;
+  auto stage = [&](float2* dst, const float2* src) {
+    for (int e = threadIdx.x; e < H * CH; e += C::T) {
+      const int i = e / CH, c = e - (e / CH) * CH;
+      cp_async16(dst + i * CS + 2 * c, src + (size_t)i * WH + 2 * c);
+    }
+  };
+  stage(Y, src_base + job.src + col0);
+  stage(Wb, spec_base + job.spec + col0);
+  cp_async_commit();
+  for (int k = 0; k < job.nbands; k++) {
+    cp_async_wait_all();
+    __syncthreads();
+    const float2* m0 = spec_base + job.m0 + (size_t)k * H;
+    // Wk .* Y for two columns, the packed DC/Nyquist column's M term on lane 0 of pair 0
+    auto ld = [&](int i, int p) -> cpx2 {
+      cpx2 r = cmul_pp(ld_pair(Wb + i * CS + 2 * p), ld_pair(Y + i * CS + 2 * p));
+      if (dc && p == 0) {
+        const float2 a = cmul(__ldg(&m0[i]), cconj(Y[((H - i) % H) * CS]));
+        r.re.x += a.x;
+        r.im.x += a.y;
+      }
+      return r;
+    };
+    auto next = [&]() {
+      if (k + 1 < job.nbands) {
+        stage(Wb, spec_base + job.spec + (size_t)(k + 1) * band_stride + col0);
+        cp_async_commit();
+      }
+    };
+    float2* dst = dst_base + job.dst + (size_t)k * band_stride + col0;
+    auto st = [&](int i, int p, cpx2 v) { st_pair(dst + (size_t)i * WH + 2 * p, v); };
+    block_fft_hook_ip<H, NP, C::T, +1>(A, twH4, ld, st, next);
+  }
+}
+
+template <int H>
+__global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
+    k_band_synthesis_p(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base,
+                       float2* dst_base, const float2* __restrict__ spec_base, size_t band_stride,
+                       const float2* __restrict__ twH4) {
+  using C = SynCfg<H>;
+  constexpr int CS = C::CS, NP = CS / 2;
+  extern __shared__ float2 smem[];
+  cpx2* A = reinterpret_cast<cpx2*>(smem);                  // transform [row][pair]
+  cpx2* S = reinterpret_cast<cpx2*>(smem + (size_t)H * CS);  // running band sum [row][pair]
+  float2* D = smem + 2 * (size_t)H * CS;                     // column 0 of the band's transform
+  float2* P = D + H;                                         // staging: the band's column group [row][column]
+  const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const int col0 = blockIdx.x * CS;
+  const bool dc = col0 == 0;
+  auto prefetch = [&](int k) {
+    constexpr int CH = CS / 2;
+    const float2* src = src_base + job.src + (size_t)k * band_stride + col0;
+    for (int e = threadIdx.x; e < H * CH; e += C::T) {
+      const int i = e / CH, c = e - (e / CH) * CH;
+      cp_async16(P + i * CS + 2 * c, src + (size_t)i * WH + 2 * c);
+    }
+    cp_async_commit();
+  };
+  prefetch(0);
+  for (int k = 0; k < job.nbands; k++) {
+    const float2* spec = spec_base + job.spec + k * band_stride + col0;
+    const bool first = k == 0;
+    auto acc_st = [&](int i, int p, cpx2 z) {
+      const float4 w = __ldg(reinterpret_cast<const float4*>(spec + (size_t)i * WH + 2 * p));
+      const cpx2 q = cmulc_pp(z, pair(make_float2(w.x, w.y), make_float2(w.z, w.w)));
+      cpx2* t = &S[i * NP + p];
+      *t = first ? q : cadd(*t, q);
+      if (dc && p == 0) D[i] = lane0(z);
+    };
+    cp_async_wait_all();
+    __syncthreads();
+    auto next = [&]() {
+      if (k + 1 < job.nbands) prefetch(k + 1);
+    };
+    auto ldp = [&](int i, int p) -> cpx2 { return ld_pair(P + i * CS + 2 * p); };
+    block_fft_hook_ip<H, NP, C::T, -1>(A, twH4, ldp, acc_st, next);
+    if (dc) {
+      for (int i = threadIdx.x; i < H; i += C::T) {
+        const float2 m = __ldg(&spec_base[job.m0 + (size_t)k * H + i]);
+        const float2 a = cconj(cmul(m, D[(H - i) % H]));  // conj(M) conj(z[-u])
+        S[i * NP].re.x += a.x;
+        S[i * NP].im.x += a.y;
+      }
+      __syncthreads();
+    }
+  }
+  float2* dst = dst_base + job.dst + col0;
+  block_fft_hook_ip<H, NP, C::T, +1>(
+      S, twH4, [&](int i, int p) -> cpx2 { return S[i * NP + p]; },
+      [&](int i, int p, cpx2 v) { st_pair(dst + (size_t)i * WH + 2 * p, v); });
+}
+
+// ---------------------------------------------------------------------------
 // Host-side launchers, dispatched on the (compile-time) transform lengths.
 // The dynamic shared-memory opt-in is done once per device and kernel by the
 // prepare_* calls (plan creation), never on the launch path.
@@ -558,6 +692,8 @@ cudaError_t prepare_col_kernels(int h) {
     if (e == cudaSuccess) e = opt_in(k_band_analysis<n>, sm);                 \
     if (e == cudaSuccess) e = opt_in(k_band_analysis_ml<n>, AnaCfg<n>::smem()); \
     if (e == cudaSuccess) e = opt_in(k_band_synthesis<n>, SynCfg<n>::smem());  \
+    if (e == cudaSuccess) e = opt_in(k_band_analysis_ml_p<n>, AnaCfg<n>::smem()); \
+    if (e == cudaSuccess) e = opt_in(k_band_synthesis_p<n>, SynCfg<n>::smem());  \
     return e;                                                                 \
   }
     NSST_COL_SIZES(CASE)
@@ -715,6 +851,12 @@ cudaError_t launch_cols(ColOp op, const ColJob* jobs, int njobs, int n_active, i
     else if (op == ColOp::Analysis)                                                                   \
       k_band_analysis<n><<<grid, ColCfg<n>::T, sm / 2, st>>>(jobs, n_active, WH, src_base, dst_base, spec_base,     \
                                                          twH);                                        \
+    else if (op == ColOp::AnalysisLevelPairs)                                                         \
+      k_band_analysis_ml_p<n><<<grid, AnaCfg<n>::T, AnaCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base,          \
+                                                                          dst_base, spec_base, band_stride, twH); \
+    else if (op == ColOp::SynthesisPairs)                                                             \
+      k_band_synthesis_p<n><<<grid, SynCfg<n>::T, SynCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base, dst_base, \
+                                                                        spec_base, band_stride, twH); \
     else if (op == ColOp::AnalysisLevel)                                                              \
       k_band_analysis_ml<n><<<grid, AnaCfg<n>::T, AnaCfg<n>::smem(), st>>>(jobs, n_active, WH, src_base, dst_base, \
                                                                         spec_base, band_stride, twH); \

@@ -30,6 +30,7 @@ struct DirChoice {
   int ana = 0;       // 0: by grid size, 1: per level, 2: per band
   int row_tile = 1;
   bool packed = false;  // row pass on split-complex row pairs (FP32x2 arithmetic)
+  bool cols_packed = false;  // analysis (per level) and synthesis on split-complex column pairs
 };
 
 // autotuner buckets of the batch size n: bucket b holds 2^b <= n < 2^(b+1)
@@ -81,7 +82,7 @@ struct nsst_plan {
   float2* spec = nullptr;  // [ndir_total][H][WH] then the column-0 side arrays [ndir_total][H]
   size_t m0_off = 0;       // offset (float2) of the side arrays from spec
   float2 *twH = nullptr, *twWh = nullptr, *twW = nullptr;
-  float4 *twWh4 = nullptr, *twW4 = nullptr;  // twWh / twW with each entry as broadcast pairs
+  float4 *twWh4 = nullptr, *twW4 = nullptr, *twH4 = nullptr;  // twWh / twW / twH with each entry as broadcast pairs
   // per-item work buffers (item i at base + i * stride)
   float* pyr = nullptr;    // (nlev+1) x H x W   analysis pyramid
   float* tmp = nullptr;    // 2 x H x W          lowpass ping-pong
@@ -437,7 +438,8 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   size_t o_spec = take(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
   size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH),
          o_twW = take(sizeof(float2) * p->WH);
-  size_t o_twWh4 = take(sizeof(float4) * p->WH), o_twW4 = take(sizeof(float4) * p->WH);
+  size_t o_twWh4 = take(sizeof(float4) * p->WH), o_twW4 = take(sizeof(float4) * p->WH),
+         o_twH4 = take(sizeof(float4) * H);
   size_t o_pyr = take(sizeof(float) * p->s_pyr * NB);
   size_t o_tmp = take(sizeof(float) * p->s_tmp * NB);
   size_t o_lev = take(sizeof(float2) * p->s_lev * NB);
@@ -497,6 +499,7 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
   p->twW = (float2*)(A + o_twW);
   p->twWh4 = (float4*)(A + o_twWh4);
   p->twW4 = (float4*)(A + o_twW4);
+  p->twH4 = (float4*)(A + o_twH4);
   p->pyr = (float*)(A + o_pyr);
   p->tmp = (float*)(A + o_tmp);
   p->lev = (float2*)(A + o_lev);
@@ -553,7 +556,8 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     ce = cudaMemcpy(p->twH, tH.data(), tH.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->twWh, tWh.data(), tWh.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->twW, tW.data(), tW.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    const auto bWh = broadcast_table(tWh), bW = broadcast_table(tW);
+    const auto bWh = broadcast_table(tWh), bW = broadcast_table(tW), bH = broadcast_table(tH);
+    if (ce == cudaSuccess) ce = cudaMemcpy(p->twH4, bH.data(), bH.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess)
       ce = cudaMemcpy(p->twWh4, bWh.data(), bWh.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(p->twW4, bW.data(), bW.size() * sizeof(float4), cudaMemcpyHostToDevice);
@@ -1009,9 +1013,14 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 // group streams all bands of the level when that grid fills the GPU once (two
 // CTAs per SM); smaller batches (a single image) keep one CTA per (band,
 // item) column group, which has ndir times more CTAs.
-nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0) {
+nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0, bool pairs = false) {
   float2* base = (float2*)(grad ? p->garena : p->arena);
   const size_t ctas = (size_t)n * p->nlev * (p->WH / 8);
+  if (pairs && ana == 1) {
+    NSST_CUDA(launch_cols(ColOp::AnalysisLevelPairs, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
+                          p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, (const float2*)p->twH4, st));
+    return NSST_OK;
+  }
   if (ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count)) {
     NSST_CUDA(launch_cols(ColOp::AnalysisLevel, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
                           p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, p->twH, st));
@@ -1035,13 +1044,14 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
     return NSST_OK;
   }
   char* A = p->arena;
-  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana));
+  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana, c.cols_packed));
   timer_mark(p, "band_analysis_cols", st);
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
-  NSST_CUDA(launch_cols(ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A,
-                        p->spec, (size_t)p->H * p->WH, p->twH, st));
+  NSST_CUDA(launch_cols(c.cols_packed ? ColOp::SynthesisPairs : ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, n,
+                        p->H, p->W, (float2*)A, (float2*)A, p->spec, (size_t)p->H * p->WH,
+                        c.cols_packed ? (const float2*)p->twH4 : p->twH, st));
   timer_mark(p, "band_synthesis_cols", st);
   return NSST_OK;
 }
@@ -1583,16 +1593,22 @@ namespace {
 std::vector<std::pair<DirChoice, std::string>> dir_candidates(const nsst_plan* p) {
   std::vector<std::pair<DirChoice, std::string>> c;
   const int rs = row_tile(p->WH);
+  // row pass: RowCfg's tile with one complex value per thread, or 1 or 2
+  // tiles of split-complex row pairs; columns: one value or column pairs
+  // (the pairs' analysis streams all bands of a level per CTA)
+  const int rows[3][2] = {{1, 0}, {1, 1}, {2, 1}};
   for (int ana : {1, 2})
-    for (bool packed : {false, true})
-      for (int rt : {1, 2}) {
+    for (bool cp : {false, true})
+      for (const auto& r : rows) {
         DirChoice d;
         d.ana = ana;
-        d.row_tile = rt;
-        d.packed = packed;
-        if (p->H % (rs * rt) != 0) continue;
-        c.push_back({d, std::string("split/") + (ana == 1 ? "level" : "band") + "-analysis/rows" +
-                            std::to_string(rs * rt) + (packed ? "-pairs" : "")});
+        d.row_tile = r[0];
+        d.packed = r[1] != 0;
+        d.cols_packed = cp;
+        if (p->H % (rs * r[0]) != 0) continue;
+        c.push_back({d, std::string("split/") + (ana == 1 ? (cp ? "level-pairs" : "level") : "band") + "/rows" +
+                            std::to_string(rs * r[0]) + (d.packed ? "-pairs" : "") +
+                            (cp ? "/synthesis-pairs" : "/synthesis")});
       }
   if (p->fused_ok) {
     DirChoice d;
