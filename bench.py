@@ -389,8 +389,26 @@ def volume_bench(sc, torch, dev, stream, flush, rank, reps=3, sizes=(128, 192), 
             res[name] = tt / reps
         res['volumes_per_s'] = batch / (res['forward_ms'] / 1000.0)
         res['ratio'] = res['forward_adjoint_ms'] / res['forward_ms']
-        out['b%dx%d' % (batch, n)] = res
         p.close()
+        # the same forward on the reference's padding (MarshalData.m: 128 -> 132, 192 -> 204)
+        pm = sc.VolumePlan(n, n, n, num_dirs=sc.V3_NUM_DIRS, batch=batch, grid='marshal')
+        sc.nsst_scalars3(pm, seed=9)
+        for _ in range(2):
+            sc.denoise3(xb, pm, 30.0, sc.DEMO_T, out=ob)
+        torch.cuda.synchronize()
+        tt = 0.0
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sc.denoise3(xb, pm, 30.0, sc.DEMO_T, out=ob)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tt += e0.elapsed_time(e1)
+        res['marshal_grid'] = {'grid': pm.grid[0], 'forward_ms': tt / reps,
+                               'volumes_per_s': batch / (tt / reps / 1000.0)}
+        pm.close()
+        out['b%dx%d' % (batch, n)] = res
         del xb, ob, gy, gx
     return out
 

@@ -485,10 +485,24 @@ void nsst_debug_fail_next_alloc(int n);
  * ------------------------------------------------------------------------ */
 typedef struct nsst3_plan nsst3_plan;
 
+/* How a volume is padded to the pyramid's grid (edge replication, cropped
+ * back after the reconstruction):
+ *   NSST3_GRID_FAST:    the smallest grid <= 192 whose level sizes are 2^a 3^b
+ *                       lengths (128 -> 144, 192 -> 192): the same result as
+ *                       the reference's DenoiseDemo/main.m on volumes whose
+ *                       sides divide by 12, and the fastest transforms;
+ *   NSST3_GRID_MARSHAL: MarshalData.m:3-22 as the reference's any-size demo
+ *                       (mainAnySize.m:51) pads: every side gains
+ *                       d - rem(n, d) planes, d = 3 2^(nlevels-1) (128 -> 132,
+ *                       192 -> 204), Pyr_mode 1.5 only; its level sizes need
+ *                       the lengths 132, 88, 44, 22 and 204, 136, 68, 34,
+ *                       which are compiled (others are rejected). */
+enum { NSST3_GRID_FAST = 0, NSST3_GRID_MARSHAL = 1 };
 typedef struct nsst3_config {
   int nlevels;                   /* pyramid levels, 1..4 (the demo uses 3) */
   int num_dirs[NSST_MAX_LEVELS]; /* numDir per level, finest first; 3*numDir^2 bands per level (numDir | 24) */
   double pyr_mode;               /* 1, 1.5 or 2 (PyrNDDec_mm.m:58-74); 1.5 in the demo */
+  int grid;                      /* NSST3_GRID_FAST (0) or NSST3_GRID_MARSHAL */
 } nsst3_config;
 
 /* Plan for batches of up to `batch` volumes of n0 x n1 x n2 (each <= 192).

@@ -30,7 +30,11 @@ class NsstItem(ctypes.Structure):
 
 
 class Nsst3Config(ctypes.Structure):
-    _fields_ = [('nlevels', ctypes.c_int), ('num_dirs', ctypes.c_int * MAX_LEVELS), ('pyr_mode', ctypes.c_double)]
+    _fields_ = [('nlevels', ctypes.c_int), ('num_dirs', ctypes.c_int * MAX_LEVELS), ('pyr_mode', ctypes.c_double),
+                ('grid', ctypes.c_int)]
+
+
+GRID_FAST, GRID_MARSHAL = 0, 1
 
 
 class NsstSeparateInfo(ctypes.Structure):

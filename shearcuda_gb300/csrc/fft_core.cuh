@@ -265,6 +265,108 @@ struct Dft<16, DIR> {
   }
 };
 
+// Odd radices 5, 7, 11, 13, 17 (the 3-D pyramid on the reference's padded
+// grids: 132 = 3 * 4 * 11, 204 = 3 * 4 * 17 and their level sizes).  With
+// a_j = v[j] + v[R-j], b_j = v[j] - v[R-j] (j = 1 .. h, h = (R-1)/2):
+//   X[k]   = v[0] + sum_j a_j cos(2 pi jk/R) + DIR i sum_j b_j sin(2 pi jk/R)
+//   X[R-k] = the same with the second sum negated,  X[0] = v[0] + sum_j a_j,
+// which is the R-point DFT with exp(DIR 2 pi i jk / R) paired over j and R - j.
+// The tables hold cos / sin(2 pi m / R) computed in FP64 and rounded to FP32.
+template <int R>
+struct OddTab;
+template <>
+struct OddTab<5> {
+  __host__ __device__ static constexpr float c(int m) {
+    constexpr float t[5] = {1.000000000e+00f, 3.090169944e-01f, -8.090169944e-01f, -8.090169944e-01f, 3.090169944e-01f};
+    return t[m];
+  }
+  __host__ __device__ static constexpr float s(int m) {
+    constexpr float t[5] = {0.000000000e+00f, 9.510565163e-01f, 5.877852523e-01f, -5.877852523e-01f, -9.510565163e-01f};
+    return t[m];
+  }
+};
+template <>
+struct OddTab<7> {
+  __host__ __device__ static constexpr float c(int m) {
+    constexpr float t[7] = {1.000000000e+00f, 6.234898019e-01f, -2.225209340e-01f, -9.009688679e-01f, -9.009688679e-01f, -2.225209340e-01f, 6.234898019e-01f};
+    return t[m];
+  }
+  __host__ __device__ static constexpr float s(int m) {
+    constexpr float t[7] = {0.000000000e+00f, 7.818314825e-01f, 9.749279122e-01f, 4.338837391e-01f, -4.338837391e-01f, -9.749279122e-01f, -7.818314825e-01f};
+    return t[m];
+  }
+};
+template <>
+struct OddTab<11> {
+  __host__ __device__ static constexpr float c(int m) {
+    constexpr float t[11] = {1.000000000e+00f, 8.412535328e-01f, 4.154150130e-01f, -1.423148383e-01f, -6.548607339e-01f, -9.594929736e-01f, -9.594929736e-01f, -6.548607339e-01f, -1.423148383e-01f, 4.154150130e-01f, 8.412535328e-01f};
+    return t[m];
+  }
+  __host__ __device__ static constexpr float s(int m) {
+    constexpr float t[11] = {0.000000000e+00f, 5.406408175e-01f, 9.096319954e-01f, 9.898214419e-01f, 7.557495744e-01f, 2.817325568e-01f, -2.817325568e-01f, -7.557495744e-01f, -9.898214419e-01f, -9.096319954e-01f, -5.406408175e-01f};
+    return t[m];
+  }
+};
+template <>
+struct OddTab<13> {
+  __host__ __device__ static constexpr float c(int m) {
+    constexpr float t[13] = {1.000000000e+00f, 8.854560257e-01f, 5.680647467e-01f, 1.205366803e-01f, -3.546048870e-01f, -7.485107482e-01f, -9.709418174e-01f, -9.709418174e-01f, -7.485107482e-01f, -3.546048870e-01f, 1.205366803e-01f, 5.680647467e-01f, 8.854560257e-01f};
+    return t[m];
+  }
+  __host__ __device__ static constexpr float s(int m) {
+    constexpr float t[13] = {0.000000000e+00f, 4.647231720e-01f, 8.229838659e-01f, 9.927088741e-01f, 9.350162427e-01f, 6.631226582e-01f, 2.393156643e-01f, -2.393156643e-01f, -6.631226582e-01f, -9.350162427e-01f, -9.927088741e-01f, -8.229838659e-01f, -4.647231720e-01f};
+    return t[m];
+  }
+};
+template <>
+struct OddTab<17> {
+  __host__ __device__ static constexpr float c(int m) {
+    constexpr float t[17] = {1.000000000e+00f, 9.324722294e-01f, 7.390089172e-01f, 4.457383558e-01f, 9.226835946e-02f, -2.736629901e-01f, -6.026346364e-01f, -8.502171357e-01f, -9.829730997e-01f, -9.829730997e-01f, -8.502171357e-01f, -6.026346364e-01f, -2.736629901e-01f, 9.226835946e-02f, 4.457383558e-01f, 7.390089172e-01f, 9.324722294e-01f};
+    return t[m];
+  }
+  __host__ __device__ static constexpr float s(int m) {
+    constexpr float t[17] = {0.000000000e+00f, 3.612416662e-01f, 6.736956436e-01f, 8.951632914e-01f, 9.957341763e-01f, 9.618256432e-01f, 7.980172273e-01f, 5.264321629e-01f, 1.837495178e-01f, -1.837495178e-01f, -5.264321629e-01f, -7.980172273e-01f, -9.618256432e-01f, -9.957341763e-01f, -8.951632914e-01f, -6.736956436e-01f, -3.612416662e-01f};
+    return t[m];
+  }
+};
+
+template <int R, int DIR>
+struct DftOdd {
+  template <class E>
+  __device__ __forceinline__ static void run(E* v) {
+    constexpr int h = (R - 1) / 2;
+    E a[h], b[h];
+#pragma unroll
+    for (int j = 1; j <= h; j++) {
+      a[j - 1] = cadd(v[j], v[R - j]);
+      b[j - 1] = csub(v[j], v[R - j]);
+    }
+    E x0 = v[0];
+#pragma unroll
+    for (int j = 0; j < h; j++) x0 = cadd(x0, a[j]);
+#pragma unroll
+    for (int k = 1; k <= h; k++) {
+      E A = caxc(v[0], OddTab<R>::c(k % R), a[0]);
+      E Bs = cscale(b[0], OddTab<R>::s(k % R));
+#pragma unroll
+      for (int j = 2; j <= h; j++) {
+        A = caxc(A, OddTab<R>::c((j * k) % R), a[j - 1]);
+        Bs = caxc(Bs, OddTab<R>::s((j * k) % R), b[j - 1]);
+      }
+      // DIR i Bs: forward (DIR = -1) X[k] = A - i Bs, inverse X[k] = A + i Bs
+      const E iB = mul_i<DIR>(Bs);
+      v[k] = cadd(A, iB);
+      v[R - k] = csub(A, iB);
+    }
+    v[0] = x0;
+  }
+};
+template <int DIR> struct Dft<5, DIR> : DftOdd<5, DIR> {};
+template <int DIR> struct Dft<7, DIR> : DftOdd<7, DIR> {};
+template <int DIR> struct Dft<11, DIR> : DftOdd<11, DIR> {};
+template <int DIR> struct Dft<13, DIR> : DftOdd<13, DIR> {};
+template <int DIR> struct Dft<17, DIR> : DftOdd<17, DIR> {};
+
 // ---------------------------------------------------------------------------
 // Radix plans per length (product of radices == N).
 // ---------------------------------------------------------------------------

@@ -213,7 +213,7 @@ struct PyrWin {  // separable pyramid window of one level (device arrays v0..v2)
 // One pass of a batched 3-D FFT with a fused prologue / epilogue
 // (k_vol3d_pass.cu).  Ranges along the two non-transformed axes select the
 // CTA's sequences: axis 2 (z rows): a = x, b = y; axis 1: a = x, b = z;
-// axis 0: a = y, b = z; b_n is a multiple of 8.
+// axis 0: a = y, b = z (b_n need not be a multiple of the 8-sequence group).
 enum { V3_LD_CPLX = 0, V3_LD_REAL = 1, V3_LD_PAIR = 2, V3_LD_MASKED = 3 };
 enum { V3_ST_CPLX = 0, V3_ST_REAL = 1, V3_ST_THRESH = 2, V3_ST_SPEC = 3, V3_ST_PAIR = 4 };
 struct V3Pass {
@@ -239,8 +239,14 @@ struct V3Pass {
   int ia = 0, ib = -1, nb_item = 0;
   float scale = 1.f;
   int first = 0;                  // ST_SPEC: assign instead of accumulate
+  int m_r2 = 0;                   // keep-bit row pitch along dim 2 (0: r2), a multiple of 8 when r2 is not
 };
 bool v3_pass_len_supported(int n);
+// the lengths with the factors 11 and 17 (k_vol3d_pass_odd.cu)
+bool v3_pass_len_supported_odd(int n);
+cudaError_t prepare_v3_pass_odd(int n);
+cudaError_t launch_v3_pass_odd(int N, int dir, int ld, int st, float2* out, const float2* in, const V3Pass& P,
+                               const float2* tw, int nitems, cudaStream_t stream);
 cudaError_t prepare_v3_pass(int n);
 cudaError_t launch_v3_pass(int N, int dir, int ld, int st, float2* out, const float2* in, const V3Pass& P,
                            const float2* tw, int nitems, cudaStream_t stream);

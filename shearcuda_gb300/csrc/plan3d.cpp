@@ -104,6 +104,43 @@ bool level_sizes(int g, int L, const double* D, int* out) {
   return true;
 }
 
+// The grid of MarshalData.m:3-22 (the reference's any-size demo,
+// mainAnySize.m:51): every dimension gains d - rem(n, d) planes, d = 3 2^(L-1)
+// (divFactor [3 6 12 24] of the level count), so that Pyr_mode 1.5's level
+// sizes g, g/1.5, g/3, ... are integers.  Its level sizes need transform
+// lengths with other prime factors (132 = 3 * 4 * 11, 204 = 3 * 4 * 17); the
+// pass kernels hold sequence groups that need not divide them.
+const int kOddLens[] = {22, 34, 44, 68, 88, 132, 136, 204};
+bool is_pyr_len(int n) {
+  if (is_fft_len(n)) return true;
+  for (int v : kOddLens)
+    if (v == n) return true;
+  return false;
+}
+int marshal_grid(int n, int L) {
+  const int d = 3 << (L - 1);
+  return n + d - n % d;
+}
+bool marshal_sizes(int g, int L, const double* D, int* out, int* missing) {
+  double v = g;
+  out[0] = g;
+  *missing = 0;
+  if (!is_pyr_len(g) || conv_len(g) < 0) {
+    *missing = g;
+    return false;
+  }
+  for (int l = 0; l < L; l++) {
+    v /= D[l];
+    const int iv = (int)std::lround(v);
+    if (std::fabs(v - iv) > 1e-9 || !is_pyr_len(iv) || (l + 1 < L && conv_len(iv) < 0)) {
+      *missing = iv;
+      return false;
+    }
+    out[l + 1] = iv;
+  }
+  return true;
+}
+
 // Smallest supported grid >= n for which every level size works.
 int grid_size(int n, int L, const double* D) {
   int tmp[NSST_MAX_LEVELS + 1];
@@ -111,6 +148,10 @@ int grid_size(int n, int L, const double* D) {
     if (g >= n && g <= kMaxGrid && level_sizes(g, L, D, tmp)) return g;
   return -1;
 }
+
+// row pitch of the keep bits along the box's last dimension: a multiple of 8,
+// so that the eight sequences of a pass group fill whole bytes
+int mask_pitch(int m2) { return (m2 + 7) / 8 * 8; }
 
 int host_threads3() {
   unsigned n = std::thread::hardware_concurrency();
@@ -354,6 +395,7 @@ nsst_status run_sh_level(nsst3_plan* p, const float* bp, int l, float* acc, cons
       P3.ib = bb;
       P3.nb_item = p->nbands;
       if (record_masks) {
+        P3.m_r2 = mask_pitch(m[2]);
         P3.mwa = p->mask + p->mask_off[ba];
         P3.mwb = bb >= 0 ? p->mask + p->mask_off[bb] : nullptr;
         P3.m_stride = p->mask_bytes;
@@ -442,12 +484,26 @@ nsst_status nsst3_plan_create(const nsst3_config* cfg, int n0, int n1, int n2, i
     return fail3(NSST_ERR_INVALID_ARG, "pyr_mode must be 1, 1.5 or 2");
   const int dims[3] = {n0, n1, n2};
   int sizes[3][NSST_MAX_LEVELS + 1];
+  if (cfg->grid != NSST3_GRID_FAST && cfg->grid != NSST3_GRID_MARSHAL)
+    return fail3(NSST_ERR_INVALID_ARG, "grid must be NSST3_GRID_FAST or NSST3_GRID_MARSHAL");
+  if (cfg->grid == NSST3_GRID_MARSHAL && cfg->pyr_mode != 1.5)
+    return fail3(NSST_ERR_INVALID_ARG, "NSST3_GRID_MARSHAL pads for Pyr_mode 1.5 (MarshalData.m's divFactor)");
   for (int k = 0; k < 3; k++) {
     if (dims[k] < 1) return fail3(NSST_ERR_INVALID_ARG, "volume dims must be positive");
     p->n[k] = dims[k];
-    p->g[k] = grid_size(dims[k], p->L, p->D);
-    if (p->g[k] < 0 || !level_sizes(p->g[k], p->L, p->D, sizes[k]))
-      return fail3(NSST_ERR_UNSUPPORTED_SIZE, "volume dimension too large for this pyramid (grid <= 192)");
+    if (cfg->grid == NSST3_GRID_MARSHAL) {
+      p->g[k] = marshal_grid(dims[k], p->L);
+      int miss = 0;
+      if (!marshal_sizes(p->g[k], p->L, p->D, sizes[k], &miss))
+        return fail3(NSST_ERR_UNSUPPORTED_SIZE,
+                     "MarshalData grid " + std::to_string(p->g[k]) + " of dimension " + std::to_string(dims[k]) +
+                         " needs transform length " + std::to_string(miss) +
+                         ", not compiled (level sizes of the 132 and 204 grids and the 2^a 3^b lengths are)");
+    } else {
+      p->g[k] = grid_size(dims[k], p->L, p->D);
+      if (p->g[k] < 0 || !level_sizes(p->g[k], p->L, p->D, sizes[k]))
+        return fail3(NSST_ERR_UNSUPPORTED_SIZE, "volume dimension too large for this pyramid (grid <= 192)");
+    }
   }
   V3_CUDA(cudaGetDevice(&p->device));
   p->in_elems = (size_t)n0 * n1 * n2;
@@ -791,7 +847,8 @@ nsst_status nsst3_plan_enable_grad(nsst3_plan* p) {
   size_t bytes = 0;
   for (int b = 0; b < p->nbands; b++) {
     p->mask_off[b] = bytes;
-    bytes += align_up3(p->lev[p->band_level[b]].vol() / 8, 256);
+    const nsst3_plan::Level& lv = p->lev[p->band_level[b]];
+    bytes += align_up3((size_t)lv.m[0] * lv.m[1] * mask_pitch(lv.m[2]) / 8, 256);
   }
   p->mask_bytes = bytes;
   void* m = nullptr;
@@ -828,6 +885,7 @@ nsst_status nsst3_denoise_backward(nsst3_plan* p, const float* gy, float* gx, in
       set_box(P1, m, o);
       P1.rsrc = p->rbp + a.bp_off;
       P1.r_stride = p->bp_floats;
+      P1.m_r2 = mask_pitch(m[2]);
       P1.mka = p->mask + p->mask_off[ba];
       P1.mkb = bb >= 0 ? p->mask + p->mask_off[bb] : nullptr;
       P1.m_stride = p->mask_bytes;

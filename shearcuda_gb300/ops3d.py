@@ -25,7 +25,7 @@ import ctypes
 import numpy as np
 import torch
 
-from ._lib import Nsst3Config, NsstError, check, lib
+from ._lib import GRID_FAST, GRID_MARSHAL, Nsst3Config, NsstError, check, lib
 from .ops import _dev, _dptr, _stream
 
 __all__ = ['VolumePlan', 'get_meyer_based_filter', 'do_pyr_dec', 'do_pyr_rec', 'sh_dec', 'sh_dec_th_rec_cuda',
@@ -52,12 +52,15 @@ class VolumePlan:
     """Filters, windows and work buffers for batches of up to ``batch``
     volumes of size (n0, n1, n2)."""
 
-    def __init__(self, n0, n1, n2, num_dirs=V3_NUM_DIRS, pyr_mode=1.5, batch=1):
+    def __init__(self, n0, n1, n2, num_dirs=V3_NUM_DIRS, pyr_mode=1.5, batch=1, grid='fast'):
+        """grid: 'fast' (edge replication to a 2^a 3^b grid) or 'marshal'
+        (MarshalData.m's padding, as the reference's any-size demo)."""
         cfg = Nsst3Config()
         cfg.nlevels = len(num_dirs)
         for i, v in enumerate(num_dirs):
             cfg.num_dirs[i] = int(v)
         cfg.pyr_mode = float(pyr_mode)
+        cfg.grid = {'fast': GRID_FAST, 'marshal': GRID_MARSHAL}[grid]
         h = ctypes.c_void_p()
         check(lib().nsst3_plan_create(ctypes.byref(cfg), int(n0), int(n1), int(n2), int(batch), ctypes.byref(h)))
         self._h = h
