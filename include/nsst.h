@@ -159,14 +159,16 @@ int nsst_plan_directional(const nsst_plan* plan, int n);
  * run whatever it says (at 256^2 .. 512^2 with dsize [32 32 16 16] the
  * windows are 110-204 px and the bound is ~200x the FFT path's time).
  * Synchronous; allocates 2 n images for the run. */
-enum { NSST_TUNE_MAX_CANDIDATES = 16 };
+enum { NSST_TUNE_MAX_CANDIDATES = 32 };
 typedef struct nsst_tune_result {
   int n;                                     /* batch size timed */
   int ncand;                                 /* candidates timed */
   int chosen;                                /* index of the fastest */
-  char name[NSST_TUNE_MAX_CANDIDATES][48];   /* "split/<analysis>/<rows>/<synthesis>" (analysis: level, level-pairs
-                                                or band; rows: rows8, rows8-pairs, rows16-pairs; synthesis:
-                                                synthesis or synthesis-pairs) or "fused/cluster<C>" */
+  char name[NSST_TUNE_MAX_CANDIDATES][64];   /* "split/<analysis>/<rows>/<synthesis>" (analysis: level, level-pairs,
+                                                level-tma, level-pairs-tma or band; rows: rows8, rows8-pairs,
+                                                rows16-pairs; synthesis: synthesis, synthesis-pairs,
+                                                synthesis-tma or synthesis-pairs-tma; "-tma": column groups
+                                                staged by TMA) or "fused/cluster<C>" */
   float ms[NSST_TUNE_MAX_CANDIDATES];        /* median ms of one directional-stage pass over n images */
   int direct_support[NSST_MAX_LEVELS];       /* per level, px (0: no window below the image size) */
   double direct_err[NSST_MAX_LEVELS];        /* per level: the worst band's truncation error at that window */

@@ -42,12 +42,12 @@ class NsstSeparateInfo(ctypes.Structure):
                 ('buff_wavelet', ctypes.c_double), ('deltamax', ctypes.c_double), ('lam', ctypes.c_double)]
 
 
-TUNE_MAX_CANDIDATES = 16
+TUNE_MAX_CANDIDATES = 32
 
 
 class NsstTuneResult(ctypes.Structure):
     _fields_ = [('n', ctypes.c_int), ('ncand', ctypes.c_int), ('chosen', ctypes.c_int),
-                ('name', (ctypes.c_char * 48) * TUNE_MAX_CANDIDATES), ('ms', ctypes.c_float * TUNE_MAX_CANDIDATES),
+                ('name', (ctypes.c_char * 64) * TUNE_MAX_CANDIDATES), ('ms', ctypes.c_float * TUNE_MAX_CANDIDATES),
                 ('direct_support', ctypes.c_int * MAX_LEVELS), ('direct_err', ctypes.c_double * MAX_LEVELS),
                 ('direct_bound_ms', ctypes.c_float), ('direct_wins', ctypes.c_int)]
 

@@ -15,9 +15,9 @@ BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libnsst.so')
 NVCC = os.environ.get('NVCC', '/usr/local/cuda/bin/nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-SOURCES = ['k_directional.cu', 'k_dir_fused.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_reduce.cu', 'k_wavelet.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'k_vol3d_pass_odd.cu', 'k_dct.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
+SOURCES = ['k_directional.cu', 'k_dir_fused.cu', 'k_cols_tma.cu', 'k_atrous.cu', 'k_adjoint.cu', 'k_reduce.cu', 'k_wavelet.cu', 'k_vol3d.cu', 'k_vol3d_pass.cu', 'k_vol3d_pass_odd.cu', 'k_dct.cu', 'noalloc.cu', 'host_filters.cpp', 'host_filterfile.cpp',
            'host_wavelets.cpp', 'host_dct.cpp', 'host_filters3d.cpp', 'plan.cpp', 'plan3d.cpp']
-HEADERS = ['fft_core.cuh', 'tiles.cuh', 'vol3d_pass.cuh', 'internal.h', 'pyramid_tables.h', 'wavelet_tables.h']
+HEADERS = ['fft_core.cuh', 'tiles.cuh', 'tma.cuh', 'vol3d_pass.cuh', 'internal.h', 'pyramid_tables.h', 'wavelet_tables.h']
 
 
 def _flags(src):

@@ -145,6 +145,27 @@ cudaError_t prepare_dir_fused(int H, int WH, int* max_clusters);
 // tensor map (a 128-byte CUtensorMap at `out`, 64-byte aligned) over `rows`
 // rows of WH float2 starting at lev
 cudaError_t make_level_tmap(void* out, const float2* lev, int H, int WH, size_t rows);
+// tensor map over `rows` rows of `inner` float2 from base (16-byte aligned,
+// inner even), box = box_x float2 x box_y rows
+cudaError_t make_tmap_2d(void* out, const void* base, int inner, size_t rows, int box_x, int box_y);
+// Rows of a column-group tensor-map box: H split into the fewest equal boxes
+// of at most 256 rows (the box-dimension limit).
+constexpr int tma_box_rows(int H) {
+  int n = (H + 255) / 256;
+  while (H % n != 0) n++;
+  return H / n;
+}
+// The level analysis and the synthesis column kernels (ColOp AnalysisLevel,
+// Synthesis and their *Pairs forms, twH the broadcast table for those) with
+// their column groups staged by 2-D TMA (k_cols_tma.cu) from a tensor map
+// over the plan's arena (box: col_tile(H) float2 x tma_box_rows(H) rows):
+// every job's src and spec offset (spec relative to the arena, as spec_row0
+// * WH plus job.spec) is a multiple of WH.  err: the plan's device error word.
+bool cols_tma_supported(int H, int WH);
+cudaError_t prepare_cols_tma(int H);
+cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int njobs, int n_active, int H, int W,
+                            float2* dst_base, const float2* spec_base, size_t spec_row0, size_t band_stride,
+                            const float2* twH, int* err, cudaStream_t st);
 cudaError_t launch_dir_fused(const void* ymap, const FusedJob* jobs, int njobs, int n_active, int nclusters, int H,
                              int W, float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                              const float2* twWh, const float2* twW, const float* thr, int mode, int* err,

@@ -44,11 +44,11 @@
 
 #include "internal.h"
 #include "tiles.cuh"
+#include "tma.cuh"
 
 namespace nsst {
 
 // ------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -81,55 +81,6 @@ __device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank) {
 __device__ __forceinline__ void st_cluster(uint32_t addr, float2 v) {
   asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
 }
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n"
-      " .reg .pred p;\n"
-      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n"
-      "}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// 2-D tiled TMA load global -> this CTA's shared memory, completion counted
-// on the mbarrier in bytes.  x (the inner coordinate, 8-byte elements) is a
-// multiple of 2, so x * 8 is a multiple of 16 bytes.
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(map), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-// generic-proxy accesses of shared memory before this are ordered before
-// later async-proxy (TMA) accesses
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// Bound on the TMA completion wait: try_wait returns after a hardware time
-// limit, so this is seconds, not a spin on a value that may never come.
-constexpr uint32_t kTmaWaitLimit = 1u << 22;
-constexpr int kFusedErrTmaTimeout = 1;
-
-// waits for phase `parity` of the mbarrier; false (and the error code set
-// once) when the limit runs out
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
-  for (uint32_t it = 0; it < kTmaWaitLimit; it++)
-    if (mbar_try_wait(bar, parity)) return true;
-  atomicOr(err, kFusedErrTmaTimeout);
-  return false;
-}
-
 // ------------------------------------------------------------ configuration
 template <class RL>
 struct LastRadix;
@@ -155,7 +106,7 @@ struct FusedCfg {
   static constexpr int CS = WH / CL;  // columns per CTA (column phases)
   static constexpr int RS = H / CL;   // rows per CTA (row phase)
   static constexpr int RP = WH + 1;   // row pitch of the row buffer (odd: conflict-free column access)
-  static constexpr int BH = H <= 256 ? H : H / 2;  // rows per TMA box (box dims <= 256)
+  static constexpr int BH = tma_box_rows(H);  // rows per TMA box (box dims <= 256)
   static constexpr int NBOX = H / BH;
   static constexpr int RL = LastRadix<ColPlan>::value;  // last column pass radix
   static constexpr int TOTAL_LAST = (H / RL) * CS;
@@ -456,9 +407,9 @@ cudaError_t prepare_dir_fused(int H, int WH, int* max_clusters) {
   return cudaErrorInvalidValue;
 }
 
-// Tensor map over the level spectra of a plan: rows x WH elements of 8 bytes
-// (one float2 each), row pitch WH * 8 bytes; box = (columns of one CTA, BH rows).
-cudaError_t make_level_tmap(void* out, const float2* lev, int H, int WH, size_t rows) {
+// 2-D tensor map over rows of `inner` 8-byte elements (one float2 each), row
+// pitch inner * 8 bytes, starting at base; box = (box_x elements, box_y rows).
+cudaError_t make_tmap_2d(void* out, const void* base, int inner, size_t rows, int box_x, int box_y) {
   using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -471,17 +422,26 @@ cudaError_t make_level_tmap(void* out, const float2* lev, int H, int WH, size_t 
     if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
     encode = reinterpret_cast<EncodeFn>(fn);
   }
+  // 16-byte base and pitch, inner box extent a multiple of 16 bytes, box dims <= 256
+  if (((uintptr_t)base & 15) != 0 || inner % 2 != 0 || box_x % 2 != 0 || box_x > 256 || box_y > 256 || box_x < 2 ||
+      box_y < 1 || rows == 0)
+    return cudaErrorInvalidValue;
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)inner * sizeof(float2)};
+  cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(reinterpret_cast<CUtensorMap*>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(base),
+                      dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Tensor map over the level spectra of a plan: rows x WH float2, box = (columns
+// of one CTA of the cluster, tma_box_rows(H) rows).
+cudaError_t make_level_tmap(void* out, const float2* lev, int H, int WH, size_t rows) {
   const int cl = dir_fused_cluster(H, WH);
   if (cl == 0) return cudaErrorInvalidValue;
-  const int CS = WH / cl, BH = H <= 256 ? H : H / 2;
-  cuuint64_t dims[2] = {(cuuint64_t)WH, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)WH * sizeof(float2)};
-  cuuint32_t box[2] = {(cuuint32_t)CS, (cuuint32_t)BH};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = encode(reinterpret_cast<CUtensorMap*>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
-                      const_cast<float2*>(lev), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+  return make_tmap_2d(out, lev, WH, rows, WH / cl, tma_box_rows(H));
 }
 
 template <int H, int WH, int CL, int T, int MB, class RP, class CP>

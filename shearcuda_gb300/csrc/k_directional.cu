@@ -27,32 +27,6 @@
 
 namespace nsst {
 
-// The synthesis CTA keeps its running band sum in shared memory next to the
-// transform buffer and the next band's staging buffer.
-template <int N>
-struct SynCfg : ColCfg<N> {
-  // two column buffers (transform, running sum), the DC column and the
-  // staging buffer that the next band streams into (cp.async) while the
-  // current one is transformed
-  static constexpr size_t smem() {
-    return (2 * (size_t)N * ColCfg<N>::LD + N + (size_t)N * ColCfg<N>::CS) * sizeof(float2);
-  }
-  // the column kernels' thread count; shared memory allows two CTAs per SM below 2048 points
-  static constexpr int T = ColCfg<N>::T;
-  static constexpr int MINB = N >= 2048 ? 1 : 2;
-};
-
-// The multi-band analysis CTA keeps its column group of the level spectrum,
-// a staging buffer for the next band's filter spectrum and the transform.
-template <int N>
-struct AnaCfg : ColCfg<N> {
-  static constexpr size_t smem() { return 3 * (size_t)N * ColCfg<N>::CS * sizeof(float2); }
-  // the column kernels' thread count (every thread busy in the radix-16
-  // passes); shared memory allows two CTAs per SM below 2048 points
-  static constexpr int T = ColCfg<N>::T;
-  static constexpr int MINB = N >= 2048 ? 1 : 2;
-};
-
 // packed-real pre-processing of index k (see c2r_pre) is C2RPreLdRM (tiles.cuh):
 // Z[k] = E + iO with E = X[k] + conj(X[WH-k]), O = (X[k] - conj(X[WH-k])) w^-k;
 // k = 0 unpacks the two real bins.
@@ -497,21 +471,6 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB) k_band_synthesi
 // the transform buffers hold [row][pair] cpx2.  twH4: the column twiddle
 // table with each entry as its broadcast pairs.
 // ---------------------------------------------------------------------------
-// a * b and a * conj(b) for two independent products
-__device__ __forceinline__ cpx2 cmul_pp(cpx2 a, cpx2 b) {
-  return {__ffma2_rn(a.re, b.re, neg2(__fmul2_rn(a.im, b.im))), __ffma2_rn(a.re, b.im, __fmul2_rn(a.im, b.re))};
-}
-__device__ __forceinline__ cpx2 cmulc_pp(cpx2 a, cpx2 b) {
-  return {__ffma2_rn(a.re, b.re, __fmul2_rn(a.im, b.im)), __ffma2_rn(a.im, b.re, neg2(__fmul2_rn(a.re, b.im)))};
-}
-__device__ __forceinline__ cpx2 ld_pair(const float2* p) {  // two adjacent float2 (16-byte aligned)
-  const float4 q = *reinterpret_cast<const float4*>(p);
-  return pair(make_float2(q.x, q.y), make_float2(q.z, q.w));
-}
-__device__ __forceinline__ void st_pair(float2* p, cpx2 v) {
-  *reinterpret_cast<float4*>(p) = make_float4(v.re.x, v.im.x, v.re.y, v.im.y);
-}
-
 template <int H>
 __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
     k_band_analysis_ml_p(const ColJob* __restrict__ jobs, int n_active, int WH, const float2* src_base,
@@ -626,8 +585,6 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
 // The dynamic shared-memory opt-in is done once per device and kernel by the
 // prepare_* calls (plan creation), never on the launch path.
 // ---------------------------------------------------------------------------
-#define NSST_ROW_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024)
-#define NSST_COL_SIZES(X) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 bool row_len_supported(int wh) {
   switch (wh) {

@@ -9,6 +9,7 @@
 // is a fixed sequence of launches on the caller's stream.
 #include <algorithm>
 #include <initializer_list>
+#include <numeric>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -31,6 +32,7 @@ struct DirChoice {
   int row_tile = 1;
   bool packed = false;  // row pass on split-complex row pairs (FP32x2 arithmetic)
   bool cols_packed = false;  // analysis (per level) and synthesis on split-complex column pairs
+  bool cols_tma = false;     // analysis (per level) and synthesis with column groups staged by TMA
 };
 
 // autotuner buckets of the batch size n: bucket b holds 2^b <= n < 2^(b+1)
@@ -135,6 +137,12 @@ struct nsst_plan {
   int dir_mode = NSST_DIRECTIONAL_AUTO;
   int fused_clusters = 0;       // co-resident clusters of the fused kernel
   alignas(64) unsigned char fused_tmap[128] = {};  // TMA tensor map over the level spectra
+  // TMA column staging of the split directional stage (k_cols_tma.cu): a
+  // tensor map over the whole arena as rows of WH float2; the filter spectra
+  // start at row spec_row0
+  alignas(64) unsigned char cols_tmap[128] = {};
+  bool cols_tma_ok = false;
+  size_t spec_row0 = 0;
   FusedJob* j_fused = nullptr;  // (B*nlev) levels with more bands first, then items
   int* dev_err = nullptr;       // error word of the bounded device waits
   // autotuner record (nsst_plan_autotune): per batch-size bucket the fastest
@@ -313,16 +321,23 @@ nsst_status check_spectral_n(const nsst_plan* p, int n, const float* const* a, c
 // The directional-stage implementation of a denoise call of n items: the
 // candidate under test while tuning; else the plan's mode (split or fused),
 // with the tuned split settings where the autotuner chose a split candidate;
-// else (auto) the tuned choice of n's bucket; else the untuned default, the
-// fused kernel where it has been measured faster and its clusters fill the
-// GPU (256 x 256, one cluster per image and level), the split kernels otherwise.
+// else (auto) the tuned choice of n's bucket; else the untuned default: the
+// split kernels with the column groups staged by TMA (measured faster than
+// the cp.async forms at every size, 2-11 %), the per-level analysis where its
+// grid fills the GPU twice and the per-band analysis below, and the row pass
+// on two tiles of row pairs at <= 192 points per row (faster there, slower at
+// 256 and up).  The fused kernel measured slower than these at every size.
 DirChoice dir_choice(const nsst_plan* p, int n) {
   if (p->forcing) return p->forced;
+  DirChoice def;
+  def.cols_tma = p->cols_tma_ok;
+  if (p->WH <= 192 && p->H % (2 * row_tile(p->WH)) == 0) {
+    def.packed = true;
+    def.row_tile = 2;
+  }
   const int b = tune_bucket(n);
-  DirChoice c;
-  if (p->tuned[b]) c = p->tuned_choice[b];
-  else c.fused = p->fused_ok && p->H == 256 && p->W == 256 && n * p->nlev >= p->fused_clusters;
-  if (p->dir_mode == NSST_DIRECTIONAL_SPLIT && c.fused) c = DirChoice{};
+  DirChoice c = p->tuned[b] ? p->tuned_choice[b] : def;
+  if (p->dir_mode == NSST_DIRECTIONAL_SPLIT && c.fused) c = def;
   if (p->dir_mode == NSST_DIRECTIONAL_FUSED) c.fused = true;
   if (!p->fused_ok) c.fused = false;
   return c;
@@ -434,16 +449,23 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
     off = align_up(off + bytes, 256);
     return at;
   };
+  // regions that the column kernels stage by TMA start on a row of the
+  // arena's tensor map (rows of WH float2)
+  const size_t row_pitch = std::lcm((size_t)256, sizeof(float2) * p->WH);
+  auto take_rows = [&](size_t bytes) {
+    off = align_up(off, row_pitch);
+    return take(bytes);
+  };
   const size_t NB = (size_t)B;
-  size_t o_spec = take(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
+  size_t o_spec = take_rows(sizeof(float2) * ((size_t)p->ndir_total * HWh + (size_t)p->ndir_total * H));
   size_t o_twH = take(sizeof(float2) * H), o_twWh = take(sizeof(float2) * p->WH),
          o_twW = take(sizeof(float2) * p->WH);
   size_t o_twWh4 = take(sizeof(float4) * p->WH), o_twW4 = take(sizeof(float4) * p->WH),
          o_twH4 = take(sizeof(float4) * H);
   size_t o_pyr = take(sizeof(float) * p->s_pyr * NB);
   size_t o_tmp = take(sizeof(float) * p->s_tmp * NB);
-  size_t o_lev = take(sizeof(float2) * p->s_lev * NB);
-  size_t o_band = take(sizeof(float2) * p->s_band * NB);
+  size_t o_lev = take_rows(sizeof(float2) * p->s_lev * NB);
+  size_t o_band = take_rows(sizeof(float2) * p->s_band * NB);
   size_t o_sum = take(sizeof(float2) * p->s_sum * NB);
   size_t o_rec = take(sizeof(float) * p->s_rec * NB);
   size_t o_red = take(sizeof(double) * p->nbands * kRedBlocks);
@@ -711,6 +733,20 @@ nsst_status create_plan(const nsst_config* cfg, int H, int W, int B, const Filte
       p->fused_clusters = ncl;
     } else {
       (void)cudaGetLastError();  // the split kernels stay; clear a refused attribute or occupancy query
+    }
+  }
+  // TMA column staging (an autotuner candidate): one tensor map over the arena
+  {
+    const size_t pitch = sizeof(float2) * p->WH, rows = p->arena_bytes / pitch;
+    if (cols_tma_supported(H, p->WH) && (size_t)(p->spec - (float2*)A) % p->WH == 0 && rows <= (size_t)INT32_MAX) {
+      ce = prepare_cols_tma(H);
+      if (ce == cudaSuccess) ce = make_tmap_2d(p->cols_tmap, A, p->WH, rows, col_tile(H), tma_box_rows(H));
+      if (ce == cudaSuccess) {
+        p->cols_tma_ok = true;
+        p->spec_row0 = (size_t)(p->spec - (float2*)A) / p->WH;
+      } else {
+        (void)cudaGetLastError();  // the cp.async column kernels stay
+      }
     }
   }
   *out = p;
@@ -1010,20 +1046,26 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 }
 
 // The band analysis of n active items: one CTA per (level, item) column
-// group streams all bands of the level when that grid fills the GPU once (two
-// CTAs per SM); smaller batches (a single image) keep one CTA per (band,
-// item) column group, which has ndir times more CTAs.
-nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0, bool pairs = false) {
+// group streams all bands of the level when that grid fills the GPU twice
+// (ana 0), or always (ana 1); otherwise (a single image, ana 2) one CTA per
+// (band, item) column group, which has ndir times more CTAs.  pairs: the
+// level form on split-complex column pairs; tma: the level form with its
+// column groups staged by TMA (forward arena only).
+nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0, bool pairs = false,
+                                  bool tma = false) {
   float2* base = (float2*)(grad ? p->garena : p->arena);
-  const size_t ctas = (size_t)n * p->nlev * (p->WH / 8);
-  if (pairs && ana == 1) {
-    NSST_CUDA(launch_cols(ColOp::AnalysisLevelPairs, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
-                          p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, (const float2*)p->twH4, st));
-    return NSST_OK;
-  }
-  if (ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count)) {
-    NSST_CUDA(launch_cols(ColOp::AnalysisLevel, grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n,
-                          p->H, p->W, base, base, p->spec, (size_t)p->H * p->WH, p->twH, st));
+  const size_t ctas = (size_t)n * p->nlev * (p->WH / col_tile(p->H));
+  const bool level = ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count);
+  const size_t bs = (size_t)p->H * p->WH;
+  const float2* tw = pairs ? (const float2*)p->twH4 : p->twH;
+  if (level && tma && !grad && p->cols_tma_ok) {
+    NSST_CUDA(launch_cols_tma(pairs ? ColOp::AnalysisLevelPairs : ColOp::AnalysisLevel, p->cols_tmap,
+                              p->j_analysis_lev, p->B * p->nlev, n, p->H, p->W, base, p->spec, p->spec_row0, bs, tw,
+                              p->dev_err, st));
+  } else if (level) {
+    NSST_CUDA(launch_cols(pairs ? ColOp::AnalysisLevelPairs : ColOp::AnalysisLevel,
+                          grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n, p->H, p->W, base, base,
+                          p->spec, bs, tw, st));
   } else {
     NSST_CUDA(launch_cols(ColOp::Analysis, grad ? p->gj_analysis : p->j_analysis, p->B * p->ndir_total, n, p->H,
                           p->W, base, base, p->spec, 0, p->twH, st));
@@ -1044,14 +1086,20 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
     return NSST_OK;
   }
   char* A = p->arena;
-  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana, c.cols_packed));
+  const bool tma = c.cols_tma && p->cols_tma_ok;
+  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana, c.cols_packed, tma));
   timer_mark(p, "band_analysis_cols", st);
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
-  NSST_CUDA(launch_cols(c.cols_packed ? ColOp::SynthesisPairs : ColOp::Synthesis, p->j_synthesis, p->B * p->nlev, n,
-                        p->H, p->W, (float2*)A, (float2*)A, p->spec, (size_t)p->H * p->WH,
-                        c.cols_packed ? (const float2*)p->twH4 : p->twH, st));
+  const ColOp syn = c.cols_packed ? ColOp::SynthesisPairs : ColOp::Synthesis;
+  const float2* twc = c.cols_packed ? (const float2*)p->twH4 : p->twH;
+  if (tma)
+    NSST_CUDA(launch_cols_tma(syn, p->cols_tmap, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, p->spec,
+                              p->spec_row0, (size_t)p->H * p->WH, twc, p->dev_err, st));
+  else
+    NSST_CUDA(launch_cols(syn, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A, p->spec,
+                          (size_t)p->H * p->WH, twc, st));
   timer_mark(p, "band_synthesis_cols", st);
   return NSST_OK;
 }
@@ -1597,19 +1645,23 @@ std::vector<std::pair<DirChoice, std::string>> dir_candidates(const nsst_plan* p
   // tiles of split-complex row pairs; columns: one value or column pairs
   // (the pairs' analysis streams all bands of a level per CTA)
   const int rows[3][2] = {{1, 0}, {1, 1}, {2, 1}};
-  for (int ana : {1, 2})
-    for (bool cp : {false, true})
-      for (const auto& r : rows) {
-        DirChoice d;
-        d.ana = ana;
-        d.row_tile = r[0];
-        d.packed = r[1] != 0;
-        d.cols_packed = cp;
-        if (p->H % (rs * r[0]) != 0) continue;
-        c.push_back({d, std::string("split/") + (ana == 1 ? (cp ? "level-pairs" : "level") : "band") + "/rows" +
-                            std::to_string(rs * r[0]) + (d.packed ? "-pairs" : "") +
-                            (cp ? "/synthesis-pairs" : "/synthesis")});
-      }
+  for (bool tma : {false, true}) {
+    if (tma && !p->cols_tma_ok) continue;
+    for (int ana : {1, 2})
+      for (bool cp : {false, true})
+        for (const auto& r : rows) {
+          DirChoice d;
+          d.ana = ana;
+          d.row_tile = r[0];
+          d.packed = r[1] != 0;
+          d.cols_packed = cp;
+          d.cols_tma = tma;
+          if (p->H % (rs * r[0]) != 0) continue;
+          const std::string cols = std::string(cp ? "-pairs" : "") + (tma ? "-tma" : "");
+          c.push_back({d, std::string("split/") + (ana == 1 ? "level" + cols : std::string("band")) + "/rows" +
+                              std::to_string(rs * r[0]) + (d.packed ? "-pairs" : "") + "/synthesis" + cols});
+        }
+  }
   if (p->fused_ok) {
     DirChoice d;
     d.fused = true;

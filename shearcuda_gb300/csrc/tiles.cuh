@@ -30,6 +30,55 @@ struct ColCfg {  // N = H points per column
   static constexpr size_t smem() { return 2 * (size_t)N * LD * sizeof(float2); }
 };
 
+// The synthesis CTA keeps its running band sum in shared memory next to the
+// transform buffer and the next band's staging buffer.
+template <int N>
+struct SynCfg : ColCfg<N> {
+  // two column buffers (transform, running sum), the DC column and the
+  // staging buffer that the next band streams into (cp.async) while the
+  // current one is transformed
+  static constexpr size_t smem() {
+    return (2 * (size_t)N * ColCfg<N>::LD + N + (size_t)N * ColCfg<N>::CS) * sizeof(float2);
+  }
+  // the column kernels' thread count; shared memory allows two CTAs per SM below 2048 points
+  static constexpr int T = ColCfg<N>::T;
+  static constexpr int MINB = N >= 2048 ? 1 : 2;
+};
+
+// The multi-band analysis CTA keeps its column group of the level spectrum,
+// a staging buffer for the next band's filter spectrum and the transform.
+template <int N>
+struct AnaCfg : ColCfg<N> {
+  static constexpr size_t smem() { return 3 * (size_t)N * ColCfg<N>::CS * sizeof(float2); }
+  // the column kernels' thread count (every thread busy in the radix-16
+  // passes); shared memory allows two CTAs per SM below 2048 points
+  static constexpr int T = ColCfg<N>::T;
+  static constexpr int MINB = N >= 2048 ? 1 : 2;
+};
+
+// Split-complex column pairs (cpx2): columns 2p and 2p + 1 of a group share a
+// thread's registers; the staging buffers keep global memory's [row][column]
+// float2 layout.
+// a * b and a * conj(b) for two independent products
+__device__ __forceinline__ cpx2 cmul_pp(cpx2 a, cpx2 b) {
+  return {__ffma2_rn(a.re, b.re, neg2(__fmul2_rn(a.im, b.im))), __ffma2_rn(a.re, b.im, __fmul2_rn(a.im, b.re))};
+}
+__device__ __forceinline__ cpx2 cmulc_pp(cpx2 a, cpx2 b) {
+  return {__ffma2_rn(a.re, b.re, __fmul2_rn(a.im, b.im)), __ffma2_rn(a.im, b.re, neg2(__fmul2_rn(a.re, b.im)))};
+}
+__device__ __forceinline__ cpx2 ld_pair(const float2* p) {  // two adjacent float2 (16-byte aligned)
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  return pair(make_float2(q.x, q.y), make_float2(q.z, q.w));
+}
+__device__ __forceinline__ void st_pair(float2* p, cpx2 v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.re.x, v.im.x, v.re.y, v.im.y);
+}
+
+
+// transform lengths with row / column kernels
+#define NSST_ROW_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024)
+#define NSST_COL_SIZES(X) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
+
 // The threshold rule of nsst_HT.m:34-46 (hard: |v| > th keeps v) and
 // soft thresholding (sign(v) max(|v| - th, 0)).
 __device__ __forceinline__ float apply_thresh(float v, float th, int mode) {

@@ -134,8 +134,8 @@ class ShearPlan:
                 'direct_wins': bool(r.direct_wins)}
 
     def directional_candidates(self):
-        buf = ctypes.create_string_buffer(1024)
-        n = lib().nsst_plan_directional_candidates(self.handle, buf, 1024)
+        buf = ctypes.create_string_buffer(4096)
+        n = lib().nsst_plan_directional_candidates(self.handle, buf, 4096)
         return buf.value.decode().split('\n')[:n]
 
     def select_directional(self, n, index):

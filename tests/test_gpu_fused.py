@@ -46,15 +46,18 @@ def test_fused_available(built_lib, cuda, HW):
     shear.set_directional('split')
     assert shear.directional(3) == 'split'
     shear.set_directional('auto')
-    # untuned default: the split kernels unless the fused kernel was measured
-    # faster for the size and its clusters fill the GPU (256 x 256, >= 9 images)
+    # untuned default: the split kernels (the fused kernel runs when forced or
+    # when the autotuner measured it fastest)
     assert shear.directional(1) == 'split'
 
 
-def test_fused_default_for_large_256_batches(built_lib, cuda):
+def test_untuned_default_is_split_for_large_256_batches(built_lib, cuda):
+    # the split kernels with TMA-staged columns and row pairs measured faster
+    # than the fused kernel at 256 x 256 (1.14 against 1.19 ms for 64 images)
     import shearcuda_gb300 as sc
     shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256, batch=16)
-    assert shear.directional(16) == 'fused'
+    assert shear.fused_clusters() > 0
+    assert shear.directional(16) == 'split'
     assert shear.directional(2) == 'split'
 
 
