@@ -607,7 +607,7 @@ bool col_len_supported(int h) {
   }
 }
 int row_tile(int wh) { return wh >= 1024 ? 4 : 8; }
-int col_tile(int h) { return h >= 1024 ? 4 : 8; }
+int col_tile(int h) { return h >= 768 ? 4 : 8; }
 
 template <typename KernelT>
 static cudaError_t opt_in(KernelT k, size_t bytes) {

@@ -23,7 +23,7 @@ struct RowCfg {  // N = W/2 complex points per row
 };
 template <int N>
 struct ColCfg {  // N = H points per column
-  static constexpr int CS = N >= 1024 ? 4 : 8;
+  static constexpr int CS = N >= 768 ? 4 : 8;  // 768 x 8 float2 per plane would leave one CTA per SM
   static constexpr int T = N >= 2048 ? 512 : 256;
   static constexpr int LD = CS;
   static constexpr int MINB = 1024 / T;  // in-place column passes: 4 CTAs of 256 threads per SM
