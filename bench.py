@@ -616,8 +616,11 @@ def run_gpu(args):
         # ---- e2e through the public API with host buffers: every step copies its
         # 64 images in from pinned host memory and its 64 results back; two
         # device buffer sets and two copy streams let step k+1's input copy and
-        # step k-1's output copy run while step k is denoised
-        pin_in = torch.from_numpy(np.stack(host)).pin_memory()
+        # step k-1's output copy run while step k is denoised.  Steps alternate
+        # between two different input sets, so the check after the loop sees
+        # that each step's results came from its own inputs.
+        host_b = [noisy_image(H, W, SIGMA, 1000 * rank + BATCH + i)[1].astype(np.float32) for i in range(BATCH)]
+        pin_in = [torch.from_numpy(np.stack(host)).pin_memory(), torch.from_numpy(np.stack(host_b)).pin_memory()]
         pin_out = [torch.empty((BATCH, H, W), dtype=torch.float32).pin_memory() for _ in range(2)]
         dev_in = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(2)]
         dev_out = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(2)]
@@ -634,7 +637,7 @@ def run_gpu(args):
                 if k >= 2:
                     s_h2d.wait_event(ev_comp[b])  # step k-2 has consumed dev_in[b]
                 with torch.cuda.stream(s_h2d):
-                    dev_in[b].copy_(pin_in, non_blocking=True)
+                    dev_in[b].copy_(pin_in[b], non_blocking=True)
                     ev_h2d[b].record(s_h2d)
                 stream.wait_event(ev_h2d[b])
                 if k >= 2:
@@ -657,9 +660,13 @@ def run_gpu(args):
         e1.record(stream)
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1) / ne
-        # the host copy of the last step's results is the device path's output, bit for bit
-        last = pin_out[(ne - 1) % 2]
-        same = all(torch.equal(last[i], outs[i].cpu()) for i in range(BATCH))
+        # the host copies of the last two steps' results (one per input set) are
+        # the device path's outputs for those inputs, bit for bit
+        xb = [torch.tensor(h, device=dev) for h in host_b]
+        outs_b = sc.nsst_denoise_batch(xb, plan, sig, K, None)
+        torch.cuda.synchronize()
+        ref = [outs, outs_b]
+        same = all(torch.equal(pin_out[b][i], ref[b][i].cpu()) for b in range(2) for i in range(BATCH))
         line['e2e'] = {'value': BATCH * world / (e2e_ms / 1000.0), 'unit': UNIT,
                        'h2d_bytes_per_step': BATCH * H * W * 4, 'd2h_bytes_per_step': BATCH * H * W * 4,
                        'ms_per_step': e2e_ms, 'pipelined': 'H2D / denoise / D2H of adjacent steps overlap',
