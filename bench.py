@@ -614,42 +614,44 @@ def run_gpu(args):
 
     if not args.no_extras:
         # ---- e2e through the public API with host buffers: every step copies its
-        # 64 images in from pinned host memory and its 64 results back; two
+        # 64 images in from pinned host memory and its 64 results back; three
         # device buffer sets and two copy streams let step k+1's input copy and
-        # step k-1's output copy run while step k is denoised.  Steps alternate
-        # between two different input sets, so the check after the loop sees
-        # that each step's results came from its own inputs.
+        # step k-1's output copy run while step k is denoised (with two sets the
+        # copies measured serialised with the compute: 5.40 against 5.09 ms).
+        # Steps alternate between two different input sets, so the check after
+        # the loop sees that each step's results came from its own inputs.
+        NBUF = 3
         host_b = [noisy_image(H, W, SIGMA, 1000 * rank + BATCH + i)[1].astype(np.float32) for i in range(BATCH)]
         pin_in = [torch.from_numpy(np.stack(host)).pin_memory(), torch.from_numpy(np.stack(host_b)).pin_memory()]
-        pin_out = [torch.empty((BATCH, H, W), dtype=torch.float32).pin_memory() for _ in range(2)]
-        dev_in = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(2)]
-        dev_out = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(2)]
+        pin_out = [torch.empty((BATCH, H, W), dtype=torch.float32).pin_memory() for _ in range(NBUF)]
+        dev_in = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(NBUF)]
+        dev_out = [torch.empty((BATCH, H, W), dtype=torch.float32, device=dev) for _ in range(NBUF)]
         views_in = [list(d.unbind(0)) for d in dev_in]
         views_out = [list(d.unbind(0)) for d in dev_out]
         s_h2d, s_d2h = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
-        ev_h2d = [torch.cuda.Event() for _ in range(2)]
-        ev_comp = [torch.cuda.Event() for _ in range(2)]
-        ev_d2h = [torch.cuda.Event() for _ in range(2)]
+        ev_h2d = [torch.cuda.Event() for _ in range(NBUF)]
+        ev_comp = [torch.cuda.Event() for _ in range(NBUF)]
+        ev_d2h = [torch.cuda.Event() for _ in range(NBUF)]
 
         def e2e_run(nsteps):
             for k in range(nsteps):
-                b = k % 2
-                if k >= 2:
-                    s_h2d.wait_event(ev_comp[b])  # step k-2 has consumed dev_in[b]
+                b = k % NBUF
+                if k >= NBUF:
+                    s_h2d.wait_event(ev_comp[b])  # step k-NBUF has consumed dev_in[b]
                 with torch.cuda.stream(s_h2d):
-                    dev_in[b].copy_(pin_in[b], non_blocking=True)
+                    dev_in[b].copy_(pin_in[k % 2], non_blocking=True)
                     ev_h2d[b].record(s_h2d)
                 stream.wait_event(ev_h2d[b])
-                if k >= 2:
-                    stream.wait_event(ev_d2h[b])  # step k-2's results have left dev_out[b]
+                if k >= NBUF:
+                    stream.wait_event(ev_d2h[b])  # step k-NBUF's results have left dev_out[b]
                 sc.nsst_denoise_batch(views_in[b], plan, sig, K, None, outs=views_out[b])
                 ev_comp[b].record(stream)
                 s_d2h.wait_event(ev_comp[b])
                 with torch.cuda.stream(s_d2h):
                     pin_out[b].copy_(dev_out[b], non_blocking=True)
                     ev_d2h[b].record(s_d2h)
-            for b in range(min(2, nsteps)):
-                stream.wait_event(ev_d2h[(nsteps - 1 - b) % 2])
+            for b in range(min(NBUF, nsteps)):
+                stream.wait_event(ev_d2h[(nsteps - 1 - b) % NBUF])
 
         e2e_run(3)
         torch.cuda.synchronize()
@@ -660,13 +662,14 @@ def run_gpu(args):
         e1.record(stream)
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1) / ne
-        # the host copies of the last two steps' results (one per input set) are
+        # the host copies of the last NBUF steps' results (both input sets) are
         # the device path's outputs for those inputs, bit for bit
         xb = [torch.tensor(h, device=dev) for h in host_b]
         outs_b = sc.nsst_denoise_batch(xb, plan, sig, K, None)
         torch.cuda.synchronize()
         ref = [outs, outs_b]
-        same = all(torch.equal(pin_out[b][i], ref[b][i].cpu()) for b in range(2) for i in range(BATCH))
+        same = all(torch.equal(pin_out[k % NBUF][i], ref[k % 2][i].cpu())
+                   for k in range(ne - NBUF, ne) for i in range(BATCH))
         line['e2e'] = {'value': BATCH * world / (e2e_ms / 1000.0), 'unit': UNIT,
                        'h2d_bytes_per_step': BATCH * H * W * 4, 'd2h_bytes_per_step': BATCH * H * W * 4,
                        'ms_per_step': e2e_ms, 'pipelined': 'H2D / denoise / D2H of adjacent steps overlap',
@@ -741,12 +744,31 @@ def run_gpu(args):
         # the two paths may run different (tuned) kernels: the same math in a
         # different FP32 rounding order
         udiff = max(float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b)) for a, b in zip(uouts, pouts))
+        # each size's batch on its own (its plan, its images, one call): the sum
+        # is what the graph's per-size branches cost back to back
+        alone = {}
+        for pp, shp in zip(plans, counts):
+            sel = [i for i, x in enumerate(uxs) if tuple(x.shape) == shp]
+            bx, bo, bs = [uxs[i] for i in sel], [uouts[i] for i in sel], [usig[i] for i in sel]
+            for _ in range(2):
+                sc.nsst_denoise_batch(bx, pp, bs, K, None, outs=bo)
+            torch.cuda.synchronize()
+            at = 0.0
+            for _ in range(3):
+                flush.fill_(1.0)
+                e0.record(stream)
+                sc.nsst_denoise_batch(bx, pp, bs, K, None, outs=bo)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                at += e0.elapsed_time(e1)
+            alone['%dx%d' % shp] = at / 3
         ub = BATCH / (ut / nu / 1000.0)
         up = BATCH / (pt / 1000.0)
         line['uneven_b64'] = {'images_per_s': ub, 'ms_per_batch': ut / nu, 'megapixels': npx / 1e6,
                               'gigapixels_per_s': npx / (ut / nu / 1000.0) / 1e9,
                               'plain_images_per_s': up, 'plain_ms': pt, 'vs_plain': ub / up,
                               'plain_vs_batched_max_rel_l2': udiff, 'directional': uchoice,
+                              'sizes_alone_ms': alone, 'sum_of_sizes_alone_ms': sum(alone.values()),
                               'sizes': {'%dx%d' % k: v for k, v in counts.items()}}
         m.close()
         del plans, singles
