@@ -61,3 +61,29 @@ def test_autotune_picks_fastest_and_every_candidate_is_exact(built_lib, cuda, HW
                 first[mode] = outs
     shear.check_device()
     shear.select_directional(n, -1)
+
+
+@pytest.mark.parametrize('HW,n', [((512, 512), 3), ((768, 1024), 2), ((256, 384), 3)])
+def test_tma_staging_is_bit_identical_to_cp_async(built_lib, cuda, HW, n):
+    # the TMA-staged column kernels change how a column group reaches shared
+    # memory, not the arithmetic: each "-tma" candidate equals its cp.async
+    # twin bit for bit (hard and soft thresholds)
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300.synth import noisy_image
+    H, W = HW
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=n)
+    sc.nsst_scalars(shear, seed=100)
+    names = shear.directional_candidates()
+    pairs = [(names.index(t), names.index(t.replace('-tma', ''))) for t in names if '-tma' in t]
+    assert len(pairs) >= 6
+    xs = [torch.tensor(noisy_image(H, W, 20.0, s)[1].astype(np.float32), device=cuda) for s in range(n)]
+    for it, ic in pairs:
+        for mode in (0, 1):
+            got = []
+            for i in (it, ic):
+                shear.select_directional(n, i)
+                got.append([o.cpu() for o in sc.nsst_denoise_batch(xs, shear, [20.0] * n, K_DEMO, None, mode=mode)])
+            for a, b in zip(*got):
+                assert torch.equal(a, b), (names[it], names[ic], mode)
+    shear.check_device()
+    shear.select_directional(n, -1)
