@@ -104,7 +104,13 @@ __global__ void __launch_bounds__(RowTile<WH, RS>::T, RowTile<WH, RS>::MINB)
   // C2R (pre-processing in the first pass) with the threshold in the last pass
   // (both transforms in place on one buffer: every pass reads all of its
   // inputs, the pre-processing's mirrored ones included, before a barrier)
-  block_fft_hook_ip<WH, RS, T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshSt<RS>{A, th, mode});
+  bool kept = false;
+  block_fft_hook_ip<WH, RS, T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshStKept<RS>{A, th, mode, &kept});
+  // a tile whose coefficients all threshold to zero has a zero transform
+  if (!__syncthreads_or(kept)) {
+    store_zero_rows<WH, RS, T>(dst_base + job.dst + off);
+    return;
+  }
   // R2C of the thresholded rows, its last pass back to the padded row-major
   // layout; post-processing fused with a store along the rows
   block_fft_hook_ip<WH, RS, T, -1>(A, twWh, SmemLd<RS>{A}, SmemStRM<WH>{A});
@@ -163,15 +169,22 @@ __global__ void __launch_bounds__(RowTileP<WH, RS>::T, RowTileP<WH, RS>::MINB)
     const cpx2 O = cmulc_b(csub(xk, xmc), make_float2(t.x, t.y), make_float2(t.z, t.w));
     return {csub(E.re, O.im), cadd(E.im, O.re)};
   };
+  bool kept = false;
   auto thr_st = [&](int i, int p, cpx2 v) {
     v.re.x = apply_thresh(v.re.x, th, mode);
     v.re.y = apply_thresh(v.re.y, th, mode);
     v.im.x = apply_thresh(v.im.x, th, mode);
     v.im.y = apply_thresh(v.im.y, th, mode);
+    kept |= (v.re.x != 0.0f) | (v.re.y != 0.0f) | (v.im.x != 0.0f) | (v.im.y != 0.0f);
     D[i * NP + p] = v;
   };
   using Plan = typename RowPlanP<WH>::type;
   block_fft_hook_ip_plan<WH, NP, T, +1, Plan>(D, twWh4, ld, thr_st);
+  // a tile whose coefficients all threshold to zero has a zero transform
+  if (!__syncthreads_or(kept)) {
+    store_zero_rows<WH, RS, T>(dst_base + job.dst + off);
+    return;
+  }
   // R2C of the thresholded rows, the last pass back to the row-major layout
   auto ldd = [&](int i, int p) -> cpx2 { return D[i * NP + p]; };
   auto st_rm = [&](int i, int p, cpx2 v) {

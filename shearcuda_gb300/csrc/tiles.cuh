@@ -100,6 +100,22 @@ struct ThreshSt {
   }
 };
 
+// ThreshSt that also records whether this thread kept any nonzero value
+// (*kept, a thread-local flag; the caller reduces it over the block).
+template <int NSEQ>
+struct ThreshStKept {
+  float2* p;
+  float th;
+  int mode;
+  bool* kept;
+  __device__ __forceinline__ void operator()(int i, int s, float2 v) const {
+    v.x = apply_thresh(v.x, th, mode);
+    v.y = apply_thresh(v.y, th, mode);
+    *kept |= (v.x != 0.0f) | (v.y != 0.0f);
+    p[i * NSEQ + s] = v;
+  }
+};
+
 // FFT hooks (see block_fft_hook).
 template <int NSEQ>
 struct SmemLd {
@@ -157,6 +173,16 @@ __device__ __forceinline__ void store_rows_rm(float2* __restrict__ dst, const fl
     const int s = e / CH, c = e - s * CH;
     *reinterpret_cast<float4*>(dst + (size_t)s * WH + 2 * c) =
         *reinterpret_cast<const float4*>(P + s * (WH + 2) + 2 * c);
+  }
+}
+// RS rows of WH zero float2 (the packed R2C of all-zero rows), 16 bytes per
+// thread and step
+template <int WH, int RS, int T>
+__device__ __forceinline__ void store_zero_rows(float2* __restrict__ dst) {
+  constexpr int CH = WH / 2;
+  for (int e = threadIdx.x; e < RS * CH; e += T) {
+    const int s = e / CH, c = e - s * CH;
+    *reinterpret_cast<float4*>(dst + (size_t)s * WH + 2 * c) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 // packed-real post-processing of every index k (see r2c_post) fused with the

@@ -114,6 +114,25 @@ def test_denoise_matches_oracle_psnr(built_lib, cuda, HW, mode):
     assert rel_l2(out, ref) <= 1e-3
 
 
+@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('batch', [1, 4])
+def test_all_bands_thresholded_away(built_lib, cuda, mode, batch):
+    # thresholds above every coefficient: each row tile of every band
+    # thresholds to zero, so the row pass writes zero tiles without the
+    # forward transform; the result is the lowpass band's reconstruction,
+    # as in the oracle with the same thresholds
+    import shearcuda_gb300 as sc
+    clean, noisy32, _, sf, scal = _setup(512, 512)
+    shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 512, 512, batch=batch)
+    K = [0.0, 1e6, 1e6, 1e6, 1e6]
+    x = torch.tensor(noisy32, device=cuda)
+    outs = sc.nsst_denoise_batch([x] * batch, shear, [20.0] * batch, K, flat_scalars(scal), mode=mode)
+    ref, _ = nsst2d.denoise(noisy32.astype(np.float64), 20.0, K, scal, DCOMP, DSIZE,
+                            mode='hard' if mode == 0 else 'soft', shear_f=sf, nthreads=8)
+    for o in outs:
+        assert rel_l2(o.cpu().numpy().astype(np.float64), ref) <= 1e-5
+
+
 def test_fused_denoise_equals_materialised_chain(built_lib, cuda):
     # with the direct pyramid the fused pass runs the chain's kernels
     # (test_gpu_dct_pyramid.py covers the spectral pyramid)
