@@ -269,9 +269,22 @@ __global__ void __launch_bounds__(RowCfg<WH>::T) k_rows_backward(const RowJob* _
   fetch_rows_rm<WH, C::RS, C::T>(Cb, dst_base + job.dst + off);
   cp_async_wait_all();
   __syncthreads();
-  // coefficients c = C2R(Qc) (pre-processing in the first pass)
+  // coefficients c = C2R(Qc) (pre-processing in the first pass), noting
+  // whether any passes the threshold
   float2* const Xc = fft_hook_target<WH>(A, B);
-  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLdRM<WH>{A, twW}, SmemSt<C::RS>{Xc});
+  bool kept = false;
+  auto c_st = [&](int i, int sq, float2 c) {
+    kept |= (fabsf(c.x) > th) | (fabsf(c.y) > th);
+    Xc[i * C::RS + sq] = c;
+  };
+  block_fft_hook<WH, C::RS, C::T, +1>(A, B, twWh, C2RPreLdRM<WH>{A, twW}, c_st);
+  // no coefficient of the tile passes: the masked gradient, its transform and
+  // the tile's share of d loss / d t are zero
+  if (!__syncthreads_or(kept)) {
+    if (threadIdx.x == 0) partials[(size_t)job.th_index * pstride + (size_t)job.item * gridDim.x + blockIdx.x] = 0.0f;
+    store_zero_rows<WH, C::RS, C::T>(dst_base + job.dst + off);
+    return;
+  }
   // gradient g = C2R(Qg), masked by 1[|c| > t] in the last pass, which also
   // accumulates this thread's share of -sum g sign(c) 1[|c| > t] (soft)
   float2* const S = (Xc == A) ? B : A;
