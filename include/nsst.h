@@ -167,8 +167,9 @@ typedef struct nsst_tune_result {
   char name[NSST_TUNE_MAX_CANDIDATES][64];   /* "split/<analysis>/<rows>/<synthesis>" (analysis: level, level-pairs,
                                                 level-tma, level-pairs-tma or band; rows: rows8, rows8-pairs,
                                                 rows16-pairs; synthesis: synthesis, synthesis-pairs,
-                                                synthesis-tma or synthesis-pairs-tma; "-tma": column groups
-                                                staged by TMA) or "fused/cluster<C>" */
+                                                synthesis-tma, synthesis-pairs-tma or synthesis-regs; "-tma":
+                                                column groups staged by TMA; "-regs": TMA-staged with the band
+                                                sum in registers) or "fused/cluster<C>" */
   float ms[NSST_TUNE_MAX_CANDIDATES];        /* median ms of one directional-stage pass over n images */
   int direct_support[NSST_MAX_LEVELS];       /* per level, px (0: no window below the image size) */
   double direct_err[NSST_MAX_LEVELS];        /* per level: the worst band's truncation error at that window */

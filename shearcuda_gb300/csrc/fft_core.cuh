@@ -812,6 +812,98 @@ __device__ __forceinline__ void fft_hook_ip_passes(E* buf, const float2* __restr
   fft_hook_ip_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, st, hook, RadixList<Rest...>{});
 }
 
+// ---------------------------------------------------------------------------
+// Transforms whose last pass accumulates into registers: acc(it, r, row, s, v)
+// receives output (row, s) of the thread's (it, r) slot instead of a store.
+// Every thread owns the same (row, s) slots on every call, so a running sum
+// over many transforms (the band sum of a synthesis) can stay in registers.
+// ---------------------------------------------------------------------------
+template <class RL>
+struct LastRadix;
+template <int R>
+struct LastRadix<RadixList<R>> {
+  static constexpr int value = R;
+};
+template <int R, int R2, int... Rs>
+struct LastRadix<RadixList<R, R2, Rs...>> {
+  static constexpr int value = LastRadix<RadixList<R2, Rs...>>::value;
+};
+
+template <int... Rs>
+__host__ __device__ constexpr int plan_product(RadixList<Rs...>) {
+  return (1 * ... * Rs);
+}
+
+// The last pass of an in-place FFT whose outputs go to acc(it, r, row, s, v)
+// (registers) instead of the buffer; see stockham_ip for the pass itself.
+template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, class Rd, class Acc>
+__device__ __forceinline__ void stockham_last_acc(const Rd& rd, Acc& acc, const float2* __restrict__ tw) {
+  constexpr int NB = N / R;
+  constexpr int TOTAL = NB * NSEQ;
+  constexpr int IPT = TOTAL / T;
+  constexpr int STEP = N / (NS * R);
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    const int s = w % NSEQ, j = w / NSEQ;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = rd(swz_row<NSEQ, SWZ_IN>(j + r * NB), s);
+    const int k = j % NS;
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        const float2 t = __ldg(&tw[r * k * STEP]);
+        v[r] = DIR < 0 ? cmul(v[r], t) : cmulc(v[r], t);
+      }
+    }
+    Dft<R, DIR>::run(v);
+    const int base = (j / NS) * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) acc(it, r, base + r * NS, s, v[r]);
+  }
+  __syncthreads();
+}
+
+// output row of accumulator (it, r) in the last pass (see stockham_last_acc)
+template <int N, int NSEQ, int T, int R>
+__device__ __forceinline__ int last_pass_row(int it, int r) {
+  constexpr int NS = N / R;
+  const int w = threadIdx.x + it * T;
+  const int j = w / NSEQ;
+  return (j / NS) * NS * R + (j % NS) + r * NS;
+}
+
+// The passes of an in-place FFT of NSEQ sequences in buf whose first pass
+// reads its inputs through ld (then calls hook, once every thread has read
+// them) and whose last pass, entered after pre_last(), accumulates through
+// acc (stockham_last_acc).  At least two passes.
+template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Ld, class Hook, class Pre, class Acc, int R,
+          int... Rest>
+__device__ __forceinline__ void fft_ld_acc_passes(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                  const Hook& hook, const Pre& pre_last, Acc& acc,
+                                                  RadixList<R, Rest...>) {
+  static_assert(NS > 1 || sizeof...(Rest) > 0, "at least two passes");
+  auto rd = [&](int row, int s) -> float2 {
+    if constexpr (NS == 1)
+      return ld(row, s);
+    else
+      return buf[row * NSEQ + s];
+  };
+  if constexpr (sizeof...(Rest) == 0) {
+    pre_last();
+    stockham_last_acc<N, NSEQ, T, R, NS, DIR, SWZ_IN>(rd, acc, tw);
+  } else {
+    constexpr int SWZ_OUT = (NS == 1 && R % 2 == 0) ? R : 0;
+    auto wr = [&](int row, int s, float2 v) { buf[row * NSEQ + s] = v; };
+    if constexpr (NS == 1)
+      stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT, decltype(rd), decltype(wr), Hook>(rd, wr, tw, hook);
+    else
+      stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+    fft_ld_acc_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, ld, hook, pre_last, acc, RadixList<Rest...>{});
+  }
+}
+
 // after_first_read: called once the first pass has read all of its inputs
 // through ld (e.g. to start refilling the buffer ld reads from).  buf holds
 // float2 (NSEQ sequences) or float4 (2 NSEQ sequences, two per element).

@@ -109,7 +109,8 @@ inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
 enum class RowOp { Fwd, Inv, Thresh, Backward };
 // AnalysisLevel: one job per level (all its bands); *Pairs: the same kernels on
 // split-complex column pairs, with twH pointing to the broadcast twiddle table
-enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis, AnalysisLevelPairs, SynthesisPairs };
+// SynthesisRegs: the synthesis with the band sum in registers (TMA only)
+enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis, AnalysisLevelPairs, SynthesisPairs, SynthesisRegs };
 
 bool row_len_supported(int wh);
 bool col_len_supported(int h);

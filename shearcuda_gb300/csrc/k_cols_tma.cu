@@ -281,6 +281,103 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
   tma.drain(err);
 }
 
+// Synthesis with the band sum in registers: the last pass of each band's
+// column FFT accumulates conj(W_k) .* X into the thread's own outputs (the
+// same (row, column) slots for every band), with W_k's column group staged
+// by TMA next to the band's, so the sum needs no shared-memory plane and the
+// spectrum no global load.  Shared memory: the transform A, the band's
+// column group P, the spectrum's column group Wc, the DC column D.  Two
+// mbarriers: P is refilled once the first pass has read it, Wc once the last
+// pass has.  Threads per CTA: RaccCfg (every thread owns the same number of
+// last-pass outputs).
+template <int H>
+struct RaccCfg {
+  using Plan = typename FftPlan<H>::type;
+  static constexpr int CS = ColCfg<H>::CS;
+  static constexpr int RL = LastRadix<Plan>::value;
+  static constexpr int TOTAL_LAST = (H / RL) * CS;
+  // a thread holds IPT * RL sums: 8 at 512 rows (512 threads, 64 registers,
+  // two CTAs per SM), 16 elsewhere
+  static constexpr int T = H == 2048 ? 512 : H == 1024 ? 256 : H == 768 || H == 384 ? 192 : H == 512 ? 512 : TOTAL_LAST;
+  static constexpr int IPT = TOTAL_LAST / T;
+  static constexpr int MINB = H == 2048 ? 1 : H <= 256 ? 3 : 2;  // shared memory: one CTA per SM at 2048 rows
+  static_assert(TOTAL_LAST % T == 0, "every thread owns the same last-pass outputs");
+  static constexpr size_t smem() { return (3 * (size_t)H * CS + H) * sizeof(float2) + 16; }
+};
+
+template <int H>
+__global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
+    k_band_synthesis_racc(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
+                          int WH, float2* dst_base, const float2* __restrict__ spec_base, int spec_row0,
+                          size_t band_stride, const float2* __restrict__ twH, int* err) {
+  using C = RaccCfg<H>;
+  constexpr int CS = C::CS, T = C::T, RL = C::RL, IPT = C::IPT;
+  extern __shared__ __align__(1024) float2 tsm[];
+  float2* A = tsm;           // transform, in place
+  float2* P = A + H * CS;    // the band's column group [row][column]
+  float2* Wc = P + H * CS;   // the band's spectrum column group [row][column]
+  float2* D = Wc + H * CS;   // column 0 of the band's transform
+  const uint32_t bars = smem_u32(D + H);
+  const ColJob job = jobs[blockIdx.y];
+  if (job.item >= n_active) return;
+  const int col0 = blockIdx.x * CS;
+  const bool dc = col0 == 0;
+  const int band_rows = (int)(band_stride / WH);
+  const int brow = (int)(job.src / WH), srow = spec_row0 + (int)(job.spec / WH);
+  ColTma<H, CS> tp{bars, col0}, tw{bars + 8, col0};
+  if (threadIdx.x == 0 && job.nbands > 0) {
+    tp.init();
+    tw.init();
+    tp.expect(1);
+    tp.load(&amap, P, brow);
+    tw.expect(1);
+    tw.load(&amap, Wc, srow);
+  }
+  __syncthreads();  // the mbarriers are initialised before any thread waits on them
+  float2 acc[IPT][RL];
+#pragma unroll
+  for (int it = 0; it < IPT; it++)
+#pragma unroll
+    for (int r = 0; r < RL; r++) acc[it][r] = make_float2(0.0f, 0.0f);
+  for (int k = 0; k < job.nbands; k++) {
+    tp.wait(err);
+    // the first pass has read band k from P: band k + 1 may come in
+    auto next = [&]() {
+      if (threadIdx.x == 0 && tp.ok && k + 1 < job.nbands) tp.refill(&amap, P, brow + (k + 1) * band_rows);
+    };
+    auto spec_ready = [&]() { tw.wait(err); };
+    auto accf = [&](int it, int r, int row, int s, float2 z) {
+      acc[it][r] = cadd(acc[it][r], cmulc(z, Wc[row * CS + s]));
+      if (dc && s == 0) D[row] = z;
+    };
+    fft_ld_acc_passes<H, CS, T, -1, 1, 0>(A, twH, SmemLd<CS>{P}, next, spec_ready, accf, typename C::Plan{});
+    // every thread has read Wc (the last pass ends with a barrier)
+    if (threadIdx.x == 0 && tw.ok && k + 1 < job.nbands) tw.refill(&amap, Wc, srow + (k + 1) * band_rows);
+    if (dc && threadIdx.x % CS == 0) {  // + conj(M[u] X[-u]) on the packed DC/Nyquist column
+      const float2* m0 = spec_base + job.m0 + (size_t)k * H;
+#pragma unroll
+      for (int it = 0; it < IPT; it++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const int row = last_pass_row<H, CS, T, RL>(it, r);
+          acc[it][r] = cadd(acc[it][r], cconj(cmul(__ldg(&m0[row]), D[(H - row) % H])));
+        }
+    }
+  }
+  // the level's band sum: one column IFFT, stored by its last pass
+  {
+    const int s = threadIdx.x % CS;
+#pragma unroll
+    for (int it = 0; it < IPT; it++)
+#pragma unroll
+      for (int r = 0; r < RL; r++) A[last_pass_row<H, CS, T, RL>(it, r) * CS + s] = acc[it][r];
+  }
+  __syncthreads();
+  block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
+  tp.drain(err);
+  tw.drain(err);
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -304,6 +401,7 @@ cudaError_t prepare_cols_tma(int H) {
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_tma<n>, SynCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_analysis_ml_p_tma<n>, AnaCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_p_tma<n>, SynCfg<n>::smem() + kBarBytes); \
+    if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_racc<n>, RaccCfg<n>::smem());              \
     return e;                                                                             \
   }
     NSST_COL_SIZES(CASE)
@@ -319,7 +417,7 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
   const int WH = W / 2;
   if (njobs == 0) return cudaSuccess;
   if (op != ColOp::AnalysisLevel && op != ColOp::Synthesis && op != ColOp::AnalysisLevelPairs &&
-      op != ColOp::SynthesisPairs)
+      op != ColOp::SynthesisPairs && op != ColOp::SynthesisRegs)
     return cudaErrorInvalidValue;
   if (band_stride % (size_t)WH != 0 || spec_row0 > (size_t)INT32_MAX) return cudaErrorInvalidValue;
   count_launch();
@@ -339,6 +437,9 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
     else if (op == ColOp::Synthesis)                                                                               \
       k_band_synthesis_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,           \
                                                               band_stride, twH, err);                              \
+    else if (op == ColOp::SynthesisRegs)                                                                           \
+      k_band_synthesis_racc<n><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(m, jobs, n_active, WH, dst_base,   \
+                                                                              spec_base, sr, band_stride, twH, err); \
     else                                                                                                           \
       k_band_synthesis_p_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,         \
                                                                 band_stride, twH, err);                            \

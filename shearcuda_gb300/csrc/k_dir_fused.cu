@@ -82,22 +82,6 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float2 v) {
   asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
 }
 // ------------------------------------------------------------ configuration
-template <class RL>
-struct LastRadix;
-template <int R>
-struct LastRadix<RadixList<R>> {
-  static constexpr int value = R;
-};
-template <int R, int R2, int... Rs>
-struct LastRadix<RadixList<R, R2, Rs...>> {
-  static constexpr int value = LastRadix<RadixList<R2, Rs...>>::value;
-};
-
-template <int... Rs>
-__host__ __device__ constexpr int plan_product(RadixList<Rs...>) {
-  return (1 * ... * Rs);
-}
-
 // H rows, WH packed columns (W/2), CL CTAs per cluster, T threads per CTA;
 // the row transforms use radix plan RowPlan (chosen so that every pass gives
 // every thread work).
@@ -147,37 +131,6 @@ struct SmemStRP {  // element (i, s) -> row s, column i
   __device__ __forceinline__ void operator()(int i, int s, float2 v) const { p[s * RP + i] = v; }
 };
 
-// The last pass of an in-place FFT whose outputs go to acc(it, r, row, s, v)
-// (registers) instead of the buffer; see stockham_ip for the pass itself.
-template <int N, int NSEQ, int T, int R, int NS, int DIR, int SWZ_IN, class Rd, class Acc>
-__device__ __forceinline__ void stockham_last_acc(const Rd& rd, Acc& acc, const float2* __restrict__ tw) {
-  constexpr int NB = N / R;
-  constexpr int TOTAL = NB * NSEQ;
-  constexpr int IPT = TOTAL / T;
-  constexpr int STEP = N / (NS * R);
-#pragma unroll
-  for (int it = 0; it < IPT; it++) {
-    const int w = threadIdx.x + it * T;
-    const int s = w % NSEQ, j = w / NSEQ;
-    float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) v[r] = rd(swz_row<NSEQ, SWZ_IN>(j + r * NB), s);
-    const int k = j % NS;
-    if (NS > 1) {
-#pragma unroll
-      for (int r = 1; r < R; r++) {
-        const float2 t = __ldg(&tw[r * k * STEP]);
-        v[r] = DIR < 0 ? cmul(v[r], t) : cmulc(v[r], t);
-      }
-    }
-    Dft<R, DIR>::run(v);
-    const int base = (j / NS) * NS * R + k;
-#pragma unroll
-    for (int r = 0; r < R; r++) acc(it, r, base + r * NS, s, v[r]);
-  }
-  __syncthreads();
-}
-
 template <int N, int NSEQ, int T, int DIR, int NS, int SWZ_IN, class Acc, int R>
 __device__ __forceinline__ void fft_ip_acc_passes(float2* buf, const float2* __restrict__ tw, Acc& acc,
                                                   RadixList<R>) {
@@ -193,15 +146,6 @@ __device__ __forceinline__ void fft_ip_acc_passes(float2* buf, const float2* __r
   stockham_ip<N, NSEQ, T, R, NS, DIR, SWZ_IN, SWZ_OUT>(rd, wr, tw);
   fft_ip_acc_passes<N, NSEQ, T, DIR, NS * R, SWZ_OUT>(buf, tw, acc, RadixList<R2, Rest...>{});
 }
-// output row of accumulator (it, r) in the last pass (see stockham_last_acc)
-template <int N, int NSEQ, int T, int R>
-__device__ __forceinline__ int last_pass_row(int it, int r) {
-  constexpr int NS = N / R;
-  const int w = threadIdx.x + it * T;
-  const int j = w / NSEQ;
-  return (j / NS) * NS * R + (j % NS) + r * NS;
-}
-
 // ------------------------------------------------------------------ kernel
 template <int H, int WH, int CL, int T, int MINB, class RowPlan, class ColPlan>
 __global__ void __launch_bounds__(T, MINB)

@@ -33,6 +33,7 @@ struct DirChoice {
   bool packed = false;  // row pass on split-complex row pairs (FP32x2 arithmetic)
   bool cols_packed = false;  // analysis (per level) and synthesis on split-complex column pairs
   bool cols_tma = false;     // analysis (per level) and synthesis with column groups staged by TMA
+  bool syn_regs = false;     // with cols_tma: the synthesis keeps the band sum in registers
 };
 
 // autotuner buckets of the batch size n: bucket b holds 2^b <= n < 2^(b+1)
@@ -323,14 +324,17 @@ nsst_status check_spectral_n(const nsst_plan* p, int n, const float* const* a, c
 // with the tuned split settings where the autotuner chose a split candidate;
 // else (auto) the tuned choice of n's bucket; else the untuned default: the
 // split kernels with the column groups staged by TMA (measured faster than
-// the cp.async forms at every size, 2-11 %), the per-level analysis where its
-// grid fills the GPU twice and the per-band analysis below, and the row pass
-// on two tiles of row pairs at <= 192 points per row (faster there, slower at
-// 256 and up).  The fused kernel measured slower than these at every size.
+// the cp.async forms at every size, 2-11 %) and the band sum of the synthesis
+// in registers (faster again at every size, 12-28 %), the per-level analysis
+// where its grid fills the GPU twice and the per-band analysis below, and the
+// row pass on two tiles of row pairs at <= 192 points per row (faster there,
+// slower at 256 and up).  The fused kernel measured slower than these at
+// every size.
 DirChoice dir_choice(const nsst_plan* p, int n) {
   if (p->forcing) return p->forced;
   DirChoice def;
   def.cols_tma = p->cols_tma_ok;
+  def.syn_regs = p->cols_tma_ok;
   if (p->WH <= 192 && p->H % (2 * row_tile(p->WH)) == 0) {
     def.packed = true;
     def.row_tile = 2;
@@ -1092,7 +1096,7 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
-  const ColOp syn = c.cols_packed ? ColOp::SynthesisPairs : ColOp::Synthesis;
+  const ColOp syn = c.cols_packed ? ColOp::SynthesisPairs : (tma && c.syn_regs) ? ColOp::SynthesisRegs : ColOp::Synthesis;
   const float2* twc = c.cols_packed ? (const float2*)p->twH4 : p->twH;
   if (tma)
     NSST_CUDA(launch_cols_tma(syn, p->cols_tmap, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, p->spec,
@@ -1662,6 +1666,20 @@ std::vector<std::pair<DirChoice, std::string>> dir_candidates(const nsst_plan* p
                               std::to_string(rs * r[0]) + (d.packed ? "-pairs" : "") + "/synthesis" + cols});
         }
   }
+  // the TMA synthesis with the band sum in registers
+  if (p->cols_tma_ok)
+    for (int ana : {1, 2})
+      for (const auto& r : rows) {
+        DirChoice d;
+        d.ana = ana;
+        d.row_tile = r[0];
+        d.packed = r[1] != 0;
+        d.cols_tma = true;
+        d.syn_regs = true;
+        if (p->H % (rs * r[0]) != 0) continue;
+        c.push_back({d, std::string("split/") + (ana == 1 ? "level-tma" : "band") + "/rows" +
+                            std::to_string(rs * r[0]) + (d.packed ? "-pairs" : "") + "/synthesis-regs"});
+      }
   if (p->fused_ok) {
     DirChoice d;
     d.fused = true;

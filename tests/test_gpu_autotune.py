@@ -67,15 +67,19 @@ def test_autotune_picks_fastest_and_every_candidate_is_exact(built_lib, cuda, HW
 def test_tma_staging_is_bit_identical_to_cp_async(built_lib, cuda, HW, n):
     # the TMA-staged column kernels change how a column group reaches shared
     # memory, not the arithmetic: each "-tma" candidate equals its cp.async
-    # twin bit for bit (hard and soft thresholds)
+    # twin bit for bit (hard and soft thresholds); so does the synthesis with
+    # the band sum in registers ("-regs") against the one summing in shared
+    # memory
     import shearcuda_gb300 as sc
     from shearcuda_gb300.synth import noisy_image
     H, W = HW
     shear = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=n)
     sc.nsst_scalars(shear, seed=100)
     names = shear.directional_candidates()
-    pairs = [(names.index(t), names.index(t.replace('-tma', ''))) for t in names if '-tma' in t]
-    assert len(pairs) >= 6
+    pairs = [(names.index(t), names.index(t.replace('-tma', ''))) for t in names if t.endswith('-tma')]
+    pairs += [(names.index(t), names.index(t.replace('synthesis-regs', 'synthesis-tma'))) for t in names
+              if t.endswith('synthesis-regs')]
+    assert len(pairs) >= 12
     xs = [torch.tensor(noisy_image(H, W, 20.0, s)[1].astype(np.float32), device=cuda) for s in range(n)]
     for it, ic in pairs:
         for mode in (0, 1):
