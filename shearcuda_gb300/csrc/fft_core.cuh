@@ -904,6 +904,104 @@ __device__ __forceinline__ void fft_ld_acc_passes(float2* buf, const float2* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// An inverse transform, an elementwise op on its output, and a forward
+// transform with the same radix plan, where the plan's first and last radix
+// are equal: the inverse transform's last pass leaves each thread exactly the
+// values the forward transform's first pass needs (output r of butterfly j is
+// index j + r N/R, the first pass's input r of butterfly j), so the turn from
+// one transform to the other happens in registers, without a shared-memory
+// round trip or a barrier.  op(v, flag) maps each value and may set a
+// thread-local flag; the turn returns the block-wide OR of the flags (false:
+// the forward transform has not run and buf holds the inverse transform's
+// next-to-last pass).
+// ---------------------------------------------------------------------------
+template <class RL>
+struct FirstRadix;
+template <int R, int... Rs>
+struct FirstRadix<RadixList<R, Rs...>> {
+  static constexpr int value = R;
+};
+template <class RL>
+struct TailRadices;
+template <int R, int... Rs>
+struct TailRadices<RadixList<R, Rs...>> {
+  using type = RadixList<Rs...>;
+};
+
+// the turn pass: inverse last pass (radix R, NS = N / R), op, forward first pass
+template <int N, int NSEQ, int T, int R, int SWZ_IN, int SWZ_OUT, class Op>
+__device__ __forceinline__ bool stockham_turn(float2* buf, const float2* __restrict__ tw, const Op& op) {
+  constexpr int NB = N / R;
+  constexpr int TOTAL = NB * NSEQ;
+  constexpr int IPT = (TOTAL + T - 1) / T;
+  float2 v[IPT][R];
+  bool flag = false;
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      const int s = w % NSEQ, j = w / NSEQ;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[it][r] = buf[swz_row<NSEQ, SWZ_IN>(j + r * NB) * NSEQ + s];
+#pragma unroll
+      for (int r = 1; r < R; r++) v[it][r] = tw_mul<+1>(v[it][r], tw, r * j);  // NS = NB: k = j, STEP = 1
+      Dft<R, +1>::run(v[it]);
+#pragma unroll
+      for (int r = 0; r < R; r++) v[it][r] = op(v[it][r], flag);
+      Dft<R, -1>::run(v[it]);  // the forward first pass: no twiddles
+    }
+  }
+  if (!__syncthreads_or(flag)) return false;  // every thread has read its inputs
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    if (TOTAL % T == 0 || w < TOTAL) {
+      const int s = w % NSEQ, j = w / NSEQ;
+#pragma unroll
+      for (int r = 0; r < R; r++) buf[swz_row<NSEQ, SWZ_OUT>(j * R + r) * NSEQ + s] = v[it][r];
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+template <int N, int NSEQ, int T, int NS, int SWZ_IN, class Plan, class Ld, class Op, int R, int... Rest>
+__device__ __forceinline__ bool fft_inv_turn_passes(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                    const Op& op, RadixList<R, Rest...>) {
+  if constexpr (sizeof...(Rest) == 0) {
+    static_assert(R == FirstRadix<Plan>::value, "the plan's first and last radix must be equal");
+    constexpr int SWZ_OUT = R % 2 == 0 ? R : 0;  // the forward transform's first pass (not its last)
+    return stockham_turn<N, NSEQ, T, R, SWZ_IN, SWZ_OUT>(buf, tw, op);
+  } else {
+    constexpr int SWZ_OUT = (NS == 1 && R % 2 == 0) ? R : 0;
+    auto rd = [&](int row, int s) -> float2 {
+      if constexpr (NS == 1)
+        return ld(row, s);
+      else
+        return buf[row * NSEQ + s];
+    };
+    auto wr = [&](int row, int s, float2 v) { buf[row * NSEQ + s] = v; };
+    stockham_ip<N, NSEQ, T, R, NS, +1, SWZ_IN, SWZ_OUT>(rd, wr, tw);
+    return fft_inv_turn_passes<N, NSEQ, T, NS * R, SWZ_OUT, Plan>(buf, tw, ld, op, RadixList<Rest...>{});
+  }
+}
+
+// inverse FFT (first pass reading through ld) -> op -> forward FFT (last pass
+// storing through st), in place on buf; false (and no forward transform)
+// when no thread set its flag
+template <int N, int NSEQ, int T, class Ld, class Op, class St>
+__device__ __forceinline__ bool block_fft_inv_op_fwd(float2* buf, const float2* __restrict__ tw, const Ld& ld,
+                                                     const Op& op, const St& st) {
+  using Plan = typename FftPlan<N>::type;
+  constexpr int RF = FirstRadix<Plan>::value;
+  if (!fft_inv_turn_passes<N, NSEQ, T, 1, 0, Plan>(buf, tw, ld, op, Plan{})) return false;
+  auto rd = [&](int row, int s) -> float2 { return buf[row * NSEQ + s]; };  // (the passes read buf)
+  fft_hook_ip_passes<N, NSEQ, T, -1, RF, RF % 2 == 0 ? RF : 0>(buf, tw, rd, st, NoHook{},
+                                                                typename TailRadices<Plan>::type{});
+  return true;
+}
+
 // after_first_read: called once the first pass has read all of its inputs
 // through ld (e.g. to start refilling the buffer ld reads from).  buf holds
 // float2 (NSEQ sequences) or float4 (2 NSEQ sequences, two per element).

@@ -101,19 +101,34 @@ __global__ void __launch_bounds__(RowTile<WH, RS>::T, RowTile<WH, RS>::MINB)
   fetch_rows_rm<WH, RS, T>(A, src_base + job.src + off);
   cp_async_wait_all();
   __syncthreads();
-  // C2R (pre-processing in the first pass) with the threshold in the last pass
-  // (both transforms in place on one buffer: every pass reads all of its
-  // inputs, the pre-processing's mirrored ones included, before a barrier)
-  bool kept = false;
-  block_fft_hook_ip<WH, RS, T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshStKept<RS>{A, th, mode, &kept});
-  // a tile whose coefficients all threshold to zero has a zero transform
-  if (!__syncthreads_or(kept)) {
-    store_zero_rows<WH, RS, T>(dst_base + job.dst + off);
-    return;
+  // C2R (pre-processing in the first pass) -> threshold -> R2C, in place on
+  // one buffer (every pass reads all of its inputs, the pre-processing's
+  // mirrored ones included, before a barrier); the R2C's last pass goes back
+  // to the padded row-major layout, the post-processing is fused with a store
+  // along the rows.  A tile whose coefficients all threshold to zero has a
+  // zero transform: it stores zero rows instead.
+  auto thresh = [&](float2 v, bool& kept) {
+    v.x = apply_thresh(v.x, th, mode);
+    v.y = apply_thresh(v.y, th, mode);
+    kept |= (v.x != 0.0f) | (v.y != 0.0f);
+    return v;
+  };
+  using Plan = typename FftPlan<WH>::type;
+  if constexpr (FirstRadix<Plan>::value == LastRadix<Plan>::value) {
+    // the turn from the C2R to the R2C in registers
+    if (!block_fft_inv_op_fwd<WH, RS, T>(A, twWh, C2RPreLdRM<WH>{A, twW}, thresh, SmemStRM<WH>{A})) {
+      store_zero_rows<WH, RS, T>(dst_base + job.dst + off);
+      return;
+    }
+  } else {
+    bool kept = false;
+    block_fft_hook_ip<WH, RS, T, +1>(A, twWh, C2RPreLdRM<WH>{A, twW}, ThreshStKept<RS>{A, th, mode, &kept});
+    if (!__syncthreads_or(kept)) {
+      store_zero_rows<WH, RS, T>(dst_base + job.dst + off);
+      return;
+    }
+    block_fft_hook_ip<WH, RS, T, -1>(A, twWh, SmemLd<RS>{A}, SmemStRM<WH>{A});
   }
-  // R2C of the thresholded rows, its last pass back to the padded row-major
-  // layout; post-processing fused with a store along the rows
-  block_fft_hook_ip<WH, RS, T, -1>(A, twWh, SmemLd<RS>{A}, SmemStRM<WH>{A});
   r2c_post_store_rm<WH, RS, T>(dst_base + job.dst + off, A, twW);
 }
 
