@@ -109,8 +109,19 @@ inline void fill_taps(AtrousTaps<0>& t, const float*) { t.ncols = 0; }
 enum class RowOp { Fwd, Inv, Thresh, Backward };
 // AnalysisLevel: one job per level (all its bands); *Pairs: the same kernels on
 // split-complex column pairs, with twH pointing to the broadcast twiddle table
-// SynthesisRegs: the synthesis with the band sum in registers (TMA only)
-enum class ColOp { Fwd, Inv, Analysis, AnalysisLevel, Synthesis, AnalysisLevelPairs, SynthesisPairs, SynthesisRegs };
+// SynthesisRegs: the synthesis with the band sum in registers (TMA only);
+// SynthesisRegsDct2: the same, the sum leaving as its column DCT-II
+enum class ColOp {
+  Fwd,
+  Inv,
+  Analysis,
+  AnalysisLevel,
+  Synthesis,
+  AnalysisLevelPairs,
+  SynthesisPairs,
+  SynthesisRegs,
+  SynthesisRegsDct2
+};
 
 bool row_len_supported(int wh);
 bool col_len_supported(int h);
@@ -166,7 +177,7 @@ bool cols_tma_supported(int H, int WH);
 cudaError_t prepare_cols_tma(int H);
 cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int njobs, int n_active, int H, int W,
                             float2* dst_base, const float2* spec_base, size_t spec_row0, size_t band_stride,
-                            const float2* twH, int* err, cudaStream_t st);
+                            const float2* twH, int* err, cudaStream_t st, const float2* wd = nullptr);
 cudaError_t launch_dir_fused(const void* ymap, const FusedJob* jobs, int njobs, int n_active, int nclusters, int H,
                              int W, float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                              const float2* twWh, const float2* twW, const float* thr, int mode, int* err,

@@ -305,11 +305,16 @@ struct RaccCfg {
   static constexpr size_t smem() { return (3 * (size_t)H * CS + H) * sizeof(float2) + 16; }
 };
 
-template <int H>
+// DCT2: the band sum leaves as its DCT-II down the columns (what the spectral
+// pyramid's synthesis takes next, k_dct.cu's kDct2 column pass): the column
+// IFFT's last pass stores in the DCT-II's input order, a forward FFT and the
+// DCT-II post-processing (wd) follow in shared memory.
+template <int H, bool DCT2>
 __global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
     k_band_synthesis_racc(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                           int WH, float2* dst_base, const float2* __restrict__ spec_base, int spec_row0,
-                          size_t band_stride, const float2* __restrict__ twH, int* err) {
+                          size_t band_stride, const float2* __restrict__ twH, const float2* __restrict__ wd,
+                          int* err) {
   using C = RaccCfg<H>;
   constexpr int CS = C::CS, T = C::T, RL = C::RL, IPT = C::IPT;
   extern __shared__ __align__(1024) float2 tsm[];
@@ -373,7 +378,15 @@ __global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
       for (int r = 0; r < RL; r++) A[last_pass_row<H, CS, T, RL>(it, r) * CS + s] = acc[it][r];
   }
   __syncthreads();
-  block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
+  if constexpr (DCT2) {
+    // row r of the IFFT goes to element r / 2 (r even) or H - 1 - (r - 1) / 2 (r odd) of the DCT-II's FFT input
+    auto st_dct = [&](int i, int sq, float2 v) { A[((i & 1) ? H - 1 - (i >> 1) : (i >> 1)) * CS + sq] = v; };
+    block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, st_dct);
+    block_fft_hook_ip<H, CS, T, -1>(A, twH, SmemLd<CS>{A}, SmemSt<CS>{A});
+    dct2_cols_store<H, T>(A, dst_base + job.dst + col0, WH, wd);
+  } else {
+    block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
+  }
   tp.drain(err);
   tw.drain(err);
 }
@@ -401,7 +414,8 @@ cudaError_t prepare_cols_tma(int H) {
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_tma<n>, SynCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_analysis_ml_p_tma<n>, AnaCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_p_tma<n>, SynCfg<n>::smem() + kBarBytes); \
-    if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_racc<n>, RaccCfg<n>::smem());              \
+    if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_racc<n, false>, RaccCfg<n>::smem());       \
+    if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_racc<n, true>, RaccCfg<n>::smem());        \
     return e;                                                                             \
   }
     NSST_COL_SIZES(CASE)
@@ -413,12 +427,13 @@ cudaError_t prepare_cols_tma(int H) {
 
 cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int njobs, int n_active, int H, int W,
                             float2* dst_base, const float2* spec_base, size_t spec_row0, size_t band_stride,
-                            const float2* twH, int* err, cudaStream_t st) {
+                            const float2* twH, int* err, cudaStream_t st, const float2* wd) {
   const int WH = W / 2;
   if (njobs == 0) return cudaSuccess;
   if (op != ColOp::AnalysisLevel && op != ColOp::Synthesis && op != ColOp::AnalysisLevelPairs &&
-      op != ColOp::SynthesisPairs && op != ColOp::SynthesisRegs)
+      op != ColOp::SynthesisPairs && op != ColOp::SynthesisRegs && op != ColOp::SynthesisRegsDct2)
     return cudaErrorInvalidValue;
+  if (op == ColOp::SynthesisRegsDct2 && !wd) return cudaErrorInvalidValue;
   if (band_stride % (size_t)WH != 0 || spec_row0 > (size_t)INT32_MAX) return cudaErrorInvalidValue;
   count_launch();
   const CUtensorMap& m = *reinterpret_cast<const CUtensorMap*>(amap);
@@ -438,8 +453,11 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
       k_band_synthesis_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,           \
                                                               band_stride, twH, err);                              \
     else if (op == ColOp::SynthesisRegs)                                                                           \
-      k_band_synthesis_racc<n><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(m, jobs, n_active, WH, dst_base,   \
-                                                                              spec_base, sr, band_stride, twH, err); \
+      k_band_synthesis_racc<n, false><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                            \
+          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err);                              \
+    else if (op == ColOp::SynthesisRegsDct2)                                                                       \
+      k_band_synthesis_racc<n, true><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                             \
+          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err);                              \
     else                                                                                                           \
       k_band_synthesis_p_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,         \
                                                                 band_stride, twH, err);                            \

@@ -307,19 +307,6 @@ __global__ void __launch_bounds__(RowCfg<WH>::T, DctMinB<RowCfg<WH>::T>::value)
 // ---------------------------------------------------------------------------
 // Column kernels, grid = (WH / CS, jobs): CS columns of a packed H x WH array.
 // ---------------------------------------------------------------------------
-// DCT-II post-processing of the FFT V (dense [row][column] in A):
-// C[k] = (wd[k] V[k] + conj(wd[k]) V[H-k]) / 2, stored down the columns
-template <int H>
-__device__ __forceinline__ void dct2_cols_store(const float2* A, float2* dst, int WH, const float2* __restrict__ wd) {
-  using C = ColCfg<H>;
-  for (int e = threadIdx.x; e < H * C::CS; e += C::T) {
-    const int s = e % C::CS, k = e / C::CS;
-    const float2 w = __ldg(&wd[k]);
-    const float2 a = A[k * C::CS + s], b = A[((H - k) % H) * C::CS + s];
-    dst[(size_t)k * WH + s] = cscale(cadd(cmul(w, a), cmulc(b, w)), 0.5f);
-  }
-}
-
 // kDct2: DCT-II; kDct3: DCT-III; kDctAna: DCT-III then the forward FFT;
 // kDctThresh: DCT-III, the threshold (th, tmode) of both real columns of each
 // element, DCT-II (the DCT-II input order undoes the DCT-III output order, so
@@ -342,7 +329,7 @@ __device__ __forceinline__ void dct_cols_body(const float2* src, float2* dst, in
     cp_async_wait_all();
     __syncthreads();
     block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{A});
-    dct2_cols_store<H>(A, dst, WH, wd);
+    dct2_cols_store<H, ColCfg<H>::T>(A, dst, WH, wd);
     return;
   }
   // the column group staged whole (the pre-processing pairs rows k and H-k)
@@ -372,7 +359,7 @@ __device__ __forceinline__ void dct_cols_body(const float2* src, float2* dst, in
       A[i * C::CS + s] = make_float2(apply_thresh(v.x, th, tmode), apply_thresh(v.y, th, tmode));
     });
     block_fft_hook_ip<H, C::CS, C::T, -1>(A, twH, SmemLd<C::CS>{A}, SmemSt<C::CS>{A});
-    dct2_cols_store<H>(A, dst, WH, wd);
+    dct2_cols_store<H, ColCfg<H>::T>(A, dst, WH, wd);
   } else {
     block_fft_hook_ip<H, C::CS, C::T, +1>(A, twH, SmemLd<C::CS>{A},
                                           [&](int i, int s, float2 v) { A[row_of(i) * C::CS + s] = v; });

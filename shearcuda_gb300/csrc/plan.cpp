@@ -1080,7 +1080,11 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
 // The directional stage of the fused denoise (level spectra in p->lev, band
 // sums out in p->sum): one cluster kernel, or the split analysis / row /
 // synthesis kernels with the bands in p->band.
-nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, cudaStream_t st) {
+// sums_dct2 (the spectral pipeline): where the chosen synthesis can, the band
+// sums leave as their column DCT-II (the next step of the spectral synthesis)
+// and *sums_dct2 is set; otherwise it is left false.
+nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, cudaStream_t st,
+                                bool* sums_dct2 = nullptr) {
   const DirChoice c = dir_choice(p, n);
   if (c.fused) {
     const int ncl = std::min(p->fused_clusters, n * p->nlev);
@@ -1096,15 +1100,19 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
-  const ColOp syn = c.cols_packed ? ColOp::SynthesisPairs : (tma && c.syn_regs) ? ColOp::SynthesisRegs : ColOp::Synthesis;
+  const bool dct2 = sums_dct2 && tma && c.syn_regs && !c.cols_packed && p->wdH;
+  const ColOp syn = c.cols_packed          ? ColOp::SynthesisPairs
+                    : (tma && c.syn_regs) ? (dct2 ? ColOp::SynthesisRegsDct2 : ColOp::SynthesisRegs)
+                                          : ColOp::Synthesis;
   const float2* twc = c.cols_packed ? (const float2*)p->twH4 : p->twH;
   if (tma)
     NSST_CUDA(launch_cols_tma(syn, p->cols_tmap, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, p->spec,
-                              p->spec_row0, (size_t)p->H * p->WH, twc, p->dev_err, st));
+                              p->spec_row0, (size_t)p->H * p->WH, twc, p->dev_err, st, p->wdH));
   else
     NSST_CUDA(launch_cols(syn, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A, p->spec,
                           (size_t)p->H * p->WH, twc, st));
   timer_mark(p, "band_synthesis_cols", st);
+  if (dct2) *sums_dct2 = true;
   return NSST_OK;
 }
 
@@ -1182,12 +1190,14 @@ nsst_status enqueue_dct_lowpass_rows(nsst_plan* p, int n, cudaStream_t st) {
 // per item at lowbase + i * lowstride), DCT-III (pyr plane 1), and DCT-III down
 // the columns into out[i].
 nsst_status enqueue_dct_synthesis(nsst_plan* p, int n, const float* lowbase, size_t lowstride, const float* lowtab,
-                                  float* const* out, cudaStream_t st) {
+                                  float* const* out, cudaStream_t st, bool sums_dct2 = false) {
   char* A = p->arena;
   const int B = p->B, H = p->H, W = p->W;
   const size_t HW = (size_t)H * W;
-  NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
-  timer_mark(p, "dct_cols_sums", st);
+  if (!sums_dct2) {  // (else the band synthesis has left the sums' column DCT-II)
+    NSST_CUDA(launch_dct_cols(kDct2, p->j_dct_sum, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+    timer_mark(p, "dct_cols_sums", st);
+  }
   NSST_CUDA(launch_dct_rows_syn(p->j_dct_syn, B, n, p->nlev, (size_t)H * p->WH, H, W, A, A, lowbase, lowstride,
                                 p->dct_rs, HW, lowtab, p->twWh, p->twW, p->twDW, st));
   timer_mark(p, "dct_rows_synthesis", st);
@@ -1227,11 +1237,11 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
     NSST_CUDA(launch_cols(ColOp::Synthesis, p->gj_synth_T, B * p->nlev, n, H, W, (float2*)p->garena, A2, p->spec,
                           (size_t)H * p->WH, p->twH, st));
     timer_mark(p, "band_synthesis_cols", st);
-  } else {
-    NSST_TRY(enqueue_directional(p, n, mode, TH, st));
   }
-  return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st)
-                    : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st);
+  bool sums_dct2 = false;
+  if (!keep) NSST_TRY(enqueue_directional(p, n, mode, TH, st, &sums_dct2));
+  return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st, sums_dct2)
+                    : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st, sums_dct2);
 }
 
 // The fused batched pipeline (no host work, no allocation): capturable.

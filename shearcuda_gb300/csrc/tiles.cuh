@@ -75,6 +75,20 @@ __device__ __forceinline__ void st_pair(float2* p, cpx2 v) {
 }
 
 
+// DCT-II post-processing of the FFT V of a column group (dense [row][column]
+// in A, CS = ColCfg<H>::CS columns, T threads):
+// C[k] = (wd[k] V[k] + conj(wd[k]) V[H-k]) / 2, stored down the columns
+template <int H, int T>
+__device__ __forceinline__ void dct2_cols_store(const float2* A, float2* dst, int WH, const float2* __restrict__ wd) {
+  constexpr int CS = ColCfg<H>::CS;
+  for (int e = threadIdx.x; e < H * CS; e += T) {
+    const int s = e % CS, k = e / CS;
+    const float2 w = __ldg(&wd[k]);
+    const float2 a = A[k * CS + s], b = A[((H - k) % H) * CS + s];
+    dst[(size_t)k * WH + s] = cscale(cadd(cmul(w, a), cmulc(b, w)), 0.5f);
+  }
+}
+
 // transform lengths with row / column kernels
 #define NSST_ROW_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024)
 #define NSST_COL_SIZES(X) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
