@@ -110,7 +110,9 @@ enum class RowOp { Fwd, Inv, Thresh, Backward };
 // AnalysisLevel: one job per level (all its bands); *Pairs: the same kernels on
 // split-complex column pairs, with twH pointing to the broadcast twiddle table
 // SynthesisRegs: the synthesis with the band sum in registers (TMA only);
-// SynthesisRegsDct2: the same, the sum leaving as its column DCT-II
+// SynthesisRegsDct2: the same, the sum leaving as its column DCT-II;
+// AnalysisLevelDct: the TMA level analysis finishing the level spectrum's
+// columns itself (the spectral pipeline's DCT-III + FFT column pass)
 enum class ColOp {
   Fwd,
   Inv,
@@ -120,7 +122,8 @@ enum class ColOp {
   AnalysisLevelPairs,
   SynthesisPairs,
   SynthesisRegs,
-  SynthesisRegsDct2
+  SynthesisRegsDct2,
+  AnalysisLevelDct
 };
 
 bool row_len_supported(int wh);

@@ -72,11 +72,18 @@ struct ColTma {
 // Analysis of all bands of one level (job.nbands consecutive bands): the
 // level spectrum's column group Y and band 0's filter group are requested
 // together; band k + 1's filter group replaces band k's in Wb.
-template <int H>
+//
+// DCTANA (the spectral pipeline): job.src holds the level plane with only its
+// rows transformed (k_dct_rows_ana); the CTA finishes its column group itself
+// as k_dct.cu's kDctAna column pass does (DCT-III down the columns, then the
+// forward FFT: pre-processing pairs with wd, inverse FFT stored in the
+// DCT-III output order, forward FFT), into Y, before the band loop.
+template <int H, bool DCTANA>
 __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
     k_band_analysis_ml_tma(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                            int WH, float2* dst_base, const float2* __restrict__ spec_base, int spec_row0,
-                           size_t band_stride, const float2* __restrict__ twH, int* err) {
+                           size_t band_stride, const float2* __restrict__ twH, const float2* __restrict__ wd,
+                           int* err) {
   using C = AnaCfg<H>;
   constexpr int CS = C::CS;
   extern __shared__ __align__(1024) float2 tsm[];
@@ -99,6 +106,22 @@ __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
   __syncthreads();  // the mbarrier is initialised before any thread waits on it
   for (int k = 0; k < job.nbands; k++) {
     tma.wait(err);
+    if (DCTANA && k == 0) {
+      // Z[k] = conj(wd[k]) (C[k] - i C[H-k]), Z[H-k] = i wd[k] (C[H-k] - i C[k]): each pair by one thread
+      for (int e = threadIdx.x; e < (H / 2 + 1) * CS; e += C::T) {
+        const int s = e % CS, kk = e / CS;
+        if (kk == 0) continue;  // Z[0] = C[0]
+        const float2 w = __ldg(&wd[kk]);
+        const float2 a = Y[kk * CS + s], b = Y[(H - kk) * CS + s];
+        Y[kk * CS + s] = cmulc(make_float2(a.x + b.y, a.y - b.x), w);
+        if (kk != H - kk) Y[(H - kk) * CS + s] = cmul(make_float2(b.x + a.y, b.y - a.x), make_float2(-w.y, w.x));
+      }
+      __syncthreads();
+      auto row_of = [](int i) { return i < H / 2 ? 2 * i : 2 * H - 1 - 2 * i; };
+      block_fft_hook_ip<H, CS, C::T, +1>(Y, twH, SmemLd<CS>{Y},
+                                        [&](int i, int s, float2 v) { A[row_of(i) * CS + s] = v; });
+      block_fft_hook_ip<H, CS, C::T, -1>(A, twH, SmemLd<CS>{A}, SmemSt<CS>{Y});
+    }
     const float2* m0 = spec_base + job.m0 + (size_t)k * H;
     // Wk .* Y, with the packed DC/Nyquist column's M term
     // Z'[u] = P[u] Z[u] + M[u] conj(Z[-u])
@@ -410,7 +433,8 @@ cudaError_t prepare_cols_tma(int H) {
   switch (H) {
 #define CASE(n)                                                                           \
   case n: {                                                                               \
-    cudaError_t e = opt_in_tma(k_band_analysis_ml_tma<n>, AnaCfg<n>::smem() + kBarBytes); \
+    cudaError_t e = opt_in_tma(k_band_analysis_ml_tma<n, false>, AnaCfg<n>::smem() + kBarBytes); \
+    if (e == cudaSuccess) e = opt_in_tma(k_band_analysis_ml_tma<n, true>, AnaCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_tma<n>, SynCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_analysis_ml_p_tma<n>, AnaCfg<n>::smem() + kBarBytes); \
     if (e == cudaSuccess) e = opt_in_tma(k_band_synthesis_p_tma<n>, SynCfg<n>::smem() + kBarBytes); \
@@ -431,9 +455,10 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
   const int WH = W / 2;
   if (njobs == 0) return cudaSuccess;
   if (op != ColOp::AnalysisLevel && op != ColOp::Synthesis && op != ColOp::AnalysisLevelPairs &&
-      op != ColOp::SynthesisPairs && op != ColOp::SynthesisRegs && op != ColOp::SynthesisRegsDct2)
+      op != ColOp::SynthesisPairs && op != ColOp::SynthesisRegs && op != ColOp::SynthesisRegsDct2 &&
+      op != ColOp::AnalysisLevelDct)
     return cudaErrorInvalidValue;
-  if (op == ColOp::SynthesisRegsDct2 && !wd) return cudaErrorInvalidValue;
+  if ((op == ColOp::SynthesisRegsDct2 || op == ColOp::AnalysisLevelDct) && !wd) return cudaErrorInvalidValue;
   if (band_stride % (size_t)WH != 0 || spec_row0 > (size_t)INT32_MAX) return cudaErrorInvalidValue;
   count_launch();
   const CUtensorMap& m = *reinterpret_cast<const CUtensorMap*>(amap);
@@ -444,8 +469,11 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
     dim3 grid(WH / ColCfg<n>::CS, njobs);                                                                          \
     constexpr size_t sa = AnaCfg<n>::smem() + kBarBytes, ss = SynCfg<n>::smem() + kBarBytes;                       \
     if (op == ColOp::AnalysisLevel)                                                                                \
-      k_band_analysis_ml_tma<n><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base, sr,     \
-                                                                band_stride, twH, err);                            \
+      k_band_analysis_ml_tma<n, false><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base,  \
+                                                                       sr, band_stride, twH, wd, err);             \
+    else if (op == ColOp::AnalysisLevelDct)                                                                        \
+      k_band_analysis_ml_tma<n, true><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base,   \
+                                                                      sr, band_stride, twH, wd, err);              \
     else if (op == ColOp::AnalysisLevelPairs)                                                                      \
       k_band_analysis_ml_p_tma<n><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base, sr,   \
                                                                   band_stride, twH, err);                          \

@@ -1055,14 +1055,31 @@ nsst_status upload_thresholds(nsst_plan* p, int n, const double* sigma, const do
 // (band, item) column group, which has ndir times more CTAs.  pairs: the
 // level form on split-complex column pairs; tma: the level form with its
 // column groups staged by TMA (forward arena only).
-nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0, bool pairs = false,
-                                  bool tma = false) {
-  float2* base = (float2*)(grad ? p->garena : p->arena);
+bool analysis_per_level(const nsst_plan* p, int n, int ana) {
   const size_t ctas = (size_t)n * p->nlev * (p->WH / col_tile(p->H));
-  const bool level = ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count);
+  return ana == 1 || (ana == 0 && ctas >= (size_t)2 * p->sm_count);
+}
+
+// Whether the directional stage of n items takes the TMA level analysis that
+// finishes the level spectra's columns itself (the spectral pipeline then
+// leaves them out of its analysis front).
+bool analysis_takes_dct(const nsst_plan* p, int n) {
+  const DirChoice c = dir_choice(p, n);
+  return !c.fused && c.cols_tma && p->cols_tma_ok && !c.cols_packed && p->wdH && analysis_per_level(p, n, c.ana);
+}
+
+nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t st, int ana = 0, bool pairs = false,
+                                  bool tma = false, bool dctana = false) {
+  float2* base = (float2*)(grad ? p->garena : p->arena);
+  const bool level = analysis_per_level(p, n, ana);
   const size_t bs = (size_t)p->H * p->WH;
   const float2* tw = pairs ? (const float2*)p->twH4 : p->twH;
-  if (level && tma && !grad && p->cols_tma_ok) {
+  if (dctana) {  // the level planes' columns are still to be transformed
+    if (!(level && tma && !pairs && !grad && p->cols_tma_ok && p->wdH))
+      return fail(NSST_ERR_INVALID_ARG, "internal: the level analysis cannot finish the level spectra");
+    NSST_CUDA(launch_cols_tma(ColOp::AnalysisLevelDct, p->cols_tmap, p->j_analysis_lev, p->B * p->nlev, n, p->H,
+                              p->W, base, p->spec, p->spec_row0, bs, p->twH, p->dev_err, st, p->wdH));
+  } else if (level && tma && !grad && p->cols_tma_ok) {
     NSST_CUDA(launch_cols_tma(pairs ? ColOp::AnalysisLevelPairs : ColOp::AnalysisLevel, p->cols_tmap,
                               p->j_analysis_lev, p->B * p->nlev, n, p->H, p->W, base, p->spec, p->spec_row0, bs, tw,
                               p->dev_err, st));
@@ -1084,7 +1101,7 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
 // sums leave as their column DCT-II (the next step of the spectral synthesis)
 // and *sums_dct2 is set; otherwise it is left false.
 nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, cudaStream_t st,
-                                bool* sums_dct2 = nullptr) {
+                                bool* sums_dct2 = nullptr, bool ana_dct = false) {
   const DirChoice c = dir_choice(p, n);
   if (c.fused) {
     const int ncl = std::min(p->fused_clusters, n * p->nlev);
@@ -1095,7 +1112,7 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   }
   char* A = p->arena;
   const bool tma = c.cols_tma && p->cols_tma_ok;
-  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana, c.cols_packed, tma));
+  NSST_TRY(enqueue_band_analysis(p, n, false, st, c.ana, c.cols_packed, tma, ana_dct));
   timer_mark(p, "band_analysis_cols", st);
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
@@ -1157,7 +1174,10 @@ nsst_status enqueue_dct_cols_out(nsst_plan* p, int n, const float* const* src, f
 
 // Spectral analysis front of n items: X = DCT2(x) in pyr plane 0 (through
 // plane 1), then every level's spectrum (p->lev) from X .* R_l.
-nsst_status enqueue_dct_analysis(nsst_plan* p, int n, const float* const* x, cudaStream_t st) {
+// skip_cols_levels: the directional stage's level analysis finishes the
+// level spectra's columns (analysis_takes_dct).
+nsst_status enqueue_dct_analysis(nsst_plan* p, int n, const float* const* x, cudaStream_t st,
+                                 bool skip_cols_levels = false) {
   char* A = p->arena;
   const int B = p->B, H = p->H, W = p->W;
   const size_t HW = (size_t)H * W;
@@ -1170,8 +1190,10 @@ nsst_status enqueue_dct_analysis(nsst_plan* p, int n, const float* const* x, cud
   NSST_CUDA(launch_dct_rows_ana(p->j_dct_ana, B * p->nlev, n, H, W, A, A, p->dct_ra, HW, p->twWh, p->twW, p->twDW,
                                 false, st));
   timer_mark(p, "dct_rows_levels", st);
-  NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
-  timer_mark(p, "dct_cols_levels", st);
+  if (!skip_cols_levels) {
+    NSST_CUDA(launch_dct_cols(kDctAna, p->j_cols_lev, B * p->nlev, n, H, W, A, A, p->twH, p->wdH, st));
+    timer_mark(p, "dct_cols_levels", st);
+  }
   return NSST_OK;
 }
 
@@ -1218,7 +1240,8 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
   char* A = p->arena;
   float2* A2 = (float2*)A;
   const int B = p->B, H = p->H, W = p->W;
-  NSST_TRY(enqueue_dct_analysis(p, n, x, st));
+  const bool ana_dct = !keep && analysis_takes_dct(p, n);
+  NSST_TRY(enqueue_dct_analysis(p, n, x, st, ana_dct));
   if (lowpass_th) {  // lowpass band -> threshold -> DCT2, in tmp plane 0
     NSST_TRY(enqueue_dct_lowpass_rows(p, n, st));
     NSST_CUDA(launch_dct_cols(kDctThresh, p->j_dct_lowc, B, n, H, W, A, A, p->twH, p->wdH, st, TH, p->nbands, mode));
@@ -1239,7 +1262,7 @@ nsst_status enqueue_denoise_dct(nsst_plan* p, int n, const float* const* x, floa
     timer_mark(p, "band_synthesis_cols", st);
   }
   bool sums_dct2 = false;
-  if (!keep) NSST_TRY(enqueue_directional(p, n, mode, TH, st, &sums_dct2));
+  if (!keep) NSST_TRY(enqueue_directional(p, n, mode, TH, st, &sums_dct2, ana_dct));
   return lowpass_th ? enqueue_dct_synthesis(p, n, p->tmp, p->s_tmp, p->dct_gl, out, st, sums_dct2)
                     : enqueue_dct_synthesis(p, n, p->pyr, p->s_pyr, p->dct_tl, out, st, sums_dct2);
 }
