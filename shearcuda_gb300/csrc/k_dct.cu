@@ -25,7 +25,9 @@
 // k_dct_cols<H, kDctThresh>, k_dct_rows_fwd).  Seven launches replace the
 // direct pyramid's FFMA-bound convolutions (two launches per analysis level,
 // one per synthesis level: twelve at four levels) and the three level-FFT
-// launches.
+// launches; with the TMA directional kernels (k_cols_tma.cu) the level
+// analysis does the DCT-III + FFT column pass and the register-sum synthesis
+// the band sums' DCT-II, leaving five.
 //
 // DCTs of length N through one N-point FFT (J. Makhoul, "A fast cosine
 // transform in one and two dimensions", IEEE Trans. ASSP 28(1), 1980), all
