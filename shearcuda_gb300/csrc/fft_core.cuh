@@ -1002,6 +1002,36 @@ __device__ __forceinline__ bool block_fft_inv_op_fwd(float2* buf, const float2* 
   return true;
 }
 
+// An FFT of NSEQ sequences whose inputs are already in registers in the
+// layout a last pass of the same radix leaves them (stockham_last_acc: slot
+// (it, r) of a thread holds row j + r N/R of column s, w = tid + it T, j =
+// w / NSEQ, s = w % NSEQ), which is the first pass's input layout when the
+// plan's first radix is R: the first pass runs on the registers and writes
+// buf, the rest are the engine's, the last storing through st.
+template <int N, int NSEQ, int T, int DIR, int R, int IPT, class St>
+__device__ __forceinline__ void block_fft_from_regs(float2* buf, const float2* __restrict__ tw,
+                                                    const float2 (&v)[IPT][R], const St& st) {
+  using Plan = typename FftPlan<N>::type;
+  static_assert(FirstRadix<Plan>::value == R, "the plan's first radix must be the registers' radix");
+  constexpr int NB = N / R;
+  static_assert(NB * NSEQ == IPT * T, "every thread owns IPT first-pass butterflies");
+  constexpr int SWZ = R % 2 == 0 ? R : 0;  // the first pass's output swizzle (as stockham_ip)
+#pragma unroll
+  for (int it = 0; it < IPT; it++) {
+    const int w = threadIdx.x + it * T;
+    const int s = w % NSEQ, j = w / NSEQ;
+    float2 u[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) u[r] = v[it][r];
+    Dft<R, DIR>::run(u);  // first pass: no twiddles
+#pragma unroll
+    for (int r = 0; r < R; r++) buf[swz_row<NSEQ, SWZ>(j * R + r) * NSEQ + s] = u[r];
+  }
+  __syncthreads();
+  auto rd = [&](int row, int sq) -> float2 { return buf[row * NSEQ + sq]; };  // (the passes read buf)
+  fft_hook_ip_passes<N, NSEQ, T, DIR, R, SWZ>(buf, tw, rd, st, NoHook{}, typename TailRadices<Plan>::type{});
+}
+
 // after_first_read: called once the first pass has read all of its inputs
 // through ld (e.g. to start refilling the buffer ld reads from).  buf holds
 // float2 (NSEQ sequences) or float4 (2 NSEQ sequences, two per element).

@@ -392,23 +392,33 @@ __global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
         }
     }
   }
-  // the level's band sum: one column IFFT, stored by its last pass
-  {
+  // the level's band sum: one column IFFT, stored by its last pass; where the
+  // plan's first radix is its last, the IFFT's first pass starts from the
+  // registers (they hold its inputs), else the sum goes to A first.  With
+  // DCT2, row r of the IFFT goes to element r / 2 (r even) or H - 1 - (r - 1)
+  // / 2 (r odd) of the DCT-II's FFT input.
+  auto st_dct = [&](int i, int sq, float2 v) { A[((i & 1) ? H - 1 - (i >> 1) : (i >> 1)) * CS + sq] = v; };
+  const ColGlobalSt st_out{dst_base + job.dst + col0, WH};
+  if constexpr (FirstRadix<typename C::Plan>::value == RL) {
+    if constexpr (DCT2)
+      block_fft_from_regs<H, CS, T, +1>(A, twH, acc, st_dct);
+    else
+      block_fft_from_regs<H, CS, T, +1>(A, twH, acc, st_out);
+  } else {
     const int s = threadIdx.x % CS;
 #pragma unroll
     for (int it = 0; it < IPT; it++)
 #pragma unroll
       for (int r = 0; r < RL; r++) A[last_pass_row<H, CS, T, RL>(it, r) * CS + s] = acc[it][r];
+    __syncthreads();
+    if constexpr (DCT2)
+      block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, st_dct);
+    else
+      block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, st_out);
   }
-  __syncthreads();
   if constexpr (DCT2) {
-    // row r of the IFFT goes to element r / 2 (r even) or H - 1 - (r - 1) / 2 (r odd) of the DCT-II's FFT input
-    auto st_dct = [&](int i, int sq, float2 v) { A[((i & 1) ? H - 1 - (i >> 1) : (i >> 1)) * CS + sq] = v; };
-    block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, st_dct);
     block_fft_hook_ip<H, CS, T, -1>(A, twH, SmemLd<CS>{A}, SmemSt<CS>{A});
     dct2_cols_store<H, T>(A, dst_base + job.dst + col0, WH, wd);
-  } else {
-    block_fft_hook_ip<H, CS, T, +1>(A, twH, SmemLd<CS>{A}, ColGlobalSt{dst_base + job.dst + col0, WH});
   }
   tp.drain(err);
   tw.drain(err);
