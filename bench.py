@@ -43,6 +43,9 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
     ap.add_argument('--batch', type=int, default=BATCH, help='images per batched pass (smaller for profiling)')
+    ap.add_argument('--size', default='%dx%d' % (H, W),
+                    help='HxW of the batched pass\'s images (other sizes for profiling their kernels; use with '
+                         '--no-extras)')
     ap.add_argument('--workload', default='2d', choices=['2d', 'v3', 'sep'],
                     help="v3 / sep: only the 3-D volume or the image-separation extra (for profiling their kernels)")
     ap.add_argument('--sep-batch', type=int, default=8, help='images per batched separation call')
@@ -580,7 +583,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     traffic_db = None
     tpath = os.path.join(ROOT, 'profiles', 'ncu_traffic.json')
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and (H, W) == (512, 512):  # captured at 512x512
         try:
             traffic_db = json.load(open(tpath))
         except ValueError:
@@ -597,8 +600,8 @@ def run_gpu(args):
     line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded ellipses + gradient + N(0, 20^2))',
-            'config': {'workload': 'batch of %d x 512x512 images, one batched NSST dec+hard-thresh+rec pass per step'
-                                   % BATCH,
+            'config': {'workload': 'batch of %d x %dx%d images, one batched NSST dec+hard-thresh+rec pass per step'
+                                   % (BATCH, H, W),
                        'H': H, 'W': W, 'batch_per_gpu': BATCH, 'dcomp': DCOMP, 'dsize': DSIZE, 'lpfilt': 'maxflat',
                        'K': K, 'sigma': SIGMA, 'parallelism': 'replicas' if world > 1 else 'single',
                        'l2': 'flushed between steps (256 MB write, untimed)', 'graphs': True,
@@ -899,8 +902,9 @@ def run_sep(args):
 
 def main():
     args = parse()
-    global BATCH
+    global BATCH, H, W
     BATCH = args.batch
+    H, W = (int(v) for v in args.size.lower().split('x'))
     if args.cpu_sweep:
         cpu_sweep()
     elif args.impl == 'reference':
