@@ -176,11 +176,15 @@ constexpr int tma_box_rows(int H) {
 // over the plan's arena (box: col_tile(H) float2 x tma_box_rows(H) rows):
 // every job's src and spec offset (spec relative to the arena, as spec_row0
 // * WH plus job.spec) is a multiple of WH.  err: the plan's device error word.
+// per_level: the jobs come level-major with this many items per level, and
+// the CTAs run in chunks of column groups across the items (0: one job per
+// grid row); njobs must be a multiple of it.
 bool cols_tma_supported(int H, int WH);
 cudaError_t prepare_cols_tma(int H);
 cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int njobs, int n_active, int H, int W,
                             float2* dst_base, const float2* spec_base, size_t spec_row0, size_t band_stride,
-                            const float2* twH, int* err, cudaStream_t st, const float2* wd = nullptr);
+                            const float2* twH, int* err, cudaStream_t st, const float2* wd = nullptr,
+                            int per_level = 0);
 cudaError_t launch_dir_fused(const void* ymap, const FusedJob* jobs, int njobs, int n_active, int nclusters, int H,
                              int W, float2* dst_base, const float2* spec_base, size_t band_stride, const float2* twH,
                              const float2* twWh, const float2* twW, const float* thr, int mode, int* err,

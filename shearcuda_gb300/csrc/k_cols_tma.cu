@@ -69,6 +69,33 @@ struct ColTma {
   }
 };
 
+// Block -> (job, column group).  The job lists come level-major with
+// per_level items per level.  Launch order: for each level, for each chunk of
+// column groups 512 bytes wide, every item's CTAs of that chunk; so the CTAs
+// resident together read the same few column groups of the level's filter
+// spectra (from DRAM once for all items of the batch: the spectra of a
+// 1024 x 1024 plan, 201 MB, do not stay in the 129 MB L2 between items) and
+// still write 512-byte row segments.  per_level == 0: job = blockIdx.y,
+// column group = blockIdx.x.
+struct ColBlock {
+  int job, col0;
+};
+template <int CS>
+__device__ __forceinline__ ColBlock col_block(int per_level) {
+  const int G = gridDim.x;
+  if (per_level <= 0) return {(int)blockIdx.y, (int)blockIdx.x * CS};
+  int cg = 64 / CS;
+  while (G % cg) cg >>= 1;
+  const long lin = (long)blockIdx.y * G + blockIdx.x;
+  const int gi = (int)(lin % cg);
+  long t = lin / cg;
+  const int i = (int)(t % per_level);
+  t /= per_level;
+  const int nch = G / cg;
+  const int c = (int)(t % nch), l = (int)(t / nch);
+  return {l * per_level + i, (c * cg + gi) * CS};
+}
+
 // Analysis of all bands of one level (job.nbands consecutive bands): the
 // level spectrum's column group Y and band 0's filter group are requested
 // together; band k + 1's filter group replaces band k's in Wb.
@@ -83,16 +110,17 @@ __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
     k_band_analysis_ml_tma(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                            int WH, float2* dst_base, const float2* __restrict__ spec_base, int spec_row0,
                            size_t band_stride, const float2* __restrict__ twH, const float2* __restrict__ wd,
-                           int* err) {
+                           int* err, int per_level) {
   using C = AnaCfg<H>;
   constexpr int CS = C::CS;
   extern __shared__ __align__(1024) float2 tsm[];
   float2* A = tsm;          // transform, in place
   float2* Y = A + H * CS;   // level spectrum column group [row][column]
   float2* Wb = Y + H * CS;  // filter spectrum of the current band
-  const ColJob job = jobs[blockIdx.y];
+  const ColBlock cb = col_block<CS>(per_level);
+  const ColJob job = jobs[cb.job];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = cb.col0;
   const bool dc = col0 == 0;
   const int band_rows = (int)(band_stride / WH);
   const int yrow = (int)(job.src / WH), srow = spec_row0 + (int)(job.spec / WH);
@@ -104,24 +132,27 @@ __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
     tma.load(&amap, Wb, srow);
   }
   __syncthreads();  // the mbarrier is initialised before any thread waits on it
-  for (int k = 0; k < job.nbands; k++) {
-    tma.wait(err);
-    if (DCTANA && k == 0) {
-      // Z[k] = conj(wd[k]) (C[k] - i C[H-k]), Z[H-k] = i wd[k] (C[H-k] - i C[k]): each pair by one thread
-      for (int e = threadIdx.x; e < (H / 2 + 1) * CS; e += C::T) {
-        const int s = e % CS, kk = e / CS;
-        if (kk == 0) continue;  // Z[0] = C[0]
-        const float2 w = __ldg(&wd[kk]);
-        const float2 a = Y[kk * CS + s], b = Y[(H - kk) * CS + s];
-        Y[kk * CS + s] = cmulc(make_float2(a.x + b.y, a.y - b.x), w);
-        if (kk != H - kk) Y[(H - kk) * CS + s] = cmul(make_float2(b.x + a.y, b.y - a.x), make_float2(-w.y, w.x));
-      }
-      __syncthreads();
-      auto row_of = [](int i) { return i < H / 2 ? 2 * i : 2 * H - 1 - 2 * i; };
-      block_fft_hook_ip<H, CS, C::T, +1>(Y, twH, SmemLd<CS>{Y},
-                                        [&](int i, int s, float2 v) { A[row_of(i) * CS + s] = v; });
-      block_fft_hook_ip<H, CS, C::T, -1>(A, twH, SmemLd<CS>{A}, SmemSt<CS>{Y});
+  if (job.nbands > 0) tma.wait(err);  // Y and band 0's filter group
+  if constexpr (DCTANA) {
+    // the level's column pass, ahead of the band loop (inside it, its
+    // registers made the loop spill)
+    // Z[k] = conj(wd[k]) (C[k] - i C[H-k]), Z[H-k] = i wd[k] (C[H-k] - i C[k]): each pair by one thread
+    for (int e = threadIdx.x; e < (H / 2 + 1) * CS; e += C::T) {
+      const int s = e % CS, kk = e / CS;
+      if (kk == 0) continue;  // Z[0] = C[0]
+      const float2 w = __ldg(&wd[kk]);
+      const float2 a = Y[kk * CS + s], b = Y[(H - kk) * CS + s];
+      Y[kk * CS + s] = cmulc(make_float2(a.x + b.y, a.y - b.x), w);
+      if (kk != H - kk) Y[(H - kk) * CS + s] = cmul(make_float2(b.x + a.y, b.y - a.x), make_float2(-w.y, w.x));
     }
+    __syncthreads();
+    auto row_of = [](int i) { return i < H / 2 ? 2 * i : 2 * H - 1 - 2 * i; };
+    block_fft_hook_ip<H, CS, C::T, +1>(Y, twH, SmemLd<CS>{Y},
+                                      [&](int i, int s, float2 v) { A[row_of(i) * CS + s] = v; });
+    block_fft_hook_ip<H, CS, C::T, -1>(A, twH, SmemLd<CS>{A}, SmemSt<CS>{Y});
+  }
+  for (int k = 0; k < job.nbands; k++) {
+    if (k > 0) tma.wait(err);
     const float2* m0 = spec_base + job.m0 + (size_t)k * H;
     // Wk .* Y, with the packed DC/Nyquist column's M term
     // Z'[u] = P[u] Z[u] + M[u] conj(Z[-u])
@@ -146,16 +177,18 @@ template <int H>
 __global__ void __launch_bounds__(AnaCfg<H>::T, AnaCfg<H>::MINB)
     k_band_analysis_ml_p_tma(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs,
                              int n_active, int WH, float2* dst_base, const float2* __restrict__ spec_base,
-                             int spec_row0, size_t band_stride, const float2* __restrict__ twH4, int* err) {
+                             int spec_row0, size_t band_stride, const float2* __restrict__ twH4, int* err,
+                             int per_level) {
   using C = AnaCfg<H>;
   constexpr int CS = C::CS, NP = CS / 2;
   extern __shared__ __align__(1024) float2 tsm[];
   cpx2* A = reinterpret_cast<cpx2*>(tsm);  // transform [row][pair], in place
   float2* Y = tsm + H * CS;                // level spectrum column group [row][column]
   float2* Wb = Y + H * CS;                 // filter spectrum of the current band
-  const ColJob job = jobs[blockIdx.y];
+  const ColBlock cb = col_block<CS>(per_level);
+  const ColJob job = jobs[cb.job];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = cb.col0;
   const bool dc = col0 == 0;
   const int band_rows = (int)(band_stride / WH);
   const int yrow = (int)(job.src / WH), srow = spec_row0 + (int)(job.spec / WH);
@@ -198,16 +231,17 @@ template <int H>
 __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
     k_band_synthesis_tma(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                          int WH, float2* dst_base, const float2* __restrict__ spec_base, size_t band_stride,
-                         const float2* __restrict__ twH, int* err) {
+                         const float2* __restrict__ twH, int* err, int per_level) {
   using C = SynCfg<H>;
   constexpr int CS = C::CS;
   static_assert(C::LD == CS, "dense column groups");
   extern __shared__ __align__(1024) float2 tsm[];
   float2 *A = tsm, *S = tsm + (size_t)H * CS, *D = tsm + 2 * (size_t)H * CS;
   float2* P = D + H;  // staging: the band's H x CS column group, [row][column]
-  const ColJob job = jobs[blockIdx.y];
+  const ColBlock cb = col_block<CS>(per_level);
+  const ColJob job = jobs[cb.job];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = cb.col0;
   const bool dc = col0 == 0;
   const int band_rows = (int)(band_stride / WH);
   const int brow = (int)(job.src / WH);
@@ -250,7 +284,7 @@ template <int H>
 __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
     k_band_synthesis_p_tma(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                            int WH, float2* dst_base, const float2* __restrict__ spec_base, size_t band_stride,
-                           const float2* __restrict__ twH4, int* err) {
+                           const float2* __restrict__ twH4, int* err, int per_level) {
   using C = SynCfg<H>;
   constexpr int CS = C::CS, NP = CS / 2;
   extern __shared__ __align__(1024) float2 tsm[];
@@ -258,9 +292,10 @@ __global__ void __launch_bounds__(SynCfg<H>::T, SynCfg<H>::MINB)
   cpx2* S = reinterpret_cast<cpx2*>(tsm + (size_t)H * CS);  // running band sum [row][pair]
   float2* D = tsm + 2 * (size_t)H * CS;                     // column 0 of the band's transform
   float2* P = D + H;                                        // staging: the band's column group [row][column]
-  const ColJob job = jobs[blockIdx.y];
+  const ColBlock cb = col_block<CS>(per_level);
+  const ColJob job = jobs[cb.job];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = cb.col0;
   const bool dc = col0 == 0;
   const int band_rows = (int)(band_stride / WH);
   const int brow = (int)(job.src / WH);
@@ -337,7 +372,7 @@ __global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
     k_band_synthesis_racc(const __grid_constant__ CUtensorMap amap, const ColJob* __restrict__ jobs, int n_active,
                           int WH, float2* dst_base, const float2* __restrict__ spec_base, int spec_row0,
                           size_t band_stride, const float2* __restrict__ twH, const float2* __restrict__ wd,
-                          int* err) {
+                          int* err, int per_level) {
   using C = RaccCfg<H>;
   constexpr int CS = C::CS, T = C::T, RL = C::RL, IPT = C::IPT;
   extern __shared__ __align__(1024) float2 tsm[];
@@ -346,9 +381,10 @@ __global__ void __launch_bounds__(RaccCfg<H>::T, RaccCfg<H>::MINB)
   float2* Wc = P + H * CS;   // the band's spectrum column group [row][column]
   float2* D = Wc + H * CS;   // column 0 of the band's transform
   const uint32_t bars = smem_u32(D + H);
-  const ColJob job = jobs[blockIdx.y];
+  const ColBlock cb = col_block<CS>(per_level);
+  const ColJob job = jobs[cb.job];
   if (job.item >= n_active) return;
-  const int col0 = blockIdx.x * CS;
+  const int col0 = cb.col0;
   const bool dc = col0 == 0;
   const int band_rows = (int)(band_stride / WH);
   const int brow = (int)(job.src / WH), srow = spec_row0 + (int)(job.spec / WH);
@@ -461,7 +497,7 @@ cudaError_t prepare_cols_tma(int H) {
 
 cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int njobs, int n_active, int H, int W,
                             float2* dst_base, const float2* spec_base, size_t spec_row0, size_t band_stride,
-                            const float2* twH, int* err, cudaStream_t st, const float2* wd) {
+                            const float2* twH, int* err, cudaStream_t st, const float2* wd, int per_level) {
   const int WH = W / 2;
   if (njobs == 0) return cudaSuccess;
   if (op != ColOp::AnalysisLevel && op != ColOp::Synthesis && op != ColOp::AnalysisLevelPairs &&
@@ -470,36 +506,37 @@ cudaError_t launch_cols_tma(ColOp op, const void* amap, const ColJob* jobs, int 
     return cudaErrorInvalidValue;
   if ((op == ColOp::SynthesisRegsDct2 || op == ColOp::AnalysisLevelDct) && !wd) return cudaErrorInvalidValue;
   if (band_stride % (size_t)WH != 0 || spec_row0 > (size_t)INT32_MAX) return cudaErrorInvalidValue;
+  if (per_level < 0 || (per_level > 0 && njobs % per_level != 0)) return cudaErrorInvalidValue;
   count_launch();
   const CUtensorMap& m = *reinterpret_cast<const CUtensorMap*>(amap);
   const int sr = (int)spec_row0;
   switch (H) {
-#define CASE(n)                                                                                                    \
-  case n: {                                                                                                        \
-    dim3 grid(WH / ColCfg<n>::CS, njobs);                                                                          \
-    constexpr size_t sa = AnaCfg<n>::smem() + kBarBytes, ss = SynCfg<n>::smem() + kBarBytes;                       \
-    if (op == ColOp::AnalysisLevel)                                                                                \
+#define CASE(n)                                                                                                     \
+  case n: {                                                                                                         \
+    dim3 grid(WH / ColCfg<n>::CS, njobs);                                                                           \
+    constexpr size_t sa = AnaCfg<n>::smem() + kBarBytes, ss = SynCfg<n>::smem() + kBarBytes;                        \
+    if (op == ColOp::AnalysisLevel)                                                                                 \
       k_band_analysis_ml_tma<n, false><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base,  \
-                                                                       sr, band_stride, twH, wd, err);             \
-    else if (op == ColOp::AnalysisLevelDct)                                                                        \
+                                                                       sr, band_stride, twH, wd, err, per_level);   \
+    else if (op == ColOp::AnalysisLevelDct)                                                                         \
       k_band_analysis_ml_tma<n, true><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base,   \
-                                                                      sr, band_stride, twH, wd, err);              \
-    else if (op == ColOp::AnalysisLevelPairs)                                                                      \
+                                                                      sr, band_stride, twH, wd, err, per_level);    \
+    else if (op == ColOp::AnalysisLevelPairs)                                                                       \
       k_band_analysis_ml_p_tma<n><<<grid, AnaCfg<n>::T, sa, st>>>(m, jobs, n_active, WH, dst_base, spec_base, sr,   \
-                                                                  band_stride, twH, err);                          \
-    else if (op == ColOp::Synthesis)                                                                               \
+                                                                  band_stride, twH, err, per_level);                \
+    else if (op == ColOp::Synthesis)                                                                                \
       k_band_synthesis_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,           \
-                                                              band_stride, twH, err);                              \
-    else if (op == ColOp::SynthesisRegs)                                                                           \
-      k_band_synthesis_racc<n, false><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                            \
-          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err);                              \
-    else if (op == ColOp::SynthesisRegsDct2)                                                                       \
-      k_band_synthesis_racc<n, true><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                             \
-          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err);                              \
-    else                                                                                                           \
+                                                              band_stride, twH, err, per_level);                    \
+    else if (op == ColOp::SynthesisRegs)                                                                            \
+      k_band_synthesis_racc<n, false><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                             \
+          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err, per_level);                    \
+    else if (op == ColOp::SynthesisRegsDct2)                                                                        \
+      k_band_synthesis_racc<n, true><<<grid, RaccCfg<n>::T, RaccCfg<n>::smem(), st>>>(                              \
+          m, jobs, n_active, WH, dst_base, spec_base, sr, band_stride, twH, wd, err, per_level);                    \
+    else                                                                                                            \
       k_band_synthesis_p_tma<n><<<grid, SynCfg<n>::T, ss, st>>>(m, jobs, n_active, WH, dst_base, spec_base,         \
-                                                                band_stride, twH, err);                            \
-    return cudaGetLastError();                                                                                     \
+                                                                band_stride, twH, err, per_level);                  \
+    return cudaGetLastError();                                                                                      \
   }
     NSST_COL_SIZES(CASE)
 #undef CASE

@@ -1085,11 +1085,11 @@ nsst_status enqueue_band_analysis(nsst_plan* p, int n, bool grad, cudaStream_t s
     if (!(level && tma && !pairs && !grad && p->cols_tma_ok && p->wdH))
       return fail(NSST_ERR_INVALID_ARG, "internal: the level analysis cannot finish the level spectra");
     NSST_CUDA(launch_cols_tma(ColOp::AnalysisLevelDct, p->cols_tmap, p->j_analysis_lev, p->B * p->nlev, n, p->H,
-                              p->W, base, p->spec, p->spec_row0, bs, p->twH, p->dev_err, st, p->wdH));
+                              p->W, base, p->spec, p->spec_row0, bs, p->twH, p->dev_err, st, p->wdH, p->B));
   } else if (level && tma && !grad && p->cols_tma_ok) {
     NSST_CUDA(launch_cols_tma(pairs ? ColOp::AnalysisLevelPairs : ColOp::AnalysisLevel, p->cols_tmap,
                               p->j_analysis_lev, p->B * p->nlev, n, p->H, p->W, base, p->spec, p->spec_row0, bs, tw,
-                              p->dev_err, st));
+                              p->dev_err, st, nullptr, p->B));
   } else if (level) {
     NSST_CUDA(launch_cols(pairs ? ColOp::AnalysisLevelPairs : ColOp::AnalysisLevel,
                           grad ? p->gj_analysis_lev : p->j_analysis_lev, p->B * p->nlev, n, p->H, p->W, base, base,
@@ -1131,7 +1131,7 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   const float2* twc = c.cols_packed ? (const float2*)p->twH4 : p->twH;
   if (tma)
     NSST_CUDA(launch_cols_tma(syn, p->cols_tmap, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, p->spec,
-                              p->spec_row0, (size_t)p->H * p->WH, twc, p->dev_err, st, p->wdH));
+                              p->spec_row0, (size_t)p->H * p->WH, twc, p->dev_err, st, p->wdH, p->B));
   else
     NSST_CUDA(launch_cols(syn, p->j_synthesis, p->B * p->nlev, n, p->H, p->W, (float2*)A, (float2*)A, p->spec,
                           (size_t)p->H * p->WH, twc, st));
