@@ -51,9 +51,14 @@ template <int N>
 struct AnaCfg : ColCfg<N> {
   static constexpr size_t smem() { return 3 * (size_t)N * ColCfg<N>::CS * sizeof(float2); }
   // the column kernels' thread count (every thread busy in the radix-16
-  // passes); shared memory allows two CTAs per SM below 2048 points
-  static constexpr int T = ColCfg<N>::T;
-  static constexpr int MINB = N >= 2048 ? 1 : 2;
+  // passes); shared memory allows two CTAs per SM below 2048 points.  The
+  // 3 x 16 x 16 and 3 x 16 x 8 plans (768 and 384 points) have 192
+  // radix-16 butterflies per column group: 192 threads, three CTAs per SM
+  // (their planes take 72 KB), where 256 threads left a quarter of the
+  // warps waiting at the barrier in those passes
+  static constexpr bool ODD3 = N == 768 || N == 384;
+  static constexpr int T = ODD3 ? 192 : ColCfg<N>::T;
+  static constexpr int MINB = N >= 2048 ? 1 : ODD3 ? 3 : 2;
 };
 
 // Split-complex column pairs (cpx2): columns 2p and 2p + 1 of a group share a
