@@ -43,6 +43,30 @@ def test_batch_equals_single(built_lib, cuda):
     np.testing.assert_array_equal(o1.cpu().numpy(), outs[0].cpu().numpy())
 
 
+@pytest.mark.parametrize('HW,B,n', [((512, 512), 8, 5), ((768, 1024), 4, 3), ((384, 512), 6, 4)])
+def test_level_kernels_partial_batch_equal_single(built_lib, cuda, HW, B, n):
+    # the TMA column kernels run, per level, chunks of column groups across
+    # all B items of the plan (the inactive items' CTAs leave at once); with
+    # the level analysis forced, every image of an n < B call equals itself
+    # denoised alone through a one-image plan running the same kernels
+    import shearcuda_gb300 as sc
+    H, W = HW
+    batch = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W, batch=B)
+    single = sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, H, W)
+    scal = sc.nsst_scalars(single, 100)
+    batch.set_scalars(scal)
+    name = 'split/level-tma/rows8/synthesis-regs'
+    for p, m in ((batch, n), (single, 1)):
+        p.select_directional(m, p.directional_candidates().index(name))
+    xs = _imgs(HW, n, 40, cuda)
+    sig = [12.0, 20.0, 35.0, 25.0, 18.0][:n]
+    outs = sc.nsst_denoise_batch(xs, batch, sig, K_DEMO, scal)
+    for x, o, s in zip(xs, outs, sig):
+        ref = sc.nsst_denoise(x, single, s, K_DEMO, scal)
+        assert torch.equal(o, ref)
+    batch.check_device()
+
+
 def test_uneven_multi_batch(built_lib, cuda):
     import shearcuda_gb300 as sc
     shapes = [(256, 256), (384, 512), (256, 384)]
