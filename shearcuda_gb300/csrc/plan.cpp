@@ -1062,16 +1062,21 @@ bool analysis_per_level(const nsst_plan* p, int n, int ana) {
 
 // Whether the directional stage of n items takes the TMA level analysis that
 // finishes the level spectra's columns itself (the spectral pipeline then
-// leaves them out of its analysis front).
-// Measured: a gain at 512 rows (64 x 512^2: -0.02 ms for the analysis
-// side, -0.05 ms for the synthesis side), none at 1024, a loss at 768, 384 and
-// 256 rows (the DCT passes there run faster on their own), so both column
-// fusions are taken from 512 rows up where the rows are a power of two.
-bool dct_fusion_pays(const nsst_plan* p) { return p->H >= 512 && (p->H & (p->H - 1)) == 0; }
+// leaves them out of its analysis front), and whether the register-sum
+// synthesis hands the band sums on as their column DCT-II.  Measured (stage
+// timers, us per megapixel, fused against the two kernels): analysis 256 rows
+// 101.2 / 105.1, 384 rows 106.1 / 105.3, 768 rows 121.7 / 119.6; synthesis
+// 256 rows 87.9 / 83.9, 384 rows 86.6 / 87.2, 768 rows 91.5 / 94.5; at 512
+// rows both sides gain (64 x 512^2: -0.02 and -0.05 ms), at 1024 neither
+// side lost.
+bool dct_ana_fusion_pays(const nsst_plan* p) { return p->H >= 256 && (p->H & (p->H - 1)) == 0; }
+bool dct_syn_fusion_pays(const nsst_plan* p) {
+  return p->H == 768 || (p->H >= 512 && (p->H & (p->H - 1)) == 0);
+}
 
 bool analysis_takes_dct(const nsst_plan* p, int n) {
   const DirChoice c = dir_choice(p, n);
-  return dct_fusion_pays(p) && !c.fused && c.cols_tma && p->cols_tma_ok && !c.cols_packed && p->wdH &&
+  return dct_ana_fusion_pays(p) && !c.fused && c.cols_tma && p->cols_tma_ok && !c.cols_packed && p->wdH &&
          analysis_per_level(p, n, c.ana);
 }
 
@@ -1124,7 +1129,7 @@ nsst_status enqueue_directional(nsst_plan* p, int n, int mode, const float* TH, 
   NSST_CUDA(launch_rows_thresh(p->j_rows_bands, p->B * p->ndir_total, n, p->H, p->W, A, A, p->twWh, p->twW, TH, mode,
                                c.row_tile, st, c.packed, p->twWh4, p->twW4));
   timer_mark(p, "band_rows_threshold", st);
-  const bool dct2 = sums_dct2 && tma && c.syn_regs && !c.cols_packed && p->wdH && dct_fusion_pays(p);
+  const bool dct2 = sums_dct2 && tma && c.syn_regs && !c.cols_packed && p->wdH && dct_syn_fusion_pays(p);
   const ColOp syn = c.cols_packed          ? ColOp::SynthesisPairs
                     : (tma && c.syn_regs) ? (dct2 ? ColOp::SynthesisRegsDct2 : ColOp::SynthesisRegs)
                                           : ColOp::Synthesis;
