@@ -44,8 +44,8 @@ def parse():
     ap.add_argument('--no-extras', action='store_true', help='skip the plain/uneven/e2e extras')
     ap.add_argument('--batch', type=int, default=BATCH, help='images per batched pass (smaller for profiling)')
     ap.add_argument('--size', default='%dx%d' % (H, W),
-                    help='HxW of the batched pass\'s images (other sizes for profiling their kernels; use with '
-                         '--no-extras)')
+                    help='HxW of the batched pass\'s images in the 2-D workload of the gb300 arm (other sizes '
+                         'for profiling their kernels; use with --no-extras)')
     ap.add_argument('--workload', default='2d', choices=['2d', 'v3', 'sep'],
                     help="v3 / sep: only the 3-D volume or the image-separation extra (for profiling their kernels)")
     ap.add_argument('--sep-batch', type=int, default=8, help='images per batched separation call')
@@ -88,8 +88,8 @@ def job_throughput(units_per_rank, world, seconds):
 # --------------------------------------------------------------- CPU baseline
 def cpu_baseline(min_seconds=10.0, max_images=8):
     """The oracle (FP64 NumPy/SciPy + C atrous restatement) on the host cores,
-    on a bounded sample of the same workload: whole 512x512 images of the
-    batch, one at a time, until min_seconds have passed; and one image on a
+    on a bounded sample of the same workload: whole images of the batch's
+    size, one at a time, until min_seconds have passed; and one image on a
     single thread."""
     from oracle import nsst2d
     from shearcuda_gb300.synth import noisy_image
@@ -110,8 +110,9 @@ def cpu_baseline(min_seconds=10.0, max_images=8):
     nsst2d.denoise(noisy, SIGMA, K, scal, DCOMP, DSIZE, shear_f=sf, nthreads=1)
     one = time.perf_counter() - t1
     return {'value': n / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': '%d of the 512x512 images, dec+thresh+rec, filter/scalar setup excluded, %.1f s' % (n, dt),
-            'single_thread': {'value': 1.0 / one, 'unit': UNIT, 'cores': 1, 'sample': 'one 512x512 image, %.1f s' % one}}
+            'sample': '%d of the %dx%d images, dec+thresh+rec, filter/scalar setup excluded, %.1f s' % (n, H, W, dt),
+            'single_thread': {'value': 1.0 / one, 'unit': UNIT, 'cores': 1,
+                              'sample': 'one %dx%d image, %.1f s' % (H, W, one)}}
 
 
 def cpu_sweep():
@@ -597,7 +598,8 @@ def run_gpu(args):
         roofline['dominant_launch'] = {'kernel': dom, 'ms': stage_avg[dom], 'bytes_as_designed': mat,
                                        'achieved_gbs': mat / (stage_avg[dom] / 1000.0) / 1e9}
 
-    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+    metric = METRIC if (H, W) == (512, 512) else METRIC.replace('512^2', '%dx%d' % (H, W))
+    line = {'metric': metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded ellipses + gradient + N(0, 20^2))',
             'config': {'workload': 'batch of %d x %dx%d images, one batched NSST dec+hard-thresh+rec pass per step'
@@ -904,7 +906,8 @@ def main():
     args = parse()
     global BATCH, H, W
     BATCH = args.batch
-    H, W = (int(v) for v in args.size.lower().split('x'))
+    if args.impl == 'gb300' and args.workload == '2d' and not args.cpu_sweep:
+        H, W = (int(v) for v in args.size.lower().split('x'))
     if args.cpu_sweep:
         cpu_sweep()
     elif args.impl == 'reference':
