@@ -120,3 +120,18 @@ def test_noalloc_rejects_overlapping_buffers_before_any_device_call(built_lib):
         st = lib().nsst_atrousdec_noalloc(ctypes.c_void_p(x), ctypes.c_void_p(y), H, W, L, b'maxflat', None)
         assert st == 1, x
         assert b'overlaps' in lib().nsst_last_error()
+
+
+def test_missing_library_fails_loudly(built_lib, monkeypatch, tmp_path):
+    # no fallback: without libnsst.so every entry point raises, the host-only
+    # ones included (nothing routes to the oracle or to PyTorch instead)
+    import shearcuda_gb300 as sc
+    from shearcuda_gb300 import _lib
+    monkeypatch.setattr(_lib, '_lib', None)
+    monkeypatch.setattr(_lib, 'LIB_PATH', str(tmp_path / 'libnsst.so'))
+    with pytest.raises(OSError, match='not built'):
+        sc.MakeONFilter('Haar')
+    with pytest.raises(OSError, match='not built'):
+        sc.launch_count()
+    with pytest.raises(OSError, match='not built'):
+        sc.prepare_shearing_filters_cuda(DCOMP, DSIZE, 256, 256)
